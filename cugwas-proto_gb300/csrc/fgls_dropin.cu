@@ -1,0 +1,299 @@
+// File-based drop-in entry points with the reference's signatures:
+// fgls_chol (src/fgls_chol.c:29), fgls_eigen (src/fgls_eigen.c:38) and
+// fgls_chol_gpu (src/fgls_chol_gpu.c:97).  Written only against the public
+// engine API of fgls_gb300.h.
+//
+// The reference's POSIX-aio double buffering (src/io.c:35-98,
+// src/fgls_chol.c:327-487) becomes a two-slot pinned host ring:
+//   reader thread:  pread(XR block b+1) -> pinned slot
+//   h2d stream:     slot -> HBM          (overlaps compute of block b)
+//   compute stream: engine block b
+//   d2h stream:     B/V of block b -> pinned slot
+//   main thread:    pwrite(B/V of block b-1) at the reference's offsets
+//                   (j*m + ib)*p and (j*m + ib)*p*p doubles (src/fgls_chol.c:464-474).
+// For chol with t > 1 the XR stream is cached in HBM during the first trait
+// when it fits (the reference re-reads the file for every trait).
+//
+// Errors print "[Error]: <msg>" and exit(EXIT_FAILURE) like the reference's
+// error_msg(msg, 1) (src/common.c:11-17).  Unlike the reference's sync_read,
+// which prints and continues on a short read (src/io.c:13-16), a short read
+// of any input is an error here.
+#include <cuda_runtime.h>
+#include <errno.h>
+#include <fcntl.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <unistd.h>
+
+#include <algorithm>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "fgls_gb300.h"
+
+namespace {
+
+[[noreturn]] void die(const std::string& msg) {
+  fprintf(stderr, "[Error]: %s\n", msg.c_str());
+  exit(EXIT_FAILURE);
+}
+
+void cuda_check(cudaError_t c, const char* what) {
+  if (c != cudaSuccess) die(std::string(what) + ": " + cudaGetErrorString(c));
+}
+
+void eng_check(fglsgpu_engine* e, int rc) {
+  if (rc != FGLSGPU_OK) die(fglsgpu_last_error(e));
+}
+
+// Reads exactly `bytes` at `off` (loops over partial reads); false on EOF/error.
+bool pread_full(int fd, void* buf, size_t bytes, off_t off) {
+  char* p = (char*)buf;
+  while (bytes > 0) {
+    ssize_t r = pread(fd, p, bytes, off);
+    if (r < 0 && errno == EINTR) continue;
+    if (r <= 0) return false;
+    p += r;
+    bytes -= (size_t)r;
+    off += r;
+  }
+  return true;
+}
+
+bool pwrite_full(int fd, const void* buf, size_t bytes, off_t off) {
+  const char* p = (const char*)buf;
+  while (bytes > 0) {
+    ssize_t r = pwrite(fd, p, bytes, off);
+    if (r < 0 && errno == EINTR) continue;
+    if (r <= 0) return false;
+    p += r;
+    bytes -= (size_t)r;
+    off += r;
+  }
+  return true;
+}
+
+void read_file(const char* path, double* buf, size_t count, const char* what) {
+  int fd = open(path, O_RDONLY);
+  if (fd < 0) die(std::string("cannot open ") + what + " file " + path + ": " + strerror(errno));
+  if (!pread_full(fd, buf, sizeof(double) * count, 0)) {
+    close(fd);
+    die(std::string("short read of ") + what + " file " + path + " (" + std::to_string(count) + " doubles expected)");
+  }
+  close(fd);
+}
+
+struct Item {
+  int trait;       // chol: trait of this pass; eigen: -1 (all traits)
+  long long ib;    // first SNP
+  int x;           // SNPs in the block
+  bool read;       // from disk (else from the HBM cache)
+};
+
+struct Slot {
+  double *hX = nullptr, *hB = nullptr, *hV = nullptr;
+  double *dX = nullptr, *dB = nullptr, *dV = nullptr;
+  cudaEvent_t evH{}, evC{}, evD{};
+  std::thread reader;
+  bool read_ok = true;
+  int item = -1;
+};
+
+int run_variant(int variant, int n, int p, int m, int t, int wXL, int wXR, int x_b, int num_threads,
+                const char* Phi_path, const char* h_path, const char* s_path, const char* XL_path,
+                const char* XR_path, const char* Y_path, const char* B_path, const char* V_path) {
+  (void)num_threads;
+  if (n <= 0 || m <= 0 || t <= 0 || wXL <= 0 || wXR <= 0 || x_b <= 0)
+    die("invalid dimensions (n, m, t, wXL, wXR and x_b must be positive)");
+  if (p != wXL + wXR) die("p must equal wXL + wXR");
+  x_b = std::min(x_b, m);
+  fglsgpu_config cfg{};
+  cfg.n = n;
+  cfg.wXL = wXL;
+  cfg.wXR = wXR;
+  cfg.t = t;
+  cfg.x_b = x_b;
+  cfg.variant = variant;
+  const char* prec = getenv("FGLS_PRECISION");
+  cfg.precision = (prec && !strcmp(prec, "split")) ? FGLSGPU_PREC_SPLIT : FGLSGPU_PREC_FP64;
+  const char* sl = getenv("FGLS_SLICES");
+  cfg.slices = sl ? atoi(sl) : 0;
+  const char* dev = getenv("FGLS_DEVICE");
+  cfg.device = dev ? atoi(dev) : 0;
+
+  std::vector<double> Phi((size_t)n * n), h(t), sg(t), XL((size_t)n * wXL), Y((size_t)n * t);
+  read_file(Phi_path, Phi.data(), Phi.size(), "Phi");
+  read_file(h_path, h.data(), t, "h");
+  read_file(s_path, sg.data(), t, "sigma");
+  read_file(XL_path, XL.data(), XL.size(), "XL");
+  read_file(Y_path, Y.data(), Y.size(), "Y");
+
+  fglsgpu_engine* e = nullptr;
+  if (fglsgpu_create(&cfg, &e) != FGLSGPU_OK) die(fglsgpu_last_error(nullptr));
+  eng_check(e, fglsgpu_set_problem(e, Phi.data(), XL.data(), Y.data(), h.data(), sg.data()));
+  Phi.clear();
+  Phi.shrink_to_fit();
+
+  int xr_fd = open(XR_path, O_RDONLY);
+  if (xr_fd < 0) die(std::string("cannot open XR file ") + XR_path + ": " + strerror(errno));
+  int b_fd = open(B_path, O_WRONLY | O_CREAT | O_TRUNC, 0644);
+  int v_fd = open(V_path, O_WRONLY | O_CREAT | O_TRUNC, 0644);
+  if (b_fd < 0 || v_fd < 0) die("cannot open the output files");
+
+  const int nt = variant == FGLSGPU_VARIANT_EIGEN ? t : 1;
+  const long long colb = (long long)n * wXR;  // doubles per SNP
+  cudaStream_t comp = (cudaStream_t)fglsgpu_stream(e);
+  cudaStream_t h2d, d2h;
+  cuda_check(cudaStreamCreateWithFlags(&h2d, cudaStreamNonBlocking), "stream");
+  cuda_check(cudaStreamCreateWithFlags(&d2h, cudaStreamNonBlocking), "stream");
+
+  // Keep XR resident in HBM across chol traits when it fits.
+  double* dXall = nullptr;
+  if (variant == FGLSGPU_VARIANT_CHOL && t > 1) {
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    const size_t need = sizeof(double) * (size_t)colb * m;
+    if (need + ((size_t)4 << 30) < fr) {
+      if (cudaMalloc((void**)&dXall, need) != cudaSuccess) {
+        cudaGetLastError();
+        dXall = nullptr;
+      }
+    }
+  }
+
+  Slot sl2[2];
+  for (Slot& s : sl2) {
+    cuda_check(cudaMallocHost((void**)&s.hX, sizeof(double) * colb * x_b), "pinned XR slot");
+    cuda_check(cudaMallocHost((void**)&s.hB, sizeof(double) * nt * x_b * p), "pinned B slot");
+    cuda_check(cudaMallocHost((void**)&s.hV, sizeof(double) * nt * x_b * p * p), "pinned V slot");
+    cuda_check(cudaMalloc((void**)&s.dX, sizeof(double) * colb * x_b), "XR slot");
+    cuda_check(cudaMalloc((void**)&s.dB, sizeof(double) * nt * x_b * p), "B slot");
+    cuda_check(cudaMalloc((void**)&s.dV, sizeof(double) * nt * x_b * p * p), "V slot");
+    cuda_check(cudaEventCreateWithFlags(&s.evH, cudaEventDisableTiming), "event");
+    cuda_check(cudaEventCreateWithFlags(&s.evC, cudaEventDisableTiming), "event");
+    cuda_check(cudaEventCreateWithFlags(&s.evD, cudaEventDisableTiming), "event");
+  }
+
+  std::vector<Item> items;
+  const int passes = variant == FGLSGPU_VARIANT_EIGEN ? 1 : t;
+  for (int j = 0; j < passes; j++)
+    for (long long ib = 0; ib < m; ib += x_b)
+      items.push_back({variant == FGLSGPU_VARIANT_EIGEN ? -1 : j, ib, (int)std::min<long long>(x_b, m - ib),
+                       !(dXall && j > 0)});
+
+  auto start_read = [&](int i) {
+    Slot& s = sl2[i & 1];
+    const Item& it = items[i];
+    s.read_ok = true;
+    if (!it.read) return;
+    s.reader = std::thread([&s, xr_fd, colb, it]() {
+      s.read_ok = pread_full(xr_fd, s.hX, sizeof(double) * colb * it.x, (off_t)(sizeof(double) * colb * it.ib));
+    });
+  };
+  auto write_out = [&](int i) {
+    Slot& s = sl2[i & 1];
+    const Item& it = items[i];
+    cuda_check(cudaEventSynchronize(s.evD), "download");
+    for (int q = 0; q < nt; q++) {
+      const int j = variant == FGLSGPU_VARIANT_EIGEN ? q : it.trait;
+      const off_t ob = (off_t)sizeof(double) * ((off_t)j * m * p + (off_t)it.ib * p);
+      const off_t ov = (off_t)sizeof(double) * ((off_t)j * m * p * p + (off_t)it.ib * p * p);
+      if (!pwrite_full(b_fd, s.hB + (size_t)q * it.x * p, sizeof(double) * it.x * p, ob) ||
+          !pwrite_full(v_fd, s.hV + (size_t)q * it.x * p * p, sizeof(double) * it.x * p * p, ov))
+        die(std::string("write to ") + B_path + " / " + V_path + " failed: " + strerror(errno));
+    }
+  };
+
+  if (!items.empty()) start_read(0);
+  int cur_trait = -1;
+  for (size_t i = 0; i < items.size(); i++) {
+    Slot& s = sl2[i & 1];
+    Slot& o = sl2[(i + 1) & 1];
+    const Item& it = items[i];
+    if (variant == FGLSGPU_VARIANT_CHOL && it.trait != cur_trait) {
+      if (cur_trait >= 0) eng_check(e, fglsgpu_sync(e));  // report device failures of the finished trait
+      eng_check(e, fglsgpu_select_trait(e, it.trait));
+      cur_trait = it.trait;
+    }
+    const double* src;
+    if (it.read) {
+      s.reader.join();
+      if (!s.read_ok)
+        die(std::string("short read of XR file ") + XR_path + " at SNP " + std::to_string(it.ib));
+      double* dst = dXall ? dXall + it.ib * colb : s.dX;
+      cuda_check(cudaStreamWaitEvent(h2d, s.evC, 0), "wait");
+      cuda_check(cudaMemcpyAsync(dst, s.hX, sizeof(double) * colb * it.x, cudaMemcpyHostToDevice, h2d), "XR upload");
+      cuda_check(cudaEventRecord(s.evH, h2d), "event");
+      cuda_check(cudaStreamWaitEvent(comp, s.evH, 0), "wait");
+      src = dst;
+    } else {
+      src = dXall + it.ib * colb;
+    }
+    cuda_check(cudaStreamWaitEvent(comp, s.evD, 0), "wait");
+    eng_check(e, fglsgpu_run_block_device(e, src, it.x, s.dB, s.dV, (long long)it.x * p, (long long)it.x * p * p));
+    cuda_check(cudaEventRecord(s.evC, comp), "event");
+    cuda_check(cudaStreamWaitEvent(d2h, s.evC, 0), "wait");
+    cuda_check(cudaMemcpyAsync(s.hB, s.dB, sizeof(double) * nt * it.x * p, cudaMemcpyDeviceToHost, d2h), "B download");
+    cuda_check(cudaMemcpyAsync(s.hV, s.dV, sizeof(double) * nt * it.x * p * p, cudaMemcpyDeviceToHost, d2h),
+               "V download");
+    cuda_check(cudaEventRecord(s.evD, d2h), "event");
+    if (i + 1 < items.size()) {
+      cuda_check(cudaEventSynchronize(o.evH), "upload");  // o.hX no longer read by block i-1's upload
+      start_read((int)i + 1);
+    }
+    if (i >= 1) write_out((int)i - 1);
+  }
+  if (!items.empty()) write_out((int)items.size() - 1);
+  eng_check(e, fglsgpu_sync(e));
+
+  for (Slot& s : sl2) {
+    if (s.reader.joinable()) s.reader.join();
+    cudaFreeHost(s.hX);
+    cudaFreeHost(s.hB);
+    cudaFreeHost(s.hV);
+    cudaFree(s.dX);
+    cudaFree(s.dB);
+    cudaFree(s.dV);
+    cudaEventDestroy(s.evH);
+    cudaEventDestroy(s.evC);
+    cudaEventDestroy(s.evD);
+  }
+  if (dXall) cudaFree(dXall);
+  cudaStreamDestroy(h2d);
+  cudaStreamDestroy(d2h);
+  close(xr_fd);
+  if (close(b_fd) != 0 || close(v_fd) != 0) die("closing the output files failed");
+  fglsgpu_destroy(e);
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fgls_chol(int n, int p, int m, int t, int wXL, int wXR, int x_b, int y_b, int num_threads, char* Phi_path,
+              char* h2_path, char* sigma2_path, char* XL_path, char* XR_path, char* Y_path, char* B_path,
+              char* V_path) {
+  if (y_b != 1) fprintf(stderr, "[Warning] y_b not used (set to 1)\n");  // src/fgls_chol.c:102-103
+  return run_variant(FGLSGPU_VARIANT_CHOL, n, p, m, t, wXL, wXR, x_b, num_threads, Phi_path, h2_path, sigma2_path,
+                     XL_path, XR_path, Y_path, B_path, V_path);
+}
+
+int fgls_chol_gpu(int n, int p, int m, int t, int wXL, int wXR, int x_b, int y_b, int num_threads, char* Phi_path,
+                  char* h2_path, char* sigma2_path, char* XL_path, char* XR_path, char* Y_path, char* B_path,
+                  char* V_path) {
+  return fgls_chol(n, p, m, t, wXL, wXR, x_b, y_b, num_threads, Phi_path, h2_path, sigma2_path, XL_path, XR_path,
+                   Y_path, B_path, V_path);
+}
+
+int fgls_eigen(int n, int p, int m, int t, int wXL, int wXR, int x_b, int y_b, int num_threads, char* Phi_path,
+               char* h2_path, char* sigma2_path, char* XL_path, char* XR_path, char* Y_path, char* B_path,
+               char* V_path) {
+  (void)y_b;  // traits are the GEMM N dimension: all t traits of a block in one pass
+  return run_variant(FGLSGPU_VARIANT_EIGEN, n, p, m, t, wXL, wXR, x_b, num_threads, Phi_path, h2_path,
+                     sigma2_path, XL_path, XR_path, Y_path, B_path, V_path);
+}
+
+}  // extern "C"

@@ -1,0 +1,499 @@
+// The fglsgpu_* engine: device buffers, streams and the per-trait / per-block
+// schedules of the two FGLS variants.
+//
+// chol  (src/fgls_chol.c:223-487):  per trait j: M_j = h s Phi + (1-h) s I on
+//   the device, blocked FP64 potrf, [y~ | XL~] = L^-1 [y | XL], null model;
+//   per SNP block: X~ = L^-1 XR_blk (blocked TRSM), skinny Gram, batched solve.
+// eigen (src/fgls_eigen.c:38-677):  once: Phi = Z W Z^T (device FP64
+//   eigensolver), Z^T XL, Z^T Y, per-trait weights d_j = 1/(a_j W + b_j) and
+//   null models; per SNP block: R = Z^T XR_blk once for all traits, Gram
+//   terms for all traits as GEMMs against d_j-weighted operands (the
+//   reference's per-trait rescale of the block, src/fgls_eigen.c:505-507, is
+//   folded into the small operand and never materialised), batched solve
+//   over SNP x trait.
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "fgls_common.cuh"
+#include "fgls_kernels.cuh"
+#include "fgls_ozaki.cuh"
+
+using namespace fgls;
+
+struct fglsgpu_engine {
+  fglsgpu_config cfg{};
+  int p = 0, topw = 0;
+  cudaStream_t comp = nullptr, h2d = nullptr, d2h = nullptr;
+  cudaEvent_t evH[2]{}, evC[2]{}, evD[2]{};
+  // in-core operands
+  double *dPhi = nullptr, *dL = nullptr, *dZ = nullptr, *dW = nullptr;
+  double *dXL = nullptr, *dY = nullptr, *dh = nullptr, *dsig = nullptr;
+  double *dWY = nullptr, *dZtXL = nullptr, *dZtY = nullptr, *ddinv = nullptr, *dAYL = nullptr;
+  double* dtop = nullptr;
+  void* deigwork = nullptr;
+  // per-block work
+  double* dX[2]{};
+  double* dWork = nullptr;  // chol: TRSM in place; eigen: R = Z^T X
+  double* dQ = nullptr;     // eigen: self-product operand
+  double *dGYL = nullptr, *dGR = nullptr;
+  double *dB[2]{}, *dV[2]{};
+  unsigned char* dU8 = nullptr;
+  DevStatus* dst = nullptr;
+  DevStatus* hst = nullptr;
+  OzakiPlan* oz = nullptr;  // split-precision state (eigen / chol)
+  std::vector<double> hh, hs;
+  int trait_sel = -1;
+  bool problem_set = false;
+  std::string err;
+};
+
+namespace {
+
+thread_local std::string tl_err;
+
+int fail(fglsgpu_engine* e, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (e) e->err = buf;
+  tl_err = buf;
+  return code;
+}
+
+int cuda_fail(fglsgpu_engine* e, cudaError_t c, const char* what) {
+  return fail(e, c == cudaErrorMemoryAllocation ? FGLSGPU_ENOMEM : FGLSGPU_ECUDA, "%s: %s (%s)", what,
+              cudaGetErrorString(c), cudaGetErrorName(c));
+}
+
+#define ENG_TRY(e, expr, what)                           \
+  do {                                                   \
+    cudaError_t _c = (expr);                             \
+    if (_c != cudaSuccess) return cuda_fail(e, _c, what); \
+  } while (0)
+
+template <class T>
+cudaError_t dalloc(T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) return cudaSuccess;
+  return cudaMalloc((void**)p, sizeof(T) * count);
+}
+
+// Reads the device status word after a sync; maps failures to messages that
+// follow the reference's error texts (src/fgls_chol.c:266-271, :309-314, :418-434).
+int check_status(fglsgpu_engine* e, const char* stage) {
+  ENG_TRY(e, cudaMemcpyAsync(e->hst, e->dst, sizeof(DevStatus), cudaMemcpyDeviceToHost, e->comp), "status copy");
+  ENG_TRY(e, cudaStreamSynchronize(e->comp), stage);
+  const DevStatus s = *e->hst;
+  if (s.code == FGLSGPU_OK) return FGLSGPU_OK;
+  if (s.code == FGLSGPU_ENOTSPD) {
+    if (!strcmp(stage, "potrf(M)"))
+      return fail(e, FGLSGPU_ENOTSPD, "dpotrf(M) failed (info: %d)", s.info);
+    if (s.info < 0) return fail(e, FGLSGPU_ENOTSPD, "dpotrf(scoreV) failed (info: -1) - trait: %lld", s.idx);
+    return fail(e, FGLSGPU_ENOTSPD, "dpotrf(V) failed (info: %d) - i: %lld", s.info, s.idx);
+  }
+  if (s.code == FGLSGPU_ETIMEOUT)
+    return fail(e, FGLSGPU_ETIMEOUT, "device wait expired in %s (site %d, item %lld)", stage, s.info, s.idx);
+  return fail(e, s.code, "device status %d in %s (info %d, item %lld)", s.code, stage, s.info, s.idx);
+}
+
+int reset_status(fglsgpu_engine* e) {
+  ENG_TRY(e, cudaMemsetAsync(e->dst, 0, sizeof(DevStatus), e->comp), "status reset");
+  return FGLSGPU_OK;
+}
+
+void free_all(fglsgpu_engine* e) {
+  void* ptrs[] = {e->dPhi, e->dL,   e->dZ,    e->dW,    e->dXL,   e->dY,    e->dh,    e->dsig, e->dWY,
+                  e->dZtXL, e->dZtY, e->ddinv, e->dAYL, e->dtop, e->deigwork, e->dX[0], e->dX[1], e->dWork,
+                  e->dQ,   e->dGYL, e->dGR,  e->dB[0], e->dB[1], e->dV[0], e->dV[1], e->dU8, e->dst};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (e->hst) cudaFreeHost(e->hst);
+  if (e->oz) ozaki_destroy(e->oz);
+  for (int k = 0; k < 2; k++) {
+    if (e->evH[k]) cudaEventDestroy(e->evH[k]);
+    if (e->evC[k]) cudaEventDestroy(e->evC[k]);
+    if (e->evD[k]) cudaEventDestroy(e->evD[k]);
+  }
+  if (e->comp) cudaStreamDestroy(e->comp);
+  if (e->h2d) cudaStreamDestroy(e->h2d);
+  if (e->d2h) cudaStreamDestroy(e->d2h);
+}
+
+bool split(const fglsgpu_engine* e) { return e->cfg.precision == FGLSGPU_PREC_SPLIT; }
+
+// Compute one block already in device memory (FP64 genotypes at dXin,
+// n x x*wXR) into dB/dV with the given trait strides, on e->comp.
+int compute_block(fglsgpu_engine* e, const double* dXin, int x, double* dB, double* dV, long long bstr,
+                  long long vstr, long long snp_base) {
+  const fglsgpu_config& c = e->cfg;
+  const int n = c.n, wXL = c.wXL, wXR = c.wXR, p = e->p;
+  const long long cols = (long long)x * wXR;
+  cudaStream_t s = e->comp;
+  if (c.variant == FGLSGPU_VARIANT_CHOL) {
+    if (e->trait_sel < 0) return fail(e, FGLSGPU_ESTATE, "fglsgpu_select_trait must precede run_block (chol)");
+    if (split(e)) {
+      ENG_TRY(e, ozaki_chol_block(e->oz, s, dXin, x, e->dWork), "split TRSM");
+    } else {
+      ENG_TRY(e, cudaMemcpyAsync(e->dWork, dXin, sizeof(double) * n * cols, cudaMemcpyDeviceToDevice, s),
+              "block copy");
+      ENG_TRY(e, dtrsm_llnn(s, n, (int)cols, e->dL, n, e->dWork, n), "TRSM");
+    }
+    ENG_TRY(e, gram_skinny(s, n, x, wXL, wXR, e->dWork, n, e->dWY, e->dGYL, e->dGR), "gram");
+    ENG_TRY(e, snp_solve(s, p, x, 1, wXL, e->dtop, e->dGYL, cols, e->dGR, cols * wXR, dB, bstr, dV, vstr,
+                         e->dst, snp_base),
+            "solve");
+    return FGLSGPU_OK;
+  }
+  // eigen
+  const int t = c.t;
+  if (split(e)) {
+    ENG_TRY(e, ozaki_eigen_block(e->oz, s, dXin, x, e->dGYL, e->dGR), "split eigen block");
+  } else {
+    ENG_TRY(e, dgemm(s, true, false, n, (int)cols, n, 1.0, e->dZ, n, dXin, n, 0.0, e->dWork, n), "Z^T XR");
+    ENG_TRY(e, dgemm(s, true, false, (int)cols, t * (1 + wXL), n, 1.0, e->dWork, n, e->dAYL, n, 0.0, e->dGYL,
+                     cols),
+            "gram YL");
+    const long long qcols = cols * wXR;
+    ENG_TRY(e, quad_products(s, n, x, wXR, e->dWork, n, e->dQ, n), "quad");
+    ENG_TRY(e, dgemm(s, true, false, (int)qcols, t, n, 1.0, e->dQ, n, e->ddinv, n, 0.0, e->dGR, qcols),
+            "gram R");
+  }
+  ENG_TRY(e, snp_solve(s, p, x, t, wXL, e->dtop, e->dGYL, cols, e->dGR, cols * wXR, dB, bstr, dV, vstr, e->dst,
+                       snp_base),
+          "solve");
+  return FGLSGPU_OK;
+}
+
+int out_traits(const fglsgpu_engine* e) { return e->cfg.variant == FGLSGPU_VARIANT_EIGEN ? e->cfg.t : 1; }
+
+}  // namespace
+
+extern "C" {
+
+int fglsgpu_version(void) { return 10000; }
+
+const char* fglsgpu_last_error(const fglsgpu_engine* e) { return e ? e->err.c_str() : tl_err.c_str(); }
+
+long long fglsgpu_launch_count(const fglsgpu_engine*) { return g_launches.load(); }
+
+void* fglsgpu_stream(fglsgpu_engine* e) { return e ? (void*)e->comp : nullptr; }
+
+int fglsgpu_create(const fglsgpu_config* cfg, fglsgpu_engine** out) {
+  if (!cfg || !out) return fail(nullptr, FGLSGPU_EINVAL, "null argument");
+  *out = nullptr;
+  const fglsgpu_config c = *cfg;
+  if (c.n <= 0 || c.wXL <= 0 || c.wXR <= 0 || c.t <= 0 || c.x_b <= 0)
+    return fail(nullptr, FGLSGPU_EINVAL, "invalid dimensions n=%d wXL=%d wXR=%d t=%d x_b=%d", c.n, c.wXL, c.wXR,
+                c.t, c.x_b);
+  if (c.wXL + c.wXR > FGLS_MAX_P || c.wXL + c.wXR < 2)
+    return fail(nullptr, FGLSGPU_EINVAL, "p = wXL + wXR = %d outside [2, %d]", c.wXL + c.wXR, FGLS_MAX_P);
+  if (c.wXR > FGLS_MAX_WXR) return fail(nullptr, FGLSGPU_EINVAL, "wXR = %d > %d", c.wXR, FGLS_MAX_WXR);
+  if (c.n <= c.wXL) return fail(nullptr, FGLSGPU_EINVAL, "n = %d must exceed wXL = %d", c.n, c.wXL);
+  if (c.variant != FGLSGPU_VARIANT_CHOL && c.variant != FGLSGPU_VARIANT_EIGEN)
+    return fail(nullptr, FGLSGPU_EINVAL, "unknown variant %d", c.variant);
+  if (c.precision != FGLSGPU_PREC_FP64 && c.precision != FGLSGPU_PREC_SPLIT)
+    return fail(nullptr, FGLSGPU_EINVAL, "unknown precision %d", c.precision);
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
+    cudaGetLastError();
+    return fail(nullptr, FGLSGPU_ENODEV, "no CUDA device available");
+  }
+  if (c.device < 0 || c.device >= ndev) return fail(nullptr, FGLSGPU_EINVAL, "device %d of %d", c.device, ndev);
+  cudaError_t ce = cudaSetDevice(c.device);
+  if (ce != cudaSuccess) return cuda_fail(nullptr, ce, "cudaSetDevice");
+  fglsgpu_engine* e = new fglsgpu_engine();
+  e->cfg = c;
+  e->p = c.wXL + c.wXR;
+  e->topw = c.wXL + c.wXL * c.wXL + 1;
+  const long long n = c.n, t = c.t, xb = c.x_b, wXL = c.wXL, wXR = c.wXR, p = e->p;
+  const int nt = c.variant == FGLSGPU_VARIANT_EIGEN ? c.t : 1;
+  cudaError_t r = cudaSuccess;
+  auto chk = [&](cudaError_t x) {
+    if (r == cudaSuccess) r = x;
+  };
+  chk(cudaStreamCreateWithFlags(&e->comp, cudaStreamNonBlocking));
+  chk(cudaStreamCreateWithFlags(&e->h2d, cudaStreamNonBlocking));
+  chk(cudaStreamCreateWithFlags(&e->d2h, cudaStreamNonBlocking));
+  for (int k = 0; k < 2; k++) {
+    chk(cudaEventCreateWithFlags(&e->evH[k], cudaEventDisableTiming));
+    chk(cudaEventCreateWithFlags(&e->evC[k], cudaEventDisableTiming));
+    chk(cudaEventCreateWithFlags(&e->evD[k], cudaEventDisableTiming));
+  }
+  chk(dalloc(&e->dPhi, n * n));
+  chk(dalloc(&e->dXL, n * wXL));
+  chk(dalloc(&e->dY, n * t));
+  chk(dalloc(&e->dh, t));
+  chk(dalloc(&e->dsig, t));
+  chk(dalloc(&e->dtop, t * e->topw));
+  chk(dalloc(&e->dst, 1));
+  chk(cudaMallocHost((void**)&e->hst, sizeof(DevStatus)));
+  for (int k = 0; k < 2; k++) {
+    chk(dalloc(&e->dX[k], n * xb * wXR));
+    chk(dalloc(&e->dB[k], (long long)nt * xb * p));
+    chk(dalloc(&e->dV[k], (long long)nt * xb * p * p));
+  }
+  chk(dalloc(&e->dGYL, xb * wXR * nt * (1 + wXL)));
+  chk(dalloc(&e->dGR, xb * wXR * wXR * nt));
+  if (c.variant == FGLSGPU_VARIANT_CHOL) {
+    chk(dalloc(&e->dL, n * n));
+    chk(dalloc(&e->dWY, n * (1 + wXL)));
+    chk(dalloc(&e->dWork, n * xb * wXR));
+  } else {
+    chk(dalloc(&e->dL, n * n));  // eigensolver scratch
+    chk(dalloc(&e->dZ, n * n));
+    chk(dalloc(&e->dW, n));
+    chk(dalloc(&e->dZtXL, n * wXL));
+    chk(dalloc(&e->dZtY, n * t));
+    chk(dalloc(&e->ddinv, n * t));
+    chk(dalloc(&e->dAYL, n * t * (1 + wXL)));
+    chk(cudaMalloc(&e->deigwork, eig_workspace_bytes(c.n)));
+    if (c.precision == FGLSGPU_PREC_FP64) {
+      chk(dalloc(&e->dWork, n * xb * wXR));
+      chk(dalloc(&e->dQ, n * xb * wXR * wXR));
+    }
+  }
+  if (r == cudaSuccess) r = cudaMemsetAsync(e->dst, 0, sizeof(DevStatus), e->comp);
+  if (r == cudaSuccess) r = cudaStreamSynchronize(e->comp);
+  if (r != cudaSuccess) {
+    int code = cuda_fail(e, r, "engine allocation");
+    tl_err = e->err;
+    free_all(e);
+    delete e;
+    return code;
+  }
+  *out = e;
+  return FGLSGPU_OK;
+}
+
+int fglsgpu_destroy(fglsgpu_engine* e) {
+  if (!e) return FGLSGPU_OK;
+  cudaSetDevice(e->cfg.device);
+  if (e->comp) cudaStreamSynchronize(e->comp);
+  free_all(e);
+  delete e;
+  return FGLSGPU_OK;
+}
+
+int fglsgpu_set_problem(fglsgpu_engine* e, const double* Phi, const double* XL, const double* Y, const double* h,
+                        const double* sigma) {
+  if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
+  if (!Phi || !XL || !Y || !h || !sigma) return fail(e, FGLSGPU_EINVAL, "null input pointer");
+  const fglsgpu_config& c = e->cfg;
+  const long long n = c.n, t = c.t;
+  ENG_TRY(e, cudaSetDevice(c.device), "cudaSetDevice");
+  for (int j = 0; j < c.t; j++)
+    if (!(h[j] >= 0.0 && h[j] <= 1.0) || !(sigma[j] > 0.0))
+      return fail(e, FGLSGPU_EINVAL, "trait %d: need 0 <= h <= 1 and sigma > 0 (h=%g sigma=%g)", j, h[j], sigma[j]);
+  e->hh.assign(h, h + c.t);
+  e->hs.assign(sigma, sigma + c.t);
+  cudaStream_t s = e->comp;
+  ENG_TRY(e, cudaMemcpyAsync(e->dPhi, Phi, sizeof(double) * n * n, cudaMemcpyHostToDevice, s), "upload Phi");
+  ENG_TRY(e, cudaMemcpyAsync(e->dXL, XL, sizeof(double) * n * c.wXL, cudaMemcpyHostToDevice, s), "upload XL");
+  ENG_TRY(e, cudaMemcpyAsync(e->dY, Y, sizeof(double) * n * t, cudaMemcpyHostToDevice, s), "upload Y");
+  ENG_TRY(e, cudaMemcpyAsync(e->dh, h, sizeof(double) * t, cudaMemcpyHostToDevice, s), "upload h");
+  ENG_TRY(e, cudaMemcpyAsync(e->dsig, sigma, sizeof(double) * t, cudaMemcpyHostToDevice, s), "upload sigma");
+  int rc = reset_status(e);
+  if (rc) return rc;
+  e->trait_sel = -1;
+  e->problem_set = false;
+  if (c.variant == FGLSGPU_VARIANT_EIGEN) {
+    int qfail = 0;
+    ENG_TRY(e, dsyev_device(s, c.n, e->dPhi, n, e->dL, e->dZ, e->dW, e->deigwork, &qfail, nullptr),
+            "eigendecomposition");
+    if (qfail) return fail(e, FGLSGPU_ENOCONV, "dsyevr failed (info: 1): QL iteration did not converge");
+    ENG_TRY(e, dgemm(s, true, false, c.n, c.wXL, c.n, 1.0, e->dZ, n, e->dXL, n, 0.0, e->dZtXL, n), "Z^T XL");
+    ENG_TRY(e, dgemm(s, true, false, c.n, c.t, c.n, 1.0, e->dZ, n, e->dY, n, 0.0, e->dZtY, n), "Z^T Y");
+    ENG_TRY(e, eigen_traits(s, c.n, c.t, c.wXL, e->dW, e->dh, e->dsig, e->dZtXL, e->dZtY, e->ddinv, e->dAYL,
+                            e->dtop, e->dst),
+            "trait weights");
+    rc = check_status(e, "eigen setup");
+    if (rc) return rc;
+    if (split(e)) {
+      if (!e->oz) {
+        ENG_TRY(e, ozaki_create(&e->oz, c.n, c.t, c.wXL, c.wXR, c.x_b, c.slices, /*eigen=*/1), "split plan");
+      }
+      ENG_TRY(e, ozaki_set_eigen(e->oz, s, e->dZ, e->dAYL, e->ddinv), "split operands");
+      ENG_TRY(e, cudaStreamSynchronize(s), "split operands");
+    }
+  }
+  ENG_TRY(e, cudaStreamSynchronize(s), "set_problem");
+  e->problem_set = true;
+  return FGLSGPU_OK;
+}
+
+int fglsgpu_select_trait(fglsgpu_engine* e, int j) {
+  if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
+  if (!e->problem_set) return fail(e, FGLSGPU_ESTATE, "set_problem must precede select_trait");
+  const fglsgpu_config& c = e->cfg;
+  if (c.variant == FGLSGPU_VARIANT_EIGEN) return FGLSGPU_OK;
+  if (j < 0 || j >= c.t) return fail(e, FGLSGPU_EINVAL, "trait %d outside [0, %d)", j, c.t);
+  ENG_TRY(e, cudaSetDevice(c.device), "cudaSetDevice");
+  const long long n = c.n;
+  cudaStream_t s = e->comp;
+  int rc = reset_status(e);
+  if (rc) return rc;
+  const double alpha = e->hh[j] * e->hs[j];          // src/fgls_chol.c:253
+  const double beta = (1.0 - e->hh[j]) * e->hs[j];   // src/fgls_chol.c:254
+  ENG_TRY(e, build_shifted(s, c.n, e->dPhi, n, alpha, beta, e->dL, n), "build M");
+  ENG_TRY(e, dpotrf_lower(s, c.n, e->dL, n, e->dst), "potrf");
+  rc = check_status(e, "potrf(M)");
+  if (rc) return rc;
+  ENG_TRY(e, cudaMemcpyAsync(e->dWY, e->dY + (long long)j * n, sizeof(double) * n, cudaMemcpyDeviceToDevice, s),
+          "copy y");
+  ENG_TRY(e, cudaMemcpyAsync(e->dWY + n, e->dXL, sizeof(double) * n * c.wXL, cudaMemcpyDeviceToDevice, s),
+          "copy XL");
+  ENG_TRY(e, dtrsm_llnn(s, c.n, 1 + c.wXL, e->dL, n, e->dWY, n), "whiten y, XL");
+  ENG_TRY(e, null_model_chol(s, c.n, c.wXL, e->dWY, e->dtop, e->dst, 0), "null model");
+  rc = check_status(e, "null model");
+  if (rc) return rc;
+  if (split(e)) {
+    if (!e->oz) ENG_TRY(e, ozaki_create(&e->oz, c.n, 1, c.wXL, c.wXR, c.x_b, c.slices, /*eigen=*/0), "split plan");
+    ENG_TRY(e, ozaki_set_chol(e->oz, s, e->dL), "split operands");
+    ENG_TRY(e, cudaStreamSynchronize(s), "split operands");
+  }
+  e->trait_sel = j;
+  return FGLSGPU_OK;
+}
+
+int fglsgpu_run_block_device(fglsgpu_engine* e, const double* dXR, int x_inc, double* dB, double* dV,
+                             long long bstr, long long vstr) {
+  if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
+  if (!e->problem_set) return fail(e, FGLSGPU_ESTATE, "set_problem must precede run_block");
+  if (x_inc <= 0 || x_inc > e->cfg.x_b) return fail(e, FGLSGPU_EINVAL, "x_inc=%d outside [1, %d]", x_inc, e->cfg.x_b);
+  if (!dXR || !dB || !dV) return fail(e, FGLSGPU_EINVAL, "null block pointer");
+  ENG_TRY(e, cudaSetDevice(e->cfg.device), "cudaSetDevice");
+  // Device failures accumulate in the status word until fglsgpu_sync.
+  return compute_block(e, dXR, x_inc, dB, dV, bstr, vstr, 0);
+}
+
+int fglsgpu_run_block_device_u8(fglsgpu_engine* e, const unsigned char* dXR, int x_inc, double* dB, double* dV,
+                                long long bstr, long long vstr) {
+  if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
+  if (!e->problem_set) return fail(e, FGLSGPU_ESTATE, "set_problem must precede run_block");
+  if (x_inc <= 0 || x_inc > e->cfg.x_b) return fail(e, FGLSGPU_EINVAL, "x_inc=%d outside [1, %d]", x_inc, e->cfg.x_b);
+  ENG_TRY(e, cudaSetDevice(e->cfg.device), "cudaSetDevice");
+  const long long cnt = (long long)x_inc * e->cfg.wXR * e->cfg.n;
+  if (split(e) && e->cfg.variant == FGLSGPU_VARIANT_EIGEN) {
+    ENG_TRY(e, ozaki_eigen_block_u8(e->oz, e->comp, dXR, x_inc, e->dGYL, e->dGR), "split eigen block");
+    ENG_TRY(e, snp_solve(e->comp, e->p, x_inc, e->cfg.t, e->cfg.wXL, e->dtop, e->dGYL, (long long)x_inc * e->cfg.wXR,
+                         e->dGR, (long long)x_inc * e->cfg.wXR * e->cfg.wXR, dB, bstr, dV, vstr, e->dst, 0),
+            "solve");
+    return FGLSGPU_OK;
+  }
+  ENG_TRY(e, u8_to_f64(e->comp, dXR, e->dX[1], cnt), "widen genotypes");
+  return compute_block(e, e->dX[1], x_inc, dB, dV, bstr, vstr, 0);
+}
+
+int fglsgpu_sync(fglsgpu_engine* e) {
+  if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
+  ENG_TRY(e, cudaSetDevice(e->cfg.device), "cudaSetDevice");
+  const int rc = check_status(e, "block");
+  const int rr = reset_status(e);
+  return rc ? rc : rr;
+}
+
+int fglsgpu_run_block(fglsgpu_engine* e, const double* XR, int x_inc, double* B, double* V, long long bstr,
+                      long long vstr) {
+  if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
+  if (!e->problem_set) return fail(e, FGLSGPU_ESTATE, "set_problem must precede run_block");
+  if (x_inc <= 0 || x_inc > e->cfg.x_b) return fail(e, FGLSGPU_EINVAL, "x_inc=%d outside [1, %d]", x_inc, e->cfg.x_b);
+  if (!XR || !B || !V) return fail(e, FGLSGPU_EINVAL, "null block pointer");
+  ENG_TRY(e, cudaSetDevice(e->cfg.device), "cudaSetDevice");
+  const fglsgpu_config& c = e->cfg;
+  const int p = e->p;
+  int rc = reset_status(e);
+  if (rc) return rc;
+  cudaStream_t s = e->comp;
+  ENG_TRY(e, cudaMemcpyAsync(e->dX[0], XR, sizeof(double) * c.n * (size_t)x_inc * c.wXR, cudaMemcpyHostToDevice, s),
+          "XR upload");
+  const long long db = (long long)x_inc * p, dv = (long long)x_inc * p * p;
+  rc = compute_block(e, e->dX[0], x_inc, e->dB[0], e->dV[0], db, dv, 0);
+  if (rc) return rc;
+  const int nt = out_traits(e);
+  ENG_TRY(e, cudaMemcpy2DAsync(B, sizeof(double) * bstr, e->dB[0], sizeof(double) * db, sizeof(double) * db, nt,
+                               cudaMemcpyDeviceToHost, s),
+          "B download");
+  ENG_TRY(e, cudaMemcpy2DAsync(V, sizeof(double) * vstr, e->dV[0], sizeof(double) * dv, sizeof(double) * dv, nt,
+                               cudaMemcpyDeviceToHost, s),
+          "V download");
+  return check_status(e, "block");
+}
+
+// Whole-job host API: m SNPs from a host array in the reference layout,
+// results into host arrays in the B.out / V.out layout of the active
+// traits (eigen: trait j at j*m*p; chol: the selected trait at 0).  Blocks
+// of x_b SNPs flow through two device slots: H2D on one stream, compute on
+// another, D2H on a third, so copies of block b+1 and b-1 overlap block b.
+int fglsgpu_run_snps(fglsgpu_engine* e, const double* XR, long long m, double* B, double* V) {
+  if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
+  if (!e->problem_set) return fail(e, FGLSGPU_ESTATE, "set_problem must precede run_snps");
+  if (m <= 0 || !XR || !B || !V) return fail(e, FGLSGPU_EINVAL, "invalid run_snps arguments");
+  const fglsgpu_config& c = e->cfg;
+  if (c.variant == FGLSGPU_VARIANT_CHOL && e->trait_sel < 0)
+    return fail(e, FGLSGPU_ESTATE, "fglsgpu_select_trait must precede run_snps (chol)");
+  ENG_TRY(e, cudaSetDevice(c.device), "cudaSetDevice");
+  int rc = reset_status(e);
+  if (rc) return rc;
+  const int p = e->p, nt = out_traits(e);
+  const long long colb = (long long)c.n * c.wXR;  // doubles per SNP
+  const long long nblk = (m + c.x_b - 1) / c.x_b;
+  for (long long b = 0; b < nblk; b++) {
+    const int k = (int)(b & 1);
+    const long long ib = b * c.x_b;
+    const int x = (int)std::min<long long>(c.x_b, m - ib);
+    // slot k's input is free once block b-2's compute finished
+    ENG_TRY(e, cudaStreamWaitEvent(e->h2d, e->evC[k], 0), "wait");
+    ENG_TRY(e, cudaMemcpyAsync(e->dX[k], XR + ib * colb, sizeof(double) * colb * x, cudaMemcpyHostToDevice, e->h2d),
+            "XR upload");
+    ENG_TRY(e, cudaEventRecord(e->evH[k], e->h2d), "event");
+    ENG_TRY(e, cudaStreamWaitEvent(e->comp, e->evH[k], 0), "wait");
+    ENG_TRY(e, cudaStreamWaitEvent(e->comp, e->evD[k], 0), "wait");  // outputs of block b-2 downloaded
+    const long long db = (long long)x * p, dv = (long long)x * p * p;
+    rc = compute_block(e, e->dX[k], x, e->dB[k], e->dV[k], db, dv, ib);
+    if (rc) return rc;
+    ENG_TRY(e, cudaEventRecord(e->evC[k], e->comp), "event");
+    ENG_TRY(e, cudaStreamWaitEvent(e->d2h, e->evC[k], 0), "wait");
+    ENG_TRY(e, cudaMemcpy2DAsync(B + ib * p, sizeof(double) * m * p, e->dB[k], sizeof(double) * db,
+                                 sizeof(double) * db, nt, cudaMemcpyDeviceToHost, e->d2h),
+            "B download");
+    ENG_TRY(e, cudaMemcpy2DAsync(V + ib * p * p, sizeof(double) * m * p * p, e->dV[k], sizeof(double) * dv,
+                                 sizeof(double) * dv, nt, cudaMemcpyDeviceToHost, e->d2h),
+            "V download");
+    ENG_TRY(e, cudaEventRecord(e->evD[k], e->d2h), "event");
+  }
+  ENG_TRY(e, cudaStreamSynchronize(e->d2h), "run_snps");
+  ENG_TRY(e, cudaStreamSynchronize(e->h2d), "run_snps");
+  return check_status(e, "block");
+}
+
+int fglsgpu_get_res_sigma(fglsgpu_engine* e, double* out) {
+  if (!e || !out) return fail(e, FGLSGPU_EINVAL, "null argument");
+  if (!e->problem_set) return fail(e, FGLSGPU_ESTATE, "set_problem first");
+  ENG_TRY(e, cudaSetDevice(e->cfg.device), "cudaSetDevice");
+  const int nt = out_traits(e);
+  for (int j = 0; j < nt; j++)
+    ENG_TRY(e, cudaMemcpy(out + j, e->dtop + (long long)j * e->topw + e->topw - 1, sizeof(double),
+                          cudaMemcpyDeviceToHost),
+            "res_sigma");
+  return FGLSGPU_OK;
+}
+
+int fglsgpu_get_eigen(fglsgpu_engine* e, double* W, double* Z) {
+  if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
+  if (e->cfg.variant != FGLSGPU_VARIANT_EIGEN || !e->problem_set) return fail(e, FGLSGPU_ESTATE, "no eigendecomposition");
+  ENG_TRY(e, cudaSetDevice(e->cfg.device), "cudaSetDevice");
+  const long long n = e->cfg.n;
+  if (W) ENG_TRY(e, cudaMemcpy(W, e->dW, sizeof(double) * n, cudaMemcpyDeviceToHost), "W");
+  if (Z) ENG_TRY(e, cudaMemcpy(Z, e->dZ, sizeof(double) * n * n, cudaMemcpyDeviceToHost), "Z");
+  return FGLSGPU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,51 @@
+// Launchers of the engine's kernels (host side).  Every launcher enqueues on
+// the given stream and returns the launch's cudaError_t.
+#pragma once
+
+#include <atomic>
+
+#include "fgls_common.cuh"
+
+#define FGLS_MAX_P 8    // p = wXL + wXR handled by the batched solve
+#define FGLS_MAX_WXR 4  // SNP columns per SNP handled by the Gram kernels
+
+namespace fgls {
+
+// Count of kernels this library has launched (all engines, all devices).
+extern std::atomic<long long> g_launches;
+inline void note_launch(long long k = 1) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+
+// chol null model.  WY = [y~ | XL~] (n x (1 + wXL), ld n).  Writes the
+// trait's top record {B_t[wXL], V_tl[wXL*wXL], res_sigma} at top + trait*topw.
+cudaError_t null_model_chol(cudaStream_t s, int n, int wXL, const double* WY, double* top, DevStatus* st,
+                            int trait);
+
+// eigen per-trait weights dinv (n x t), AYL = [ZtY.*dinv | ZtXL.*dinv_j ...]
+// (n x t(1+wXL)) and top records for all t traits.
+cudaError_t eigen_traits(cudaStream_t s, int n, int t, int wXL, const double* W, const double* h,
+                         const double* sigma, const double* ZtXL, const double* ZtY, double* dinv,
+                         double* AYL, double* top, DevStatus* st);
+
+// chol Gram of one block: X (n x x*wXR, ld ldx) against C = [y~ | XL~].
+cudaError_t gram_skinny(cudaStream_t s, int n, int x, int wXL, int wXR, const double* X, long long ldx,
+                        const double* C, double* GYL, double* GR);
+
+// Q[:, (i*wXR+c)*wXR+d] = R[:, i*wXR+c] .* R[:, i*wXR+d]
+cudaError_t quad_products(cudaStream_t s, int n, int x, int wXR, const double* R, long long ldr, double* Q,
+                          long long ldq);
+
+// Batched p x p solve of x SNPs x t traits (see fgls_snp.cu for layouts).
+cudaError_t snp_solve(cudaStream_t s, int p, int x, int t, int wXL, const double* top, const double* GYL,
+                      long long ldg, const double* GR, long long ldr, double* B, long long bstride, double* V,
+                      long long vstride, DevStatus* st, long long snp_base);
+
+// Eigendecomposition (fgls_eig.cu).  A and Z: n x n device scratch/outputs
+// (ld n); work: eig_workspace_bytes(n).  *fail_out = 1 if QL did not converge.
+size_t eig_workspace_bytes(int n);
+cudaError_t dsyev_device(cudaStream_t s, int n, const double* Phi, long long ldp, double* A, double* Z,
+                         double* W, void* work, int* fail_out, long long* launches);
+
+// Genotype conversion: FP64 or u8 hard calls -> FP64 (device to device).
+cudaError_t u8_to_f64(cudaStream_t s, const unsigned char* in, double* out, long long count);
+
+}  // namespace fgls

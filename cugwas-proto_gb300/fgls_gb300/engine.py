@@ -1,0 +1,230 @@
+"""Python mirror of the C ABI in include/fgls_gb300.h (ctypes, no torch types).
+
+The drop-in functions ``fgls_chol`` / ``fgls_eigen`` / ``fgls_chol_gpu`` take
+the reference's 17 arguments (src/fgls_chol.h:4-10, src/fgls_eigen.h:68-74,
+src/fgls_chol_gpu.h:4-10) and raise ``FGLSError`` where the reference would
+print "[Error]: ..." and exit; they run in a child process so that the
+library's exit-on-error behaviour cannot end the caller.
+
+``Engine`` wraps the fglsgpu_* engine API.  Array arguments are numpy FP64
+arrays in the natural orientation of the reference's column-major files
+(Phi n x n, XL n x wXL, Y n x t, XR n x (m*wXR)); results are returned as
+B (traits, m, p) and V (traits, m, p, p) with V[..., r, c] = row r, column c.
+There is no CPU fallback: if the CUDA library cannot be loaded, every call
+raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libfgls_gb300.so")
+DRIVER_PATH = os.path.join(PKG, "lib", "fgls-driver")
+
+OK, EINVAL, ENOTSPD, ECUDA, EIO, ENOMEM, ETIMEOUT, ENOCONV, ENODEV, ESTATE = range(10)
+VARIANT = {"chol": 0, "eigen": 1}
+PRECISION = {"fp64": 0, "split": 1}
+
+# every symbol include/fgls_gb300.h declares
+EXPORTS = (
+    "fgls_chol", "fgls_eigen", "fgls_chol_gpu", "fglsgpu_create", "fglsgpu_destroy",
+    "fglsgpu_set_problem", "fglsgpu_select_trait", "fglsgpu_run_block", "fglsgpu_run_snps",
+    "fglsgpu_run_block_device", "fglsgpu_run_block_device_u8", "fglsgpu_sync",
+    "fglsgpu_get_res_sigma", "fglsgpu_get_eigen", "fglsgpu_stream", "fglsgpu_launch_count",
+    "fglsgpu_last_error", "fglsgpu_version",
+)
+
+
+class FGLSError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class Config(C.Structure):
+    _fields_ = [(f, C.c_int) for f in
+                ("n", "wXL", "wXR", "t", "x_b", "variant", "precision", "slices", "device", "reserved")]
+
+
+_lib = None
+
+
+def lib():
+    """Loads libfgls_gb300.so (built in-tree); raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise FGLSError(ENODEV, f"{LIB_PATH} not built: run __graft_entry__.build()")
+    L = C.CDLL(LIB_PATH)
+    P, I, LL, D = C.c_void_p, C.c_int, C.c_longlong, C.POINTER(C.c_double)
+    L.fglsgpu_create.argtypes = [C.POINTER(Config), C.POINTER(P)]
+    L.fglsgpu_destroy.argtypes = [P]
+    L.fglsgpu_set_problem.argtypes = [P, P, P, P, P, P]
+    L.fglsgpu_select_trait.argtypes = [P, I]
+    L.fglsgpu_run_block.argtypes = [P, P, I, P, P, LL, LL]
+    L.fglsgpu_run_snps.argtypes = [P, P, LL, P, P]
+    L.fglsgpu_run_block_device.argtypes = [P, P, I, P, P, LL, LL]
+    L.fglsgpu_run_block_device_u8.argtypes = [P, P, I, P, P, LL, LL]
+    L.fglsgpu_sync.argtypes = [P]
+    L.fglsgpu_get_res_sigma.argtypes = [P, P]
+    L.fglsgpu_get_eigen.argtypes = [P, P, P]
+    L.fglsgpu_stream.argtypes = [P]
+    L.fglsgpu_stream.restype = P
+    L.fglsgpu_launch_count.argtypes = [P]
+    L.fglsgpu_launch_count.restype = LL
+    L.fglsgpu_last_error.argtypes = [P]
+    L.fglsgpu_last_error.restype = C.c_char_p
+    L.fglsgpu_version.restype = I
+    _lib = L
+    return L
+
+
+def _ptr(a: np.ndarray):
+    return C.c_void_p(a.ctypes.data)
+
+
+def _f64(a, order="F"):
+    return np.require(np.asarray(a, dtype=np.float64), requirements=[order, "A"])
+
+
+class Engine:
+    """One fglsgpu engine (one GPU)."""
+
+    def __init__(self, n, wXL, wXR, t, x_b, variant="chol", precision="fp64", slices=0, device=0):
+        self.L = lib()
+        self.cfg = Config(n, wXL, wXR, t, x_b, VARIANT[variant], PRECISION[precision], slices, device, 0)
+        self.n, self.wXL, self.wXR, self.t, self.x_b = n, wXL, wXR, t, x_b
+        self.p = wXL + wXR
+        self.variant = variant
+        h = C.c_void_p()
+        self._h = None
+        self._check(self.L.fglsgpu_create(C.byref(self.cfg), C.byref(h)), None)
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _check(self, rc, h="self"):
+        if rc != OK:
+            hh = self._h if h == "self" else h
+            msg = self.L.fglsgpu_last_error(hh).decode(errors="replace")
+            raise FGLSError(rc, msg)
+
+    @property
+    def out_traits(self):
+        return self.t if self.variant == "eigen" else 1
+
+    def set_problem(self, Phi, XL, Y, h, sigma):
+        self._keep = [_f64(Phi), _f64(XL), _f64(Y), _f64(h), _f64(sigma)]
+        self._check(self.L.fglsgpu_set_problem(self._h, *[_ptr(a) for a in self._keep]))
+
+    def select_trait(self, j):
+        self._check(self.L.fglsgpu_select_trait(self._h, int(j)))
+
+    def run_block(self, XR):
+        XR = _f64(XR)
+        x = XR.shape[1] // self.wXR
+        nt, p = self.out_traits, self.p
+        B = np.empty((nt, x, p))
+        V = np.empty((nt, x, p, p))
+        self._check(self.L.fglsgpu_run_block(self._h, _ptr(XR), x, _ptr(B), _ptr(V), x * p, x * p * p))
+        return B, V.transpose(0, 1, 3, 2)
+
+    def run_snps(self, XR, B=None, V=None):
+        XR = _f64(XR)
+        m = XR.shape[1] // self.wXR
+        nt, p = self.out_traits, self.p
+        B = np.empty((nt, m, p)) if B is None else B
+        V = np.empty((nt, m, p, p)) if V is None else V
+        self._check(self.L.fglsgpu_run_snps(self._h, _ptr(XR), m, _ptr(B), _ptr(V)))
+        return B, V.transpose(0, 1, 3, 2)
+
+    def run_snps_ptr(self, xr_ptr, m, b_ptr, v_ptr):
+        """Host pointers (e.g. pinned torch tensors): XR, B, V."""
+        self._check(self.L.fglsgpu_run_snps(self._h, C.c_void_p(xr_ptr), int(m), C.c_void_p(b_ptr),
+                                            C.c_void_p(v_ptr)))
+
+    def run_block_device(self, xr_ptr, x, b_ptr, v_ptr, bstride, vstride, u8=False):
+        f = self.L.fglsgpu_run_block_device_u8 if u8 else self.L.fglsgpu_run_block_device
+        self._check(f(self._h, C.c_void_p(xr_ptr), int(x), C.c_void_p(b_ptr), C.c_void_p(v_ptr),
+                      int(bstride), int(vstride)))
+
+    def sync(self):
+        self._check(self.L.fglsgpu_sync(self._h))
+
+    def res_sigma(self):
+        out = np.empty(self.out_traits)
+        self._check(self.L.fglsgpu_get_res_sigma(self._h, _ptr(out)))
+        return out
+
+    def eigen(self):
+        W = np.empty(self.n)
+        Z = np.empty((self.n, self.n), order="F")
+        self._check(self.L.fglsgpu_get_eigen(self._h, _ptr(W), _ptr(Z)))
+        return W, Z
+
+    def stream(self):
+        return self.L.fglsgpu_stream(self._h)
+
+    def close(self):
+        if self._h is not None:
+            self.L.fglsgpu_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def launch_count() -> int:
+    return int(lib().fglsgpu_launch_count(None))
+
+
+def _dropin(name, n, p, m, t, wXL, wXR, x_b, y_b, num_threads, Phi_path, h2_path, sigma2_path,
+            XL_path, XR_path, Y_path, B_path, V_path, env=None):
+    """Calls the C entry point in a child process (it exits on error, like the
+    reference); raises FGLSError with the "[Error]: ..." text on failure."""
+    lib()  # fail loudly if missing
+    code = (
+        "import ctypes,sys\n"
+        f"L=ctypes.CDLL({LIB_PATH!r})\n"
+        "a=[int(x) for x in sys.argv[1:10]]+[s.encode() for s in sys.argv[10:]]\n"
+        f"sys.exit(L.{name}(*[ctypes.c_int(v) if isinstance(v,int) else ctypes.c_char_p(v) for v in a]))\n"
+    )
+    args = [str(v) for v in (n, p, m, t, wXL, wXR, x_b, y_b, num_threads)] + [
+        Phi_path, h2_path, sigma2_path, XL_path, XR_path, Y_path, B_path, V_path]
+    e = dict(os.environ)
+    if env:
+        e.update(env)
+    r = subprocess.run([sys.executable, "-c", code] + args, capture_output=True, text=True, env=e)
+    if r.returncode != 0:
+        msg = (r.stderr or r.stdout).strip().splitlines()
+        raise FGLSError(r.returncode, msg[-1] if msg else f"{name} exited {r.returncode}")
+    return 0
+
+
+def fgls_chol(*args, **kw):
+    return _dropin("fgls_chol", *args, **kw)
+
+
+def fgls_eigen(*args, **kw):
+    return _dropin("fgls_eigen", *args, **kw)
+
+
+def fgls_chol_gpu(*args, **kw):
+    return _dropin("fgls_chol_gpu", *args, **kw)

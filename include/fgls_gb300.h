@@ -1,0 +1,163 @@
+/*
+ * fgls_gb300.h -- C ABI of the GB300-native FGLS association engine.
+ *
+ * Two layers:
+ *
+ * 1. Drop-in entry points with the reference's exact 17-argument C
+ *    signatures.  They are file-path based like the reference (the callee
+ *    opens, reads, allocates and frees everything and writes B/V), read the
+ *    reference's on-disk layout, and on failure print "[Error]: ..." and
+ *    exit(EXIT_FAILURE) as the reference's error_msg(..., 1) does
+ *    (src/common.c:11-17).
+ *
+ * 2. The engine API (fglsgpu_*): plain C types and host or device pointers,
+ *    status codes instead of exit(), one GPU.  The drop-in entry points are
+ *    written on top of it.
+ *
+ * Layouts (all FP64, column-major, as in the reference files):
+ *   Phi n x n (lower triangle used), XL n x wXL, Y t x n (trait j at j*n),
+ *   XR block: x SNPs x wXR columns x n (SNP i column c at (i*wXR+c)*n),
+ *   B: per trait x*p doubles (SNP i at i*p, order [XL coefs, XR coefs]),
+ *   V: per trait x*p*p doubles (SNP i block at i*p*p, column-major p x p):
+ *      lower = res_sigma * S^-1, diagonal = standard errors, strict upper 0.
+ */
+#ifndef FGLS_GB300_H
+#define FGLS_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define FGLSGPU_OK 0
+#define FGLSGPU_EINVAL 1   /* invalid argument or dimensions                */
+#define FGLSGPU_ENOTSPD 2  /* M_j, the covariate Gram or a per-SNP S_i is not positive definite */
+#define FGLSGPU_ECUDA 3    /* CUDA runtime error (message in last_error)    */
+#define FGLSGPU_EIO 4      /* open/read/write failure or short read         */
+#define FGLSGPU_ENOMEM 5   /* device or pinned host allocation failed       */
+#define FGLSGPU_ETIMEOUT 6 /* a bounded device-side wait expired            */
+#define FGLSGPU_ENOCONV 7  /* the eigensolver did not converge              */
+#define FGLSGPU_ENODEV 8   /* no usable CUDA device                         */
+#define FGLSGPU_ESTATE 9   /* call out of order (e.g. run before set_problem) */
+
+/* ------------------------------------------------- drop-in entry points */
+
+/* Replaces fgls_chol, src/fgls_chol.h:4-10 (defined src/fgls_chol.c:29).
+ * y_b is ignored (the reference forces it to 1, src/fgls_chol.c:97,102-103);
+ * num_threads sizes the host I/O threads only. */
+int fgls_chol(int n, int p, int m, int t, int wXL, int wXR, int x_b, int y_b, int num_threads,
+              char *Phi_path, char *h2_path, char *sigma2_path, char *XL_path, char *XR_path,
+              char *Y_path, char *B_path, char *V_path);
+
+/* Replaces fgls_eigen, src/fgls_eigen.h:68-74 (defined src/fgls_eigen.c:38).
+ * Writes no <path>.tmp files: the rotations Z^T XL, Z^T XR, Z^T Y stay on
+ * the device.  Uses the split-precision tensor-core path when the
+ * environment variable FGLS_PRECISION=split is set, FP64 otherwise. */
+int fgls_eigen(int n, int p, int m, int t, int wXL, int wXR, int x_b, int y_b, int num_threads,
+               char *Phi_path, char *h2_path, char *sigma2_path, char *XL_path, char *XR_path,
+               char *Y_path, char *B_path, char *V_path);
+
+/* Replaces fgls_chol_gpu, src/fgls_chol_gpu.h:4-10 (defined
+ * src/fgls_chol_gpu.c:97).  Same computation as fgls_chol on one GPU; unlike
+ * the reference it accepts t > 1 (src/fgls_chol_gpu.c:169-174). */
+int fgls_chol_gpu(int n, int p, int m, int t, int wXL, int wXR, int x_b, int y_b,
+                  int num_threads, char *Phi_path, char *h2_path, char *sigma2_path,
+                  char *XL_path, char *XR_path, char *Y_path, char *B_path, char *V_path);
+
+/* ------------------------------------------------------------ engine API */
+
+typedef struct fglsgpu_engine fglsgpu_engine;
+
+#define FGLSGPU_VARIANT_CHOL 0  /* per-trait Cholesky whitening (fgls_chol)  */
+#define FGLSGPU_VARIANT_EIGEN 1 /* eigenbasis of Phi, all traits per block (fgls_eigen) */
+
+#define FGLSGPU_PREC_FP64 0     /* all-FP64 arithmetic                       */
+#define FGLSGPU_PREC_SPLIT 1    /* bulk GEMMs as BF16 slices on tcgen05 tensor cores,
+                                   FP32 accumulation, FP64 recombination      */
+
+typedef struct {
+  int n;         /* individuals                                  */
+  int wXL;       /* covariate columns (intercept included)       */
+  int wXR;       /* columns per SNP                              */
+  int t;         /* traits                                       */
+  int x_b;       /* maximum SNPs per block                       */
+  int variant;   /* FGLSGPU_VARIANT_*                            */
+  int precision; /* FGLSGPU_PREC_*                               */
+  int slices;    /* split precision: BF16 slices of the FP64 operand (0 = automatic) */
+  int device;    /* CUDA device ordinal                          */
+  int reserved;
+} fglsgpu_config;
+
+/* Creates an engine on cfg->device and allocates its device buffers. */
+int fglsgpu_create(const fglsgpu_config *cfg, fglsgpu_engine **out);
+int fglsgpu_destroy(fglsgpu_engine *e);
+
+/* Uploads the in-core operands (host pointers, reference layouts; only the
+ * first t entries of h and sigma are read) and runs the one-off setup:
+ * eigen: FP64 eigendecomposition of Phi on the device, Z^T XL, Z^T Y and the
+ * per-trait null-model residual variances (src/fgls_eigen.c:686-854,998-1195);
+ * chol: nothing beyond the upload (the per-trait work is select_trait). */
+int fglsgpu_set_problem(fglsgpu_engine *e, const double *Phi, const double *XL, const double *Y,
+                        const double *h, const double *sigma);
+
+/* chol only: factor M_j = sigma_j (h_j Phi + (1 - h_j) I) and compute trait
+ * j's null model (src/fgls_chol.c:251-325).  Subsequent blocks produce
+ * trait j's results.  Ignored (returns OK) for the eigen variant. */
+int fglsgpu_select_trait(fglsgpu_engine *e, int j);
+
+/* Processes one SNP block given as a HOST pointer (x_inc <= x_b SNPs,
+ * reference layout, genotypes as FP64).  Host->device copy, compute and
+ * device->host copy of the results run on the engine's streams; the call
+ * returns when B and V are in host memory.  Results for trait j (eigen: all
+ * traits; chol: the selected trait, written as trait 0) go to
+ * B + j*b_trait_stride and V + j*v_trait_stride. */
+int fglsgpu_run_block(fglsgpu_engine *e, const double *XR, int x_inc, double *B, double *V,
+                      long long b_trait_stride, long long v_trait_stride);
+
+/* Whole job over m SNPs given as one HOST array in the reference XR layout;
+ * results to host arrays in the B.out / V.out layout (trait j of the active
+ * traits at B + j*m*p and V + j*m*p*p; chol: the selected trait only).  Blocks
+ * of x_b SNPs are pipelined: upload of block b+1 and download of block b-1
+ * overlap the compute of block b (replaces the reference's aio double
+ * buffering, src/fgls_chol.c:327-487). */
+int fglsgpu_run_snps(fglsgpu_engine *e, const double *XR, long long m, double *B, double *V);
+
+/* Same with DEVICE pointers (XR, B, V already in HBM); asynchronous with
+ * respect to the host: call fglsgpu_sync before reading B/V. */
+int fglsgpu_run_block_device(fglsgpu_engine *e, const double *dXR, int x_inc, double *dB,
+                             double *dV, long long b_trait_stride, long long v_trait_stride);
+
+/* As run_block_device with genotypes as bytes (hard calls 0/1/2, same
+ * layout as XR); 8x fewer bytes to move than FP64. */
+int fglsgpu_run_block_device_u8(fglsgpu_engine *e, const unsigned char *dXR, int x_inc,
+                                double *dB, double *dV, long long b_trait_stride,
+                                long long v_trait_stride);
+
+/* Waits for the engine's device work and reports device-side failures
+ * (non-SPD per-SNP systems, expired waits). */
+int fglsgpu_sync(fglsgpu_engine *e);
+
+/* Per-trait null-model residual variance (t values; chol: selected trait). */
+int fglsgpu_get_res_sigma(fglsgpu_engine *e, double *out);
+
+/* The eigenvalues (n, ascending) and eigenvectors (n x n column-major) of
+ * Phi computed by set_problem (eigen variant); either pointer may be NULL. */
+int fglsgpu_get_eigen(fglsgpu_engine *e, double *W, double *Z);
+
+/* The CUDA stream the engine computes on (a cudaStream_t). */
+void *fglsgpu_stream(fglsgpu_engine *e);
+
+/* Number of the engine's own kernel launches since creation. */
+long long fglsgpu_launch_count(const fglsgpu_engine *e);
+
+/* Message describing the last failure on e (or on the calling thread when e
+ * is NULL). */
+const char *fglsgpu_last_error(const fglsgpu_engine *e);
+
+/* Library version, major*10000 + minor*100 + patch. */
+int fglsgpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FGLS_GB300_H */

@@ -1,0 +1,160 @@
+"""CUDA path vs the reference's own outputs (golden fixtures) and vs the FP64
+oracle, through the C ABI (engine API and the file-based drop-in entry
+points).
+
+Tolerances (FP64 path):
+* chol: beta normwise per (trait, SNP) <= 1e-12, standard errors element-wise
+  <= 1e-12, off-diagonal covariances normwise <= 1e-12, strict upper == 0.
+* eigen: |dbeta_k| / (|beta_k| + SE_k) <= 1e-11 and SE <= 1e-11: the
+  eigenvector route amplifies rounding on near-zero coefficients (the
+  reference's own chol and eigen outputs differ by ~2e-12 normwise there).
+"""
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+from conftest import golden_cases, load_golden
+from oracle import fgls_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+CHOL_TOL = dict(beta_normwise=1e-12, se_rel=1e-12, v_offdiag_normwise=1e-12)
+EIGEN_TOL = dict(beta_se_scaled=1e-11, se_rel=1e-11, v_offdiag_normwise=1e-11)
+
+
+def check(d, tol):
+    assert d["finite"], d
+    assert d["upper_abs_max"] == 0.0, d
+    for k, v in tol.items():
+        assert d[k] <= v, (k, d)
+
+
+def run_engine(pb, variant, x_b, precision="fp64"):
+    from fgls_gb300 import Engine
+    with Engine(pb.n, pb.wXL, pb.wXR, pb.t, x_b, variant=variant, precision=precision) as e:
+        e.set_problem(pb.Phi, pb.XL, pb.Y, pb.h, pb.sigma)
+        if variant == "eigen":
+            return e.run_snps(pb.XR)
+        Bs, Vs = [], []
+        for j in range(pb.t):
+            e.select_trait(j)
+            B, V = e.run_snps(pb.XR)
+            Bs.append(B[0])
+            Vs.append(V[0])
+        return np.stack(Bs), np.stack(Vs)
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_engine_vs_reference_golden(name):
+    pb, var, xb, Bref, Vref = load_golden(name)
+    variant = "chol" if var == "c" else "eigen"
+    B, V = run_engine(pb, variant, xb)
+    check(O.compare(B, V, Bref, Vref), CHOL_TOL if var == "c" else EIGEN_TOL)
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_dropin_files_vs_reference_golden(name):
+    """fgls_chol / fgls_eigen with the reference's 17 arguments, reading and
+    writing the reference's file layout."""
+    from fgls_gb300 import datagen, fgls_chol, fgls_eigen
+    pb, var, xb, Bref, Vref = load_golden(name)
+    d = tempfile.mkdtemp()
+    paths = datagen.write_problem(pb, d)
+    args = (pb.n, pb.p, pb.m, pb.t, pb.wXL, pb.wXR, xb, 1, 2, paths["Phi.in"], paths["H.in"], paths["Sig.in"],
+            paths["XL.in"], paths["XR.in"], paths["Y.in"], os.path.join(d, "B.out"), os.path.join(d, "V.out"))
+    (fgls_chol if var == "c" else fgls_eigen)(*args)
+    raw_v = np.fromfile(os.path.join(d, "V.out"))
+    assert raw_v.size == pb.t * pb.m * pb.p * pb.p
+    B, V = datagen.read_outputs(d, pb.m, pb.t, pb.p)
+    check(O.compare(B, V, Bref, Vref), CHOL_TOL if var == "c" else EIGEN_TOL)
+
+
+@pytest.mark.parametrize("n,m,t,wXL,wXR,xb", [
+    (300, 1000, 3, 3, 1, 256),   # ragged last block
+    (257, 97, 2, 1, 1, 97),      # p = 2, single block, odd n
+    (130, 33, 1, 6, 2, 7),       # p = 8 (maximum), tiny blocks
+    (200, 1, 2, 3, 1, 64),       # m = 1 < x_b
+    (129, 50, 2, 2, 3, 16),      # wXR = 3
+])
+@pytest.mark.parametrize("variant", ["chol", "eigen"])
+def test_engine_vs_oracle_shapes(n, m, t, wXL, wXR, xb, variant):
+    from fgls_gb300 import datagen
+    pb = datagen.make_problem(n, m, t, wXL=wXL, wXR=wXR, seed=n + m, hsig_uniform=True)
+    B, V = run_engine(pb, variant, xb)
+    Br, Vr = O.fgls_chol(pb, xb) if variant == "chol" else O.fgls_eigen(pb)
+    check(O.compare(B, V, Br, Vr), CHOL_TOL if variant == "chol" else EIGEN_TOL)
+
+
+def test_chol_larger_n_vs_oracle():
+    """n spans several 128-row potrf/TRSM blocks plus a ragged one."""
+    from fgls_gb300 import datagen
+    pb = datagen.make_problem(1000, 600, 2, seed=9, hsig_uniform=True)
+    B, V = run_engine(pb, "chol", 256)
+    Br, Vr = O.fgls_chol(pb, 256)
+    check(O.compare(B, V, Br, Vr), CHOL_TOL)
+
+
+def test_eigensolver_properties():
+    from fgls_gb300 import Engine, datagen
+    pb = datagen.make_problem(700, 4, 1, seed=4)
+    with Engine(pb.n, 3, 1, 1, 4, variant="eigen") as e:
+        e.set_problem(pb.Phi, pb.XL, pb.Y, pb.h, pb.sigma)
+        W, Z = e.eigen()
+    Wr = np.linalg.eigvalsh(pb.Phi)
+    nrm = np.abs(Wr).max()
+    assert np.all(np.diff(W) >= 0)
+    assert np.abs(W - Wr).max() < 1e-13 * nrm * 10
+    assert np.abs(Z.T @ Z - np.eye(pb.n)).max() < 1e-12
+    assert np.abs(pb.Phi @ Z - Z * W).max() < 1e-12 * nrm
+
+
+def test_run_block_host_api_matches_run_snps():
+    from fgls_gb300 import Engine, datagen
+    pb = datagen.make_problem(150, 70, 3, seed=2, hsig_uniform=True)
+    with Engine(pb.n, 3, 1, 3, 32, variant="eigen") as e:
+        e.set_problem(pb.Phi, pb.XL, pb.Y, pb.h, pb.sigma)
+        B, V = e.run_snps(pb.XR)
+        B2, V2 = e.run_block(pb.XR[:, 32:64])
+    assert np.array_equal(B[:, 32:64], B2) and np.array_equal(V[:, 32:64], V2)
+
+
+def test_not_spd_phi_is_reported():
+    """A non-positive-definite M must fail like the reference's dpotrf(M)
+    check (src/fgls_chol.c:266-271), through the status word, not a fault."""
+    from fgls_gb300 import Engine, FGLSError, datagen
+    pb = datagen.make_problem(64, 8, 1, seed=1)
+    Phi = -np.eye(pb.n) * 5.0
+    with Engine(pb.n, 3, 1, 1, 8, variant="chol") as e:
+        e.set_problem(Phi, pb.XL, pb.Y, np.array([0.9]), np.array([1.0]))
+        with pytest.raises(FGLSError, match="dpotrf\\(M\\) failed"):
+            e.select_trait(0)
+
+
+def test_truncated_xr_file_is_an_error():
+    from fgls_gb300 import FGLSError, datagen, fgls_chol
+    pb = datagen.make_problem(64, 20, 1, seed=1)
+    d = tempfile.mkdtemp()
+    paths = datagen.write_problem(pb, d)
+    with open(paths["XR.in"], "r+b") as f:
+        f.truncate(64 * 8 * 15)
+    with pytest.raises(FGLSError, match="short read of XR"):
+        fgls_chol(64, 4, 20, 1, 3, 1, 8, 1, 1, paths["Phi.in"], paths["H.in"], paths["Sig.in"],
+                  paths["XL.in"], paths["XR.in"], paths["Y.in"], os.path.join(d, "B.out"), os.path.join(d, "V.out"))
+
+
+def test_u8_genotypes_match_fp64():
+    import torch
+    from fgls_gb300 import Engine, datagen
+    pb = datagen.make_problem(160, 48, 2, seed=8, hsig_uniform=True)
+    with Engine(pb.n, 3, 1, 2, 48, variant="eigen") as e:
+        e.set_problem(pb.Phi, pb.XL, pb.Y, pb.h, pb.sigma)
+        B, V = e.run_snps(pb.XR)
+        xu8 = torch.from_numpy(np.asfortranarray(pb.XR).T.astype(np.uint8).copy()).cuda()
+        dB = torch.empty(2 * 48 * 4, dtype=torch.float64, device="cuda")
+        dV = torch.empty(2 * 48 * 16, dtype=torch.float64, device="cuda")
+        e.run_block_device(xu8.data_ptr(), 48, dB.data_ptr(), dV.data_ptr(), 48 * 4, 48 * 16, u8=True)
+        e.sync()
+    B2 = dB.cpu().numpy().reshape(2, 48, 4)
+    assert np.array_equal(B, B2)

@@ -1,0 +1,77 @@
+"""The oracle (numpy FP64 restatement) against the reference's own outputs:
+tests/golden/*.npz hold B/V written by the reference driver built from its
+sources (see tests/golden/make_golden.py)."""
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+from conftest import golden_cases, load_golden
+from oracle import fgls_oracle as O
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_oracle_matches_reference_golden(name):
+    pb, var, xb, Bref, Vref = load_golden(name)
+    B, V = O.fgls_chol(pb, xb) if var == "c" else O.fgls_eigen(pb)
+    d = O.compare(B, V, Bref, Vref)
+    assert d["finite"]
+    assert d["upper_abs_max"] == 0.0
+    assert float(np.abs(np.triu(Vref, 1)).max()) == 0.0  # the reference leaves the strict upper triangle 0
+    if var == "c":
+        assert d["beta_normwise"] < 1e-12, d
+        assert d["se_rel"] < 1e-12, d
+        assert d["v_offdiag_normwise"] < 1e-12, d
+    else:
+        # eigen: eigenvector-route rounding; the reference's own chol and
+        # eigen variants differ by ~2e-12 normwise on small coefficients
+        assert d["beta_se_scaled"] < 1e-11, d
+        assert d["beta_normwise"] < 2e-10, d
+        assert d["se_rel"] < 1e-12, d
+
+
+def test_goldens_present():
+    assert len(golden_cases()) >= 5
+
+
+def test_oracle_detects_a_planted_error():
+    """A mistake planted in the oracle's output must be caught by compare()."""
+    pb, var, xb, Bref, Vref = load_golden("chol_n128_m200_t2")
+    B, V = O.fgls_chol(pb, xb)
+    B = B.copy()
+    B[1, 17, 3] *= 1 + 1e-9
+    assert O.compare(B, V, Bref, Vref)["beta_normwise"] > 1e-10
+
+
+def test_chol_and_eigen_oracles_agree():
+    pb, var, xb, Bref, Vref = load_golden("chol_n128_m200_t2")
+    B1, V1 = O.fgls_chol(pb, 64)
+    B2, V2 = O.fgls_eigen(pb)
+    d = O.compare(B2, V2, B1, V1)
+    assert d["beta_se_scaled"] < 1e-11 and d["se_rel"] < 1e-11, d
+
+
+@pytest.mark.skipif(not os.path.isdir("/root/reference/test_cases/test_XL"), reason="reference fixture absent")
+def test_oracle_on_reference_fixture_inputs():
+    """The reference's own fixture inputs (test_cases/test_XL: n=500, t=20,
+    wXL=3; its XR.in is missing) with a synthetic XR, run through the
+    reference driver and the oracle."""
+    from oracle import run_ref
+    from fgls_gb300 import datagen
+    if not run_ref.available():
+        pytest.skip("reference driver not built")
+    src = "/root/reference/test_cases/test_XL"
+    n, t, wXL, m = 500, 4, 3, 64
+    d = tempfile.mkdtemp()
+    for f in ("Phi.in", "H.in", "Sig.in", "XL.in", "Y.in"):
+        os.symlink(os.path.join(src, f), os.path.join(d, f))
+    rng = np.random.default_rng(3)
+    XR = datagen.hardcall_genotypes(rng, n, m)
+    np.asfortranarray(XR).T.astype("<f8").tofile(os.path.join(d, "XR.in"))
+    run_ref.run("c", d, n, 4, m, t, wXL, 32, threads=1)
+    Bref, Vref = datagen.read_outputs(d, m, t, 4)
+    pb = datagen.read_problem(d, n, m, t, wXL)
+    B, V = O.fgls_chol(pb, 32)
+    r = O.compare(B, V, Bref, Vref)
+    assert r["beta_normwise"] < 1e-12 and r["se_rel"] < 1e-12, r
