@@ -51,6 +51,15 @@ struct fglsgpu_engine {
   int trait_sel = -1;
   bool problem_set = false;
   std::string err;
+  // per-kernel-class timing with CUDA events on the launching stream
+  struct PEv {
+    cudaEvent_t a, b;
+    int cls;
+  };
+  bool prof = false;
+  std::vector<PEv> pev_live, pev_pool;
+  double prof_ms[FGLSGPU_PROF_CLASSES] = {0};
+  long long prof_cnt[FGLSGPU_PROF_CLASSES] = {0};
 };
 
 namespace {
@@ -116,6 +125,11 @@ void free_all(fglsgpu_engine* e) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (e->hst) cudaFreeHost(e->hst);
+  for (auto* v : {&e->pev_live, &e->pev_pool})
+    for (auto& ev : *v) {
+      cudaEventDestroy(ev.a);
+      cudaEventDestroy(ev.b);
+    }
   if (e->oz) ozaki_destroy(e->oz);
   for (int k = 0; k < 2; k++) {
     if (e->evH[k]) cudaEventDestroy(e->evH[k]);
@@ -129,35 +143,84 @@ void free_all(fglsgpu_engine* e) {
 
 bool split(const fglsgpu_engine* e) { return e->cfg.precision == FGLSGPU_PREC_SPLIT; }
 
+// Brackets the kernels launched in its scope with two events on stream s
+// when profiling is on; resolved by fglsgpu_profile_read.
+struct Prof {
+  fglsgpu_engine* e;
+  cudaStream_t s;
+  fglsgpu_engine::PEv ev{};
+  bool on;
+  Prof(fglsgpu_engine* e_, int cls, cudaStream_t s_) : e(e_), s(s_), on(e_->prof) {
+    if (!on) return;
+    if (e->pev_pool.empty()) {
+      cudaEventCreate(&ev.a);
+      cudaEventCreate(&ev.b);
+    } else {
+      ev = e->pev_pool.back();
+      e->pev_pool.pop_back();
+    }
+    ev.cls = cls;
+    cudaEventRecord(ev.a, s);
+  }
+  ~Prof() {
+    if (!on) return;
+    cudaEventRecord(ev.b, s);
+    e->pev_live.push_back(ev);
+  }
+};
+
 // Compute one block already in device memory (FP64 genotypes at dXin,
 // n x x*wXR) into dB/dV with the given trait strides, on e->comp.
-int compute_block(fglsgpu_engine* e, const double* dXin, int x, double* dB, double* dV, long long bstr,
-                  long long vstr, long long snp_base) {
+int compute_block(fglsgpu_engine* e, const double* dXin, const unsigned char* dXu8, int x, double* dB, double* dV,
+                  long long bstr, long long vstr, long long snp_base) {
   const fglsgpu_config& c = e->cfg;
   const int n = c.n, wXL = c.wXL, wXR = c.wXR, p = e->p;
+  const int t = c.variant == FGLSGPU_VARIANT_EIGEN ? c.t : 1;
   const long long cols = (long long)x * wXR;
   cudaStream_t s = e->comp;
+  if (c.variant == FGLSGPU_VARIANT_CHOL && e->trait_sel < 0)
+    return fail(e, FGLSGPU_ESTATE, "fglsgpu_select_trait must precede run_block (chol)");
+  if (split(e)) {
+    {
+      Prof pr(e, FGLSGPU_PROF_GENOTYPES, s);
+      ENG_TRY(e, dXu8 ? ozaki_genotypes_u8(e->oz, s, dXu8, x) : ozaki_genotypes(e->oz, s, dXin, x), "genotypes");
+    }
+    {
+      Prof pr(e, FGLSGPU_PROF_SPLIT_GEMM, s);
+      ENG_TRY(e, ozaki_product(e->oz, s, x), "split GEMM");
+    }
+    {
+      Prof pr(e, FGLSGPU_PROF_SELFGRAM, s);
+      ENG_TRY(e, ozaki_selfgram(e->oz, s, x, e->dGR), "quadratic Gram");
+    }
+    long long ld = 0;
+    const double* gyl = ozaki_gram_rows(e->oz, &ld);
+    Prof pr(e, FGLSGPU_PROF_SOLVE, s);
+    ENG_TRY(e, snp_solve(s, p, x, t, wXL, e->dtop, gyl, ld, 1, e->dGR, cols * wXR, dB, bstr, dV, vstr, e->dst,
+                         snp_base),
+            "solve");
+    return FGLSGPU_OK;
+  }
+  if (dXu8) {
+    Prof pr(e, FGLSGPU_PROF_GENOTYPES, s);
+    ENG_TRY(e, u8_to_f64(s, dXu8, e->dX[1], (long long)cols * n), "widen genotypes");
+    dXin = e->dX[1];
+  }
   if (c.variant == FGLSGPU_VARIANT_CHOL) {
-    if (e->trait_sel < 0) return fail(e, FGLSGPU_ESTATE, "fglsgpu_select_trait must precede run_block (chol)");
-    if (split(e)) {
-      ENG_TRY(e, ozaki_chol_block(e->oz, s, dXin, x, e->dWork), "split TRSM");
-    } else {
+    {
+      Prof pr(e, FGLSGPU_PROF_TRSM, s);
       ENG_TRY(e, cudaMemcpyAsync(e->dWork, dXin, sizeof(double) * n * cols, cudaMemcpyDeviceToDevice, s),
               "block copy");
       ENG_TRY(e, dtrsm_llnn(s, n, (int)cols, e->dL, n, e->dWork, n), "TRSM");
     }
+    Prof pr(e, FGLSGPU_PROF_GRAM, s);
     ENG_TRY(e, gram_skinny(s, n, x, wXL, wXR, e->dWork, n, e->dWY, e->dGYL, e->dGR), "gram");
-    ENG_TRY(e, snp_solve(s, p, x, 1, wXL, e->dtop, e->dGYL, cols, e->dGR, cols * wXR, dB, bstr, dV, vstr,
-                         e->dst, snp_base),
-            "solve");
-    return FGLSGPU_OK;
-  }
-  // eigen
-  const int t = c.t;
-  if (split(e)) {
-    ENG_TRY(e, ozaki_eigen_block(e->oz, s, dXin, x, e->dGYL, e->dGR), "split eigen block");
   } else {
-    ENG_TRY(e, dgemm(s, true, false, n, (int)cols, n, 1.0, e->dZ, n, dXin, n, 0.0, e->dWork, n), "Z^T XR");
+    {
+      Prof pr(e, FGLSGPU_PROF_FP64_GEMM, s);
+      ENG_TRY(e, dgemm(s, true, false, n, (int)cols, n, 1.0, e->dZ, n, dXin, n, 0.0, e->dWork, n), "Z^T XR");
+    }
+    Prof pr(e, FGLSGPU_PROF_GRAM, s);
     ENG_TRY(e, dgemm(s, true, false, (int)cols, t * (1 + wXL), n, 1.0, e->dWork, n, e->dAYL, n, 0.0, e->dGYL,
                      cols),
             "gram YL");
@@ -166,7 +229,8 @@ int compute_block(fglsgpu_engine* e, const double* dXin, int x, double* dB, doub
     ENG_TRY(e, dgemm(s, true, false, (int)qcols, t, n, 1.0, e->dQ, n, e->ddinv, n, 0.0, e->dGR, qcols),
             "gram R");
   }
-  ENG_TRY(e, snp_solve(s, p, x, t, wXL, e->dtop, e->dGYL, cols, e->dGR, cols * wXR, dB, bstr, dV, vstr, e->dst,
+  Prof pr(e, FGLSGPU_PROF_SOLVE, s);
+  ENG_TRY(e, snp_solve(s, p, x, t, wXL, e->dtop, e->dGYL, 1, cols, e->dGR, cols * wXR, dB, bstr, dV, vstr, e->dst,
                        snp_base),
           "solve");
   return FGLSGPU_OK;
@@ -356,7 +420,7 @@ int fglsgpu_select_trait(fglsgpu_engine* e, int j) {
   if (rc) return rc;
   if (split(e)) {
     if (!e->oz) ENG_TRY(e, ozaki_create(&e->oz, c.n, 1, c.wXL, c.wXR, c.x_b, c.slices, /*eigen=*/0), "split plan");
-    ENG_TRY(e, ozaki_set_chol(e->oz, s, e->dL), "split operands");
+    ENG_TRY(e, ozaki_set_chol(e->oz, s, e->dL, e->dWY), "split operands");
     ENG_TRY(e, cudaStreamSynchronize(s), "split operands");
   }
   e->trait_sel = j;
@@ -371,7 +435,7 @@ int fglsgpu_run_block_device(fglsgpu_engine* e, const double* dXR, int x_inc, do
   if (!dXR || !dB || !dV) return fail(e, FGLSGPU_EINVAL, "null block pointer");
   ENG_TRY(e, cudaSetDevice(e->cfg.device), "cudaSetDevice");
   // Device failures accumulate in the status word until fglsgpu_sync.
-  return compute_block(e, dXR, x_inc, dB, dV, bstr, vstr, 0);
+  return compute_block(e, dXR, nullptr, x_inc, dB, dV, bstr, vstr, 0);
 }
 
 int fglsgpu_run_block_device_u8(fglsgpu_engine* e, const unsigned char* dXR, int x_inc, double* dB, double* dV,
@@ -380,16 +444,8 @@ int fglsgpu_run_block_device_u8(fglsgpu_engine* e, const unsigned char* dXR, int
   if (!e->problem_set) return fail(e, FGLSGPU_ESTATE, "set_problem must precede run_block");
   if (x_inc <= 0 || x_inc > e->cfg.x_b) return fail(e, FGLSGPU_EINVAL, "x_inc=%d outside [1, %d]", x_inc, e->cfg.x_b);
   ENG_TRY(e, cudaSetDevice(e->cfg.device), "cudaSetDevice");
-  const long long cnt = (long long)x_inc * e->cfg.wXR * e->cfg.n;
-  if (split(e) && e->cfg.variant == FGLSGPU_VARIANT_EIGEN) {
-    ENG_TRY(e, ozaki_eigen_block_u8(e->oz, e->comp, dXR, x_inc, e->dGYL, e->dGR), "split eigen block");
-    ENG_TRY(e, snp_solve(e->comp, e->p, x_inc, e->cfg.t, e->cfg.wXL, e->dtop, e->dGYL, (long long)x_inc * e->cfg.wXR,
-                         e->dGR, (long long)x_inc * e->cfg.wXR * e->cfg.wXR, dB, bstr, dV, vstr, e->dst, 0),
-            "solve");
-    return FGLSGPU_OK;
-  }
-  ENG_TRY(e, u8_to_f64(e->comp, dXR, e->dX[1], cnt), "widen genotypes");
-  return compute_block(e, e->dX[1], x_inc, dB, dV, bstr, vstr, 0);
+  if (!dXR || !dB || !dV) return fail(e, FGLSGPU_EINVAL, "null block pointer");
+  return compute_block(e, nullptr, dXR, x_inc, dB, dV, bstr, vstr, 0);
 }
 
 int fglsgpu_sync(fglsgpu_engine* e) {
@@ -415,7 +471,7 @@ int fglsgpu_run_block(fglsgpu_engine* e, const double* XR, int x_inc, double* B,
   ENG_TRY(e, cudaMemcpyAsync(e->dX[0], XR, sizeof(double) * c.n * (size_t)x_inc * c.wXR, cudaMemcpyHostToDevice, s),
           "XR upload");
   const long long db = (long long)x_inc * p, dv = (long long)x_inc * p * p;
-  rc = compute_block(e, e->dX[0], x_inc, e->dB[0], e->dV[0], db, dv, 0);
+  rc = compute_block(e, e->dX[0], nullptr, x_inc, e->dB[0], e->dV[0], db, dv, 0);
   if (rc) return rc;
   const int nt = out_traits(e);
   ENG_TRY(e, cudaMemcpy2DAsync(B, sizeof(double) * bstr, e->dB[0], sizeof(double) * db, sizeof(double) * db, nt,
@@ -457,7 +513,7 @@ int fglsgpu_run_snps(fglsgpu_engine* e, const double* XR, long long m, double* B
     ENG_TRY(e, cudaStreamWaitEvent(e->comp, e->evH[k], 0), "wait");
     ENG_TRY(e, cudaStreamWaitEvent(e->comp, e->evD[k], 0), "wait");  // outputs of block b-2 downloaded
     const long long db = (long long)x * p, dv = (long long)x * p * p;
-    rc = compute_block(e, e->dX[k], x, e->dB[k], e->dV[k], db, dv, ib);
+    rc = compute_block(e, e->dX[k], nullptr, x, e->dB[k], e->dV[k], db, dv, ib);
     if (rc) return rc;
     ENG_TRY(e, cudaEventRecord(e->evC[k], e->comp), "event");
     ENG_TRY(e, cudaStreamWaitEvent(e->d2h, e->evC[k], 0), "wait");
@@ -472,6 +528,39 @@ int fglsgpu_run_snps(fglsgpu_engine* e, const double* XR, long long m, double* B
   ENG_TRY(e, cudaStreamSynchronize(e->d2h), "run_snps");
   ENG_TRY(e, cudaStreamSynchronize(e->h2d), "run_snps");
   return check_status(e, "block");
+}
+
+int fglsgpu_profile(fglsgpu_engine* e, int enable) {
+  if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
+  ENG_TRY(e, cudaSetDevice(e->cfg.device), "cudaSetDevice");
+  ENG_TRY(e, cudaStreamSynchronize(e->comp), "profile");
+  for (auto& ev : e->pev_live) e->pev_pool.push_back(ev);
+  e->pev_live.clear();
+  for (int k = 0; k < FGLSGPU_PROF_CLASSES; k++) {
+    e->prof_ms[k] = 0.0;
+    e->prof_cnt[k] = 0;
+  }
+  e->prof = enable != 0;
+  return FGLSGPU_OK;
+}
+
+int fglsgpu_profile_read(fglsgpu_engine* e, double* ms, long long* count) {
+  if (!e || !ms || !count) return fail(e, FGLSGPU_EINVAL, "null argument");
+  ENG_TRY(e, cudaSetDevice(e->cfg.device), "cudaSetDevice");
+  for (auto& ev : e->pev_live) {
+    ENG_TRY(e, cudaEventSynchronize(ev.b), "profile event");
+    float t = 0.f;
+    ENG_TRY(e, cudaEventElapsedTime(&t, ev.a, ev.b), "profile event");
+    e->prof_ms[ev.cls] += t;
+    e->prof_cnt[ev.cls] += 1;
+    e->pev_pool.push_back(ev);
+  }
+  e->pev_live.clear();
+  for (int k = 0; k < FGLSGPU_PROF_CLASSES; k++) {
+    ms[k] = e->prof_ms[k];
+    count[k] = e->prof_cnt[k];
+  }
+  return FGLSGPU_OK;
 }
 
 int fglsgpu_get_res_sigma(fglsgpu_engine* e, double* out) {

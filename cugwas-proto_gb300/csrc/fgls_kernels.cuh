@@ -35,8 +35,9 @@ cudaError_t quad_products(cudaStream_t s, int n, int x, int wXR, const double* R
                           long long ldq);
 
 // Batched p x p solve of x SNPs x t traits (see fgls_snp.cu for layouts).
+// Gram term (row, q) is read at GYL[row*rsg + q*ldg].
 cudaError_t snp_solve(cudaStream_t s, int p, int x, int t, int wXL, const double* top, const double* GYL,
-                      long long ldg, const double* GR, long long ldr, double* B, long long bstride, double* V,
+                      long long rsg, long long ldg, const double* GR, long long ldr, double* B, long long bstride, double* V,
                       long long vstride, DevStatus* st, long long snp_base);
 
 // Eigendecomposition (fgls_eig.cu).  A and Z: n x n device scratch/outputs

@@ -1,23 +1,812 @@
+// Split-precision (Ozaki-style) tensor-core path for the bulk GEMMs.
+//
+//   C[r, c] = sum_k A[r, k] * G[c, k]        A FP64 (rows of Z^T, U^T or L^-1),
+//                                            G genotypes (0/1/2), K = n
+//
+// A is cut once per problem into S BF16 "digit" slices with a per-row
+// power-of-two scale 2^e_r:
+//   A[r, k] = 2^(e_r - 7) * sum_s d_s[r, k] * 2^(-8 s),   d_s integer in [-128, 128]
+// (round-to-nearest digits: each slice carries 8 bits, truncation error
+// <= 2^(e_r - 8 S)).  Genotypes are exact in BF16.  Every slice product
+// P_s = d_s G^T is an integer with |P_s| <= 128 * 2 * K < 2^22 for K <= 16383,
+// so FP32 accumulation in TMEM is exact and the result is bit-reproducible.
+//
+// Kernel ozaki_gemm_kernel (one 128 x 256 output tile per CTA, 6 warps):
+//   warp 0      TMA producer: per K-step of 64, two A-slice tiles (128 x 64)
+//               and one genotype tile (256 x 64), 128B-swizzled, 3 stages.
+//   warp 1      allocates 512 TMEM columns and issues tcgen05.mma
+//               (kind::f16, BF16 x BF16 -> F32, M=128 N=256 K=16): slice 2p
+//               into columns [0,256), slice 2p+1 into [256,512).
+//   warps 2-5   epilogue: tcgen05.ld the two accumulators, combine them
+//               exactly in int32 (q = P_2p * 256 + P_2p+1), Horner-accumulate
+//               the passes in int64 in the output buffer (V = V * 2^16 + q),
+//               and on the last pass write V * 2^(e_r - 15 - 16 (passes-1))
+//               as FP64.  |V| < 2^62 for S <= 6.
+// Every mbarrier wait is bounded; on expiry the kernel raises an error flag,
+// drains its own in-flight copies and MMAs (bounded), frees TMEM and exits.
+//
+// Consumers (fgls eigen / chol split path):
+//   eigen: A = [Z^T ; U^T], U = Z * [ZtY .* d_j | ZtXL .* d_j] (n x t(1+wXL)):
+//          rows [0, n) of C are R = Z^T X, rows [n, n + t(1+wXL)) are the
+//          Gram terms x~^T y~_j and x~^T XL~_j directly (one-sided: the exact
+//          genotypes are the other operand).  The quadratic terms
+//          sum_l R_l^2 d_j(l) run in double-FP32 (error-free products and
+//          sums) on the CUDA cores: selfgram_kernel.
+//   chol:  A = [L^-1 ; U^T], U = L^-T [y~ | XL~].
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "fgls_common.cuh"
+#include "fgls_kernels.cuh"
 #include "fgls_ozaki.cuh"
 
 namespace fgls {
-struct OzakiPlan {
-  int dummy;
+
+namespace oz {
+
+constexpr int BM = 128, BN = 256, BK = 64;
+constexpr int STAGES = 3;
+constexpr int A_TILE = BM * BK * 2;               // 16 KB
+constexpr int B_TILE = BN * BK * 2;               // 32 KB
+constexpr int STAGE_BYTES = 2 * A_TILE + B_TILE;  // 64 KB
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+constexpr int THREADS = 192;
+constexpr int MAX_SLICES = 6;
+constexpr int GROUP_M = 8;
+
+// tcgen05.mma instruction descriptor, kind::f16: D=F32, A=B=BF16, both
+// K-major, N=256, M=128.
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                           ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+constexpr uint64_t WAIT_NS = 2000000000ull;  // one wait gives up after 2 s
+
+// Bounded wait: false if the phase does not complete within WAIT_NS (the
+// kernel-wide error word `err` then records `site`), or if this CTA or any
+// other CTA of the launch already gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                                          int* err, int site) {
+  const uint64_t t0 = globaltimer_ns();
+  for (uint32_t it = 0;; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((it & 63) == 63) {
+      if (*abort_flag || *(volatile int*)err) {
+        *abort_flag = 1;
+        return false;
+      }
+      if (globaltimer_ns() - t0 > WAIT_NS) {
+        *abort_flag = 1;
+        atomicCAS(err, 0, site);
+        return false;
+      }
+    }
+  }
+}
+
+// Bounded drain wait used on the abort path only.
+__device__ __forceinline__ void mbar_drain(uint64_t* bar, uint32_t parity) {
+  const uint64_t t0 = globaltimer_ns();
+  while (!mbar_try_wait(bar, parity) && globaltimer_ns() - t0 < WAIT_NS) {
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"((uint64_t)tm), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ uint64_t desc_sw128(const void* p) {
+  const uint32_t a = smem_u32(p);
+  uint64_t d = 0;
+  d |= (uint64_t)((a & 0x3FFFFu) >> 4);  // start address
+  d |= (uint64_t)1 << 16;                // leading byte offset (unused for SW128 K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;      // stride byte offset: 8 rows x 128 B
+  d |= (uint64_t)1 << 46;                // descriptor version (sm_100 family)
+  d |= (uint64_t)2 << 61;                // 128B swizzle
+  return d;
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t dt, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dt),
+      "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+struct GemmArgs {
+  int M;            // valid rows of A
+  int Mpad;         // rows per slice in the A tensor (multiple of BM)
+  int N;            // valid genotype columns
+  int Kpad;         // K padded to a multiple of BK
+  int S;            // slices (1..MAX_SLICES)
+  int tiles_m, tiles_n;
+  int tri_rows;     // rows [0, tri_rows) of A are lower triangular in K (0: none)
+  const double* row_scale;  // per row 2^(e_r - 15 - 16 (passes-1))
+  double* C;        // FP64 output, column-major, ld = ldc (int64 between passes)
+  long long ldc;
+  int* err;         // first failing wait site (0 = ok)
 };
-cudaError_t ozaki_create(OzakiPlan** out, int, int, int, int, int, int, int) {
+
+__global__ void __launch_bounds__(THREADS, 1)
+    ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                      const GemmArgs g) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
+  uint64_t* empty = full + STAGES;
+  uint64_t* tfull = empty + STAGES;
+  uint64_t* tempty = tfull + 1;
+  uint64_t* drain = tempty + 1;
+  uint32_t* tbase_slot = (uint32_t*)(drain + 1);
+  volatile int* abort_flag = (volatile int*)(tbase_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // grouped rasterization: GROUP_M row tiles share the resident column tiles
+  const int tile = blockIdx.x;
+  const int per_group = GROUP_M * g.tiles_n;
+  const int group = tile / per_group;
+  const int first_m = group * GROUP_M;
+  const int gsz = min(g.tiles_m - first_m, GROUP_M);
+  const int m_tile = first_m + (tile % per_group) % gsz;
+  const int n_tile = (tile % per_group) / gsz;
+  const int m0 = m_tile * BM, n0 = n_tile * BN;
+  const int passes = (g.S + 1) / 2;
+  int nk = g.Kpad / BK;
+  if (m0 + BM <= g.tri_rows) nk = min(nk, (m0 + BM + BK - 1) / BK);  // zero upper part of L^-1
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(tfull, 1);
+    mbar_init(tempty, 128);
+    mbar_init(drain, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tbase_slot)),
+                 "r"(512)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = *tbase_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      int issued[STAGES];
+      uint32_t issued_phase[STAGES];
+      for (int s = 0; s < STAGES; s++) issued[s] = 0;
+      bool ok = true;
+      for (int p = 0; p < passes && ok; p++) {
+        const int s0 = 2 * p, s1 = 2 * p + 1;
+        const bool two = s1 < g.S;
+        for (int kb = 0; kb < nk; kb++) {
+          if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, g.err, 1)) { ok = false; break; }
+          issued[stage] = 0;
+          uint8_t* sb = smem + stage * STAGE_BYTES;
+          mbar_expect_tx(&full[stage], (two ? 2 * A_TILE : A_TILE) + B_TILE);
+          tma_load_2d(sb, &tmA, kb * BK, s0 * g.Mpad + m0, &full[stage]);
+          if (two) tma_load_2d(sb + A_TILE, &tmA, kb * BK, s1 * g.Mpad + m0, &full[stage]);
+          tma_load_2d(sb + 2 * A_TILE, &tmB, kb * BK, n0, &full[stage]);
+          issued[stage] = 1;
+          issued_phase[stage] = phase;
+          if (++stage == STAGES) { stage = 0; phase ^= 1; }
+        }
+      }
+      if (!ok) {
+        // let this CTA's own copies land before the shared memory is released
+        for (int s = 0; s < STAGES; s++)
+          if (issued[s]) mbar_drain(&full[s], issued_phase[s]);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      bool ok = true;
+      bool any = false;
+      for (int p = 0; p < passes && ok; p++) {
+        const bool two = 2 * p + 1 < g.S;
+        if (!mbar_wait(tempty, (p & 1) ^ 1, abort_flag, g.err, 2)) { ok = false; break; }
+        tc_fence_after();
+        for (int kb = 0; kb < nk; kb++) {
+          if (!mbar_wait(&full[stage], phase, abort_flag, g.err, 3)) { ok = false; break; }
+          tc_fence_after();
+          uint8_t* sb = smem + stage * STAGE_BYTES;
+          const uint64_t a0 = desc_sw128(sb), a1 = desc_sw128(sb + A_TILE), b = desc_sw128(sb + 2 * A_TILE);
+#pragma unroll
+          for (int k = 0; k < BK / 16; k++) {
+            const uint64_t koff = (uint64_t)((k * 32) >> 4);
+            const uint32_t acc = (kb > 0 || k > 0) ? 1u : 0u;
+            mma_bf16(tbase, a0 + koff, b + koff, IDESC, acc);
+            if (two) mma_bf16(tbase + 256, a1 + koff, b + koff, IDESC, acc);
+          }
+          any = true;
+          mma_commit(&empty[stage]);
+          if (++stage == STAGES) { stage = 0; phase ^= 1; }
+        }
+        if (!ok) break;
+        mma_commit(tfull);
+      }
+      if (!ok && any) {
+        // all MMAs issued by this thread complete before TMEM is released
+        mma_commit(drain);
+        mbar_drain(drain, 0);
+      }
+    }
+    __syncwarp();
+  } else {
+    // epilogue: warps 2..5 -> TMEM lane quarter (warp % 4)
+    const int q = warp & 3;
+    const int row = q * 32 + lane;
+    const int r = m0 + row;
+    const bool rvalid = r < g.M;
+    const double scale = rvalid ? g.row_scale[r] : 0.0;
+    for (int p = 0; p < passes; p++) {
+      const bool two = 2 * p + 1 < g.S;
+      const bool last = p == passes - 1;
+      int ok = 1;
+      if (lane == 0) ok = mbar_wait(tfull, p & 1, abort_flag, g.err, 4) ? 1 : 0;
+      ok = __shfl_sync(0xffffffffu, ok, 0);  // warp-uniform: tcgen05.ld is .sync.aligned
+      if (!ok) break;
+      tc_fence_after();
+#pragma unroll 1
+      for (int ch = 0; ch < BN / 32; ch++) {
+        uint32_t v0[32], v1[32];
+        const uint32_t ta = tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)(ch * 32);
+        tmem_ld32(ta, v0);
+        if (two) tmem_ld32(ta + 256, v1);
+        tmem_ld_wait();
+        if (!rvalid) continue;
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+          const int col = n0 + ch * 32 + j;
+          if (col >= g.N) break;
+          int qv = __float2int_rn(__uint_as_float(v0[j])) * 256;
+          if (two) qv += __float2int_rn(__uint_as_float(v1[j]));
+          long long* cp = (long long*)(g.C + (long long)r + (long long)col * g.ldc);
+          long long V = (p == 0) ? (long long)qv : (*cp) * 65536LL + (long long)qv;
+          if (last)
+            *(double*)cp = (double)V * scale;
+          else
+            *cp = V;
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(tempty);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(512) : "memory");
+}
+
+// ---------------------------------------------------------------------------
+// Slicing: row r of A (K-contiguous source, element k at src[k + r*lds]) ->
+// S digit slices (BF16) at A[(s*Mpad + r)*Kpad + k], scale per row.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) slice_rows_kernel(int K, int rows, const double* __restrict__ src,
+                                                         long long lds, int row_off, int S, int Mpad, int Kpad,
+                                                         __nv_bfloat16* __restrict__ A, double* __restrict__ row_scale) {
+  const int r = blockIdx.x;
+  if (r >= rows) return;
+  const double* a = src + (long long)r * lds;
+  __shared__ double red[32];
+  double mx = 0.0;
+  for (int k = threadIdx.x; k < K; k += blockDim.x) mx = fmax(mx, fabs(a[k]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (threadIdx.x == 0) red[0] = v;
+  }
+  __syncthreads();
+  mx = red[0];
+  const int e = (mx > 0.0) ? ilogb(mx) + 1 : 0;  // max * 2^-e in [0.5, 1)
+  const int passes = (S + 1) / 2;
+  const int R = row_off + r;
+  if (threadIdx.x == 0) row_scale[R] = ldexp(1.0, e - 15 - 16 * (passes - 1));
+  for (int k = threadIdx.x; k < K; k += blockDim.x) {
+    double v = ldexp(a[k], 7 - e);  // |v| < 128
+#pragma unroll 1
+    for (int s = 0; s < S; s++) {
+      const double d = rint(v);
+      A[((long long)s * Mpad + R) * Kpad + k] = __double2bfloat16(d);  // |d| <= 128: exact
+      v = (v - d) * 256.0;
+    }
+  }
+}
+
+// genotypes (FP64 or bytes, column c at src[c*lds + k]) -> BF16 [c*Kpad + k]
+template <typename T>
+__global__ void genotypes_bf16_kernel(int K, int cols, const T* __restrict__ src, long long lds,
+                                      __nv_bfloat16* __restrict__ G, int Kpad) {
+  const long long total = (long long)cols * K;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(e % K);
+    const long long c = e / K;
+    G[c * Kpad + k] = __float2bfloat16((float)src[c * lds + k]);
+  }
+}
+
+__global__ void eye_kernel(int n, double* A) {
+  const long long total = (long long)n * n;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x)
+    A[e] = (e % n == e / n) ? 1.0 : 0.0;
+}
+
+// B = A^T for n x n column-major, 32 x 32 tiles through shared memory
+__global__ void transpose_kernel(int n, const double* __restrict__ A, double* __restrict__ B) {
+  __shared__ double tile[32][33];
+  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+  for (int j = threadIdx.y; j < 32; j += 8) {
+    const int r = bx + threadIdx.x, c = by + j;
+    if (r < n && c < n) tile[j][threadIdx.x] = A[r + (long long)c * n];
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += 8) {
+    const int r = by + threadIdx.x, c = bx + j;
+    if (r < n && c < n) B[r + (long long)c * n] = tile[threadIdx.x][j];
+  }
+}
+
+__global__ void fill_pairs_kernel(int count, float* hi, float* lo) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < count; e += gridDim.x * blockDim.x) {
+    hi[e] = 1.0f;
+    lo[e] = 0.0f;
+  }
+}
+
+// d (FP64, n x t) -> float pair (hi, lo)
+__global__ void split_pairs_kernel(long long count, const double* __restrict__ d, float* __restrict__ hi,
+                                   float* __restrict__ lo) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < count;
+       e += (long long)gridDim.x * blockDim.x) {
+    const double v = d[e];
+    const float h = (float)v;
+    hi[e] = h;
+    lo[e] = (float)(v - (double)h);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Quadratic Gram terms in double-FP32:  GR[i + j*x] = sum_l R[l,i]^2 * D[l,j]
+// with D = (Dh + Dl) float pairs.  Error-free products (fma) and sums
+// (TwoSum) keep ~2^-44 relative accuracy; all terms are non-negative so there
+// is no cancellation.  Tile 64 SNPs x 64 traits, 256 threads, 4 x 4 each.
+// ---------------------------------------------------------------------------
+constexpr int QG_I = 64, QG_J = 64, QG_L = 32;
+__global__ void __launch_bounds__(256) selfgram_kernel(int n, int x, int t, const double* __restrict__ R,
+                                                       long long ldr, const float* __restrict__ Dh,
+                                                       const float* __restrict__ Dl, long long ldd,
+                                                       double* __restrict__ GR, long long ldg) {
+  __shared__ float Ah[QG_L][QG_I + 1], Al[QG_L][QG_I + 1];
+  __shared__ float Bh[QG_L][QG_J + 1], Bl[QG_L][QG_J + 1];
+  const int i0 = blockIdx.x * QG_I, j0 = blockIdx.y * QG_J;
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  float sh[4][4], sl[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = 0; b < 4; b++) sh[a][b] = sl[a][b] = 0.0f;
+  for (int l0 = 0; l0 < n; l0 += QG_L) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < QG_L * QG_I; e += 256) {
+      const int l = e % QG_L, i = e / QG_L;
+      float h = 0.0f, lo = 0.0f;
+      if (l0 + l < n && i0 + i < x) {
+        const double r = R[(l0 + l) + (long long)(i0 + i) * ldr];
+        const float rh = (float)r;
+        const float rl = (float)(r - (double)rh);
+        h = rh * rh;
+        lo = fmaf(rh, rh, -h) + 2.0f * rh * rl;
+      }
+      Ah[l][i] = h;
+      Al[l][i] = lo;
+    }
+    for (int e = threadIdx.x; e < QG_L * QG_J; e += 256) {
+      const int l = e % QG_L, j = e / QG_L;
+      float h = 0.0f, lo = 0.0f;
+      if (l0 + l < n && j0 + j < t) {
+        h = Dh[(l0 + l) + (long long)(j0 + j) * ldd];
+        lo = Dl[(l0 + l) + (long long)(j0 + j) * ldd];
+      }
+      Bh[l][j] = h;
+      Bl[l][j] = lo;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int l = 0; l < QG_L; l++) {
+      float ah[4], al[4], bh[4], bl[4];
+#pragma unroll
+      for (int a = 0; a < 4; a++) {
+        ah[a] = Ah[l][ty + 16 * a];
+        al[a] = Al[l][ty + 16 * a];
+      }
+#pragma unroll
+      for (int b = 0; b < 4; b++) {
+        bh[b] = Bh[l][tx + 16 * b];
+        bl[b] = Bl[l][tx + 16 * b];
+      }
+#pragma unroll
+      for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+          const float p = ah[a] * bh[b];
+          const float pe = fmaf(ah[a], bh[b], -p);
+          const float low = fmaf(ah[a], bl[b], fmaf(al[a], bh[b], pe));
+          const float s = sh[a][b] + p;
+          const float bp = s - sh[a][b];
+          const float err = (sh[a][b] - (s - bp)) + (p - bp);
+          sh[a][b] = s;
+          sl[a][b] += err + low;
+        }
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+    const int i = i0 + ty + 16 * a;
+    if (i >= x) continue;
+#pragma unroll
+    for (int b = 0; b < 4; b++) {
+      const int j = j0 + tx + 16 * b;
+      if (j >= t) continue;
+      GR[i + (long long)j * ldg] = (double)sh[a][b] + (double)sl[a][b];
+    }
+  }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn get_encoder() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  }
+  return fn;
+}
+
+// 2D BF16 tensor map, K innermost, 128B swizzle, box {BK, box_rows}
+cudaError_t make_map(CUtensorMap* m, const void* base, long long K, long long rows, int box_rows) {
+  EncodeTiledFn enc = get_encoder();
+  if (!enc) return cudaErrorNotSupported;
+  cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)K * 2};
+  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+int grid_for(long long total) { return (int)std::min<long long>((total + 255) / 256, 152LL * 32); }
+
+}  // namespace oz
+
+using namespace oz;
+
+struct OzakiPlan {
+  int n = 0, t = 0, wXL = 0, wXR = 0, x_b = 0, S = 0;
+  int eigen = 0;
+  int nU = 0;           // U rows appended below the n rows of Z^T / L^-1
+  int M = 0, Mpad = 0;  // rows of A
+  int Kpad = 0, Ncap = 0;
+  __nv_bfloat16* A = nullptr;   // S x Mpad x Kpad
+  __nv_bfloat16* G = nullptr;   // Ncap x Kpad
+  double* scale = nullptr;      // Mpad
+  double* C = nullptr;          // Mpad x Ncap (ld Mpad)
+  double* U = nullptr;          // n x nU
+  float *Dh = nullptr, *Dl = nullptr;  // n x t (eigen weights; chol: ones)
+  double* Linv = nullptr;       // chol: n x n, L^-1
+  double* LinvT = nullptr;      // chol: n x n, (L^-1)^T (rows of L^-1 contiguous)
+  int* err = nullptr;
+  CUtensorMap mapA, mapB;
+  bool maps = false;
+};
+
+cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_b, int slices, int eigen) {
   *out = nullptr;
-  return cudaErrorNotSupported;
+  if (wXR != 1) return cudaErrorNotSupported;  // split path: one column per SNP
+  if (n > 16383) return cudaErrorNotSupported;  // exactness bound of the FP32 accumulation
+  OzakiPlan* p = new OzakiPlan();
+  p->n = n;
+  p->t = t;
+  p->wXL = wXL;
+  p->wXR = wXR;
+  p->x_b = x_b;
+  p->S = slices > 0 ? std::min(slices, MAX_SLICES) : 6;
+  p->eigen = eigen;
+  p->nU = eigen ? t * (1 + wXL) : (1 + wXL);
+  p->M = n + p->nU;
+  p->Mpad = (p->M + BM - 1) / BM * BM;
+  p->Kpad = (n + BK - 1) / BK * BK;
+  p->Ncap = (x_b + BN - 1) / BN * BN;
+  cudaError_t r = cudaSuccess;
+  auto chk = [&](cudaError_t e) {
+    if (r == cudaSuccess) r = e;
+  };
+  chk(cudaMalloc(&p->A, sizeof(__nv_bfloat16) * (size_t)p->S * p->Mpad * p->Kpad));
+  chk(cudaMalloc(&p->G, sizeof(__nv_bfloat16) * (size_t)p->Ncap * p->Kpad));
+  chk(cudaMalloc(&p->scale, sizeof(double) * p->Mpad));
+  chk(cudaMalloc(&p->C, sizeof(double) * (size_t)p->Mpad * p->Ncap));
+  chk(cudaMalloc(&p->U, sizeof(double) * (size_t)n * p->nU));
+  chk(cudaMalloc(&p->Dh, sizeof(float) * (size_t)n * t));
+  chk(cudaMalloc(&p->Dl, sizeof(float) * (size_t)n * t));
+  chk(cudaMalloc(&p->err, sizeof(int)));
+  if (!eigen) chk(cudaMalloc(&p->Linv, sizeof(double) * (size_t)n * n));
+  if (!eigen) chk(cudaMalloc(&p->LinvT, sizeof(double) * (size_t)n * n));
+  if (r == cudaSuccess) chk(cudaMemset(p->A, 0, sizeof(__nv_bfloat16) * (size_t)p->S * p->Mpad * p->Kpad));
+  if (r == cudaSuccess) chk(cudaMemset(p->G, 0, sizeof(__nv_bfloat16) * (size_t)p->Ncap * p->Kpad));
+  if (r == cudaSuccess) chk(cudaMemset(p->scale, 0, sizeof(double) * p->Mpad));
+  if (r == cudaSuccess) chk(cudaMemset(p->err, 0, sizeof(int)));
+  if (r == cudaSuccess) chk(make_map(&p->mapA, p->A, p->Kpad, (long long)p->S * p->Mpad, BM));
+  if (r == cudaSuccess) chk(make_map(&p->mapB, p->G, p->Kpad, p->Ncap, BN));
+  if (r == cudaSuccess) chk(cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 SMEM_BYTES));
+  if (r != cudaSuccess) {
+    ozaki_destroy(p);
+    return r;
+  }
+  p->maps = true;
+  *out = p;
+  return cudaSuccess;
 }
-void ozaki_destroy(OzakiPlan*) {}
-cudaError_t ozaki_set_eigen(OzakiPlan*, cudaStream_t, const double*, const double*, const double*) {
-  return cudaErrorNotSupported;
+
+void ozaki_destroy(OzakiPlan* p) {
+  if (!p) return;
+  void* ptrs[] = {p->A, p->G, p->scale, p->C, p->U, p->Dh, p->Dl, p->Linv, p->LinvT, p->err};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  delete p;
 }
-cudaError_t ozaki_set_chol(OzakiPlan*, cudaStream_t, const double*) { return cudaErrorNotSupported; }
-cudaError_t ozaki_eigen_block(OzakiPlan*, cudaStream_t, const double*, int, double*, double*) {
-  return cudaErrorNotSupported;
+
+namespace {
+
+cudaError_t slice_operands(OzakiPlan* p, cudaStream_t s, const double* top, long long ldtop, int toprows) {
+  // rows [0, toprows) from `top` (row r contiguous at top + r*ldtop), rows
+  // [n, n + nU) from the columns of U.
+  slice_rows_kernel<<<toprows, 256, 0, s>>>(p->n, toprows, top, ldtop, 0, p->S, p->Mpad, p->Kpad, p->A, p->scale);
+  note_launch();
+  slice_rows_kernel<<<p->nU, 256, 0, s>>>(p->n, p->nU, p->U, p->n, p->n, p->S, p->Mpad, p->Kpad, p->A, p->scale);
+  note_launch();
+  return cudaGetLastError();
 }
-cudaError_t ozaki_eigen_block_u8(OzakiPlan*, cudaStream_t, const unsigned char*, int, double*, double*) {
-  return cudaErrorNotSupported;
+
+cudaError_t run_gemm(OzakiPlan* p, cudaStream_t s, int x, int tri_rows) {
+  GemmArgs g;
+  g.M = p->M;
+  g.Mpad = p->Mpad;
+  g.N = x;
+  g.Kpad = p->Kpad;
+  g.S = p->S;
+  g.tiles_m = p->Mpad / BM;
+  g.tiles_n = (x + BN - 1) / BN;
+  g.tri_rows = tri_rows;
+  g.row_scale = p->scale;
+  g.C = p->C;
+  g.ldc = p->Mpad;
+  g.err = p->err;
+  ozaki_gemm_kernel<<<g.tiles_m * g.tiles_n, THREADS, SMEM_BYTES, s>>>(p->mapA, p->mapB, g);
+  note_launch();
+  return cudaGetLastError();
 }
-cudaError_t ozaki_chol_block(OzakiPlan*, cudaStream_t, const double*, int, double*) { return cudaErrorNotSupported; }
+
+template <typename T>
+cudaError_t load_genotypes(OzakiPlan* p, cudaStream_t s, const T* X, int x) {
+  genotypes_bf16_kernel<T><<<grid_for((long long)x * p->n), 256, 0, s>>>(p->n, x, X, p->n, p->G, p->Kpad);
+  note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t selfgram(OzakiPlan* p, cudaStream_t s, int x, int t, double* GR) {
+  dim3 grid((x + QG_I - 1) / QG_I, (t + QG_J - 1) / QG_J);
+  selfgram_kernel<<<grid, 256, 0, s>>>(p->n, x, t, p->C, p->Mpad, p->Dh, p->Dl, p->n, GR, x);
+  note_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t ozaki_set_eigen(OzakiPlan* p, cudaStream_t s, const double* Z, const double* AYL, const double* dinv) {
+  // U = Z * AYL (FP64, once per problem): x~^T y~_j = x^T U[:, j] etc.
+  FGLS_CUDA_TRY(dgemm(s, false, false, p->n, p->nU, p->n, 1.0, Z, p->n, AYL, p->n, 0.0, p->U, p->n));
+  // rows of Z^T are the columns of Z (contiguous): ld n
+  FGLS_CUDA_TRY(slice_operands(p, s, Z, p->n, p->n));
+  split_pairs_kernel<<<grid_for((long long)p->n * p->t), 256, 0, s>>>((long long)p->n * p->t, dinv, p->Dh, p->Dl);
+  note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t ozaki_set_chol(OzakiPlan* p, cudaStream_t s, const double* L, const double* WY) {
+  const int n = p->n;
+  // L^-1 by the FP64 blocked TRSM on the identity, then U = L^-T [y~ | XL~]
+  eye_kernel<<<grid_for((long long)n * n), 256, 0, s>>>(n, p->Linv);
+  note_launch();
+  FGLS_CUDA_TRY(dtrsm_llnn(s, n, n, L, n, p->Linv, n));
+  FGLS_CUDA_TRY(dgemm(s, true, false, n, p->nU, n, 1.0, p->Linv, n, WY, n, 0.0, p->U, n));
+  // rows of L^-1 contiguous: transpose, then slice
+  dim3 tg((n + 31) / 32, (n + 31) / 32);
+  transpose_kernel<<<tg, dim3(32, 8), 0, s>>>(n, p->Linv, p->LinvT);
+  note_launch();
+  FGLS_CUDA_TRY(slice_operands(p, s, p->LinvT, n, n));
+  // unit weights for the quadratic term |x~|^2
+  fill_pairs_kernel<<<grid_for(n), 256, 0, s>>>(n, p->Dh, p->Dl);
+  note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t ozaki_genotypes(OzakiPlan* p, cudaStream_t s, const double* X, int x) {
+  return load_genotypes<double>(p, s, X, x);
+}
+
+cudaError_t ozaki_genotypes_u8(OzakiPlan* p, cudaStream_t s, const unsigned char* X, int x) {
+  return load_genotypes<unsigned char>(p, s, X, x);
+}
+
+cudaError_t ozaki_product(OzakiPlan* p, cudaStream_t s, int x) {
+  return run_gemm(p, s, x, p->eigen ? 0 : p->n);
+}
+
+cudaError_t ozaki_selfgram(OzakiPlan* p, cudaStream_t s, int x, double* GR) {
+  return selfgram(p, s, x, p->eigen ? p->t : 1, GR);
+}
+
+double ozaki_flops_per_snp(const OzakiPlan* p) {
+  // sliced tensor-core MMA operations actually issued per genotype column
+  // (chol: the zero upper part of L^-1 is skipped by 64-column K blocks)
+  double rows_k = (double)p->M * p->n;
+  if (!p->eigen) rows_k = (double)p->nU * p->n + 0.5 * (double)p->n * p->n;
+  return 2.0 * p->S * rows_k;
+}
+
+// Gram operand view of the last block's output: rows [n, n + nU) of C.
+const double* ozaki_gram_rows(const OzakiPlan* p, long long* ld) {
+  *ld = p->Mpad;
+  return p->C + p->n;
+}
+
+int ozaki_read_error(OzakiPlan* p) {
+  int h = 0;
+  cudaMemcpy(&h, p->err, sizeof(int), cudaMemcpyDeviceToHost);
+  return h;
+}
+
 }  // namespace fgls
+
+// Self-test of the split-precision GEMM on caller data (host pointers):
+// C = A * X^T with A (M x K, row-major FP64) cut into S slices and X (K x N,
+// column-major, integer values in [0, 2]).  C is M x N column-major.
+extern "C" int fglsgpu_selftest_split_gemm(int M, int K, int N, int S, const double* A, const double* X,
+                                           double* C) {
+  using namespace fgls;
+  using namespace fgls::oz;
+  if (M <= 0 || K <= 0 || K > 16383 || N <= 0 || S < 1 || S > MAX_SLICES) return FGLSGPU_EINVAL;
+  OzakiPlan p;
+  p.n = K;
+  p.S = S;
+  p.M = M;
+  p.Mpad = (M + BM - 1) / BM * BM;
+  p.Kpad = (K + BK - 1) / BK * BK;
+  p.Ncap = (N + BN - 1) / BN * BN;
+  double *dA = nullptr, *dX = nullptr;
+  cudaError_t r = cudaSuccess;
+  auto chk = [&](cudaError_t e) {
+    if (r == cudaSuccess) r = e;
+  };
+  cudaStream_t s = nullptr;
+  chk(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  chk(cudaMalloc(&p.A, sizeof(__nv_bfloat16) * (size_t)S * p.Mpad * p.Kpad));
+  chk(cudaMalloc(&p.G, sizeof(__nv_bfloat16) * (size_t)p.Ncap * p.Kpad));
+  chk(cudaMalloc(&p.scale, sizeof(double) * p.Mpad));
+  chk(cudaMalloc(&p.C, sizeof(double) * (size_t)p.Mpad * p.Ncap));
+  chk(cudaMalloc(&p.err, sizeof(int)));
+  chk(cudaMalloc(&dA, sizeof(double) * (size_t)M * K));
+  chk(cudaMalloc(&dX, sizeof(double) * (size_t)K * N));
+  if (r == cudaSuccess) chk(cudaMemset(p.A, 0, sizeof(__nv_bfloat16) * (size_t)S * p.Mpad * p.Kpad));
+  if (r == cudaSuccess) chk(cudaMemset(p.G, 0, sizeof(__nv_bfloat16) * (size_t)p.Ncap * p.Kpad));
+  if (r == cudaSuccess) chk(cudaMemset(p.scale, 0, sizeof(double) * p.Mpad));
+  if (r == cudaSuccess) chk(cudaMemset(p.err, 0, sizeof(int)));
+  if (r == cudaSuccess) chk(cudaMemcpy(dA, A, sizeof(double) * (size_t)M * K, cudaMemcpyHostToDevice));
+  if (r == cudaSuccess) chk(cudaMemcpy(dX, X, sizeof(double) * (size_t)K * N, cudaMemcpyHostToDevice));
+  if (r == cudaSuccess) chk(make_map(&p.mapA, p.A, p.Kpad, (long long)S * p.Mpad, BM));
+  if (r == cudaSuccess) chk(make_map(&p.mapB, p.G, p.Kpad, p.Ncap, BN));
+  if (r == cudaSuccess)
+    chk(cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+  if (r == cudaSuccess) {
+    slice_rows_kernel<<<M, 256, 0, s>>>(K, M, dA, K, 0, S, p.Mpad, p.Kpad, p.A, p.scale);
+    chk(cudaGetLastError());
+  }
+  if (r == cudaSuccess) chk(load_genotypes<double>(&p, s, dX, N));
+  if (r == cudaSuccess) chk(run_gemm(&p, s, N, 0));
+  if (r == cudaSuccess) chk(cudaStreamSynchronize(s));
+  int herr = 0;
+  if (r == cudaSuccess) chk(cudaMemcpy(&herr, p.err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (r == cudaSuccess)
+    chk(cudaMemcpy2D(C, sizeof(double) * M, p.C, sizeof(double) * p.Mpad, sizeof(double) * M, N,
+                     cudaMemcpyDeviceToHost));
+  void* ptrs[] = {p.A, p.G, p.scale, p.C, p.err, dA, dX};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  p.A = nullptr; p.G = nullptr; p.scale = nullptr; p.C = nullptr; p.err = nullptr;
+  if (s) cudaStreamDestroy(s);
+  if (r != cudaSuccess) return FGLSGPU_ECUDA;
+  return herr ? FGLSGPU_ETIMEOUT : FGLSGPU_OK;
+}

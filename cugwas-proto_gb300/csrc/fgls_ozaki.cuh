@@ -16,13 +16,22 @@ cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_
 void ozaki_destroy(OzakiPlan* p);
 // eigen: Z (n x n), AYL (n x t(1+wXL)), dinv (n x t)
 cudaError_t ozaki_set_eigen(OzakiPlan* p, cudaStream_t s, const double* Z, const double* AYL, const double* dinv);
-// chol: L (n x n lower)
-cudaError_t ozaki_set_chol(OzakiPlan* p, cudaStream_t s, const double* L);
-// eigen block: genotypes (FP64 or u8, n x x*wXR) -> GYL, GR (Gram layout of fgls_snp.cu)
-cudaError_t ozaki_eigen_block(OzakiPlan* p, cudaStream_t s, const double* X, int x, double* GYL, double* GR);
-cudaError_t ozaki_eigen_block_u8(OzakiPlan* p, cudaStream_t s, const unsigned char* X, int x, double* GYL,
-                                 double* GR);
-// chol block: Xout = L^-1 X (FP64, n x x*wXR)
-cudaError_t ozaki_chol_block(OzakiPlan* p, cudaStream_t s, const double* X, int x, double* Xout);
+// chol: L (n x n lower), WY = [y~ | XL~] (n x (1+wXL)) of the selected trait
+cudaError_t ozaki_set_chol(OzakiPlan* p, cudaStream_t s, const double* L, const double* WY);
+// Per-block stages:
+//  1. genotypes (FP64 or bytes, n x x) -> BF16 operand
+cudaError_t ozaki_genotypes(OzakiPlan* p, cudaStream_t s, const double* X, int x);
+cudaError_t ozaki_genotypes_u8(OzakiPlan* p, cudaStream_t s, const unsigned char* X, int x);
+//  2. the tcgen05 split GEMM: C = [Z^T ; U^T] X  (chol: [L^-1 ; U^T] X)
+cudaError_t ozaki_product(OzakiPlan* p, cudaStream_t s, int x);
+//  3. quadratic Gram terms GR[i + j*x] = sum_l C[l,i]^2 d_j(l)  (chol: d = 1)
+cudaError_t ozaki_selfgram(OzakiPlan* p, cudaStream_t s, int x, double* GR);
+// sliced MMA operations per genotype column (2 * slices * rows * K)
+double ozaki_flops_per_snp(const OzakiPlan* p);
+
+// Rows [n, n + nU) of the last block's split GEMM output: the Gram terms
+// x~^T y~_j, x~^T XL~_j; element (SNP i, q) at ptr[q + i * ld].
+const double* ozaki_gram_rows(const OzakiPlan* p, long long* ld);
+int ozaki_read_error(OzakiPlan* p);
 
 }  // namespace fgls

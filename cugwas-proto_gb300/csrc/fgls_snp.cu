@@ -262,8 +262,8 @@ __global__ void quad_products_kernel(int n, int x, int wXR, const double* __rest
 // ---------------------------------------------------------------------------
 template <int P>
 __global__ void __launch_bounds__(128) snp_solve_kernel(
-    int x, int t, int wXL, const double* __restrict__ top, const double* __restrict__ GYL, long long ldg,
-    const double* __restrict__ GR, long long ldr, double* __restrict__ Bout, long long bstride,
+    int x, int t, int wXL, const double* __restrict__ top, const double* __restrict__ GYL, long long rsg,
+    long long ldg, const double* __restrict__ GR, long long ldr, double* __restrict__ Bout, long long bstride,
     double* __restrict__ Vout, long long vstride, DevStatus* st, long long snp_base) {
   extern __shared__ double stage[];  // [128][P + P*P]
   const int wXR = P - wXL;
@@ -282,8 +282,8 @@ __global__ void __launch_bounds__(128) snp_solve_kernel(
     }
     for (int c = 0; c < wXR; c++) {
       const long long row = (long long)i * wXR + c;
-      b[wXL + c] = GYL[row + (long long)j * ldg];
-      for (int k = 0; k < wXL; k++) S[wXL + c][k] = GYL[row + (long long)(t + j * wXL + k) * ldg];
+      b[wXL + c] = GYL[row * rsg + (long long)j * ldg];
+      for (int k = 0; k < wXL; k++) S[wXL + c][k] = GYL[row * rsg + (long long)(t + j * wXL + k) * ldg];
       for (int d = 0; d <= c; d++) S[wXL + c][wXL + d] = GR[row * wXR + d + (long long)j * ldr];
     }
   }
@@ -369,7 +369,7 @@ __global__ void __launch_bounds__(128) snp_solve_kernel(
 
 template <int P>
 cudaError_t launch_solve(cudaStream_t s, int x, int t, int wXL, const double* top, const double* GYL,
-                         long long ldg, const double* GR, long long ldr, double* B, long long bstride,
+                         long long rsg, long long ldg, const double* GR, long long ldr, double* B, long long bstride,
                          double* V, long long vstride, DevStatus* st, long long snp_base) {
   const size_t smem = sizeof(double) * 128 * (P + P * P);
   static bool attr = false;
@@ -378,7 +378,7 @@ cudaError_t launch_solve(cudaStream_t s, int x, int t, int wXL, const double* to
     attr = true;
   }
   dim3 grid(ceil_div(x, 128), t);
-  snp_solve_kernel<P><<<grid, 128, smem, s>>>(x, t, wXL, top, GYL, ldg, GR, ldr, B, bstride, V, vstride, st,
+  snp_solve_kernel<P><<<grid, 128, smem, s>>>(x, t, wXL, top, GYL, rsg, ldg, GR, ldr, B, bstride, V, vstride, st,
                                               snp_base);
   note_launch();
   return cudaGetLastError();
@@ -434,12 +434,12 @@ cudaError_t quad_products(cudaStream_t s, int n, int x, int wXR, const double* R
 }
 
 cudaError_t snp_solve(cudaStream_t s, int p, int x, int t, int wXL, const double* top, const double* GYL,
-                      long long ldg, const double* GR, long long ldr, double* B, long long bstride, double* V,
+                      long long rsg, long long ldg, const double* GR, long long ldr, double* B, long long bstride, double* V,
                       long long vstride, DevStatus* st, long long snp_base) {
   switch (p) {
 #define FGLS_P_CASE(P) \
   case P:              \
-    return launch_solve<P>(s, x, t, wXL, top, GYL, ldg, GR, ldr, B, bstride, V, vstride, st, snp_base);
+    return launch_solve<P>(s, x, t, wXL, top, GYL, rsg, ldg, GR, ldr, B, bstride, V, vstride, st, snp_base);
     FGLS_P_CASE(2)
     FGLS_P_CASE(3)
     FGLS_P_CASE(4)

@@ -36,7 +36,7 @@ EXPORTS = (
     "fglsgpu_set_problem", "fglsgpu_select_trait", "fglsgpu_run_block", "fglsgpu_run_snps",
     "fglsgpu_run_block_device", "fglsgpu_run_block_device_u8", "fglsgpu_sync",
     "fglsgpu_get_res_sigma", "fglsgpu_get_eigen", "fglsgpu_stream", "fglsgpu_launch_count",
-    "fglsgpu_last_error", "fglsgpu_version",
+    "fglsgpu_last_error", "fglsgpu_version", "fglsgpu_selftest_split_gemm",
 )
 
 
@@ -81,6 +81,7 @@ def lib():
     L.fglsgpu_last_error.argtypes = [P]
     L.fglsgpu_last_error.restype = C.c_char_p
     L.fglsgpu_version.restype = I
+    L.fglsgpu_selftest_split_gemm.argtypes = [I, I, I, I, P, P, P]
     _lib = L
     return L
 
@@ -189,6 +190,20 @@ class Engine:
 
     def __exit__(self, *a):
         self.close()
+
+
+def split_gemm_selftest(A, X, slices):
+    """C = A @ X (A M x K FP64, X K x N integer genotypes) through the
+    split-precision tensor-core GEMM."""
+    A = np.ascontiguousarray(A, dtype=np.float64)          # row-major M x K
+    X = np.asfortranarray(X, dtype=np.float64)             # column-major K x N
+    M, K = A.shape
+    N = X.shape[1]
+    C = np.empty((M, N), order="F")
+    rc = lib().fglsgpu_selftest_split_gemm(M, K, N, slices, _ptr(A), _ptr(X), _ptr(C))
+    if rc != OK:
+        raise FGLSError(rc, "split GEMM self-test failed")
+    return C
 
 
 def launch_count() -> int:

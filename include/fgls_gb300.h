@@ -144,6 +144,22 @@ int fglsgpu_get_res_sigma(fglsgpu_engine *e, double *out);
  * Phi computed by set_problem (eigen variant); either pointer may be NULL. */
 int fglsgpu_get_eigen(fglsgpu_engine *e, double *W, double *Z);
 
+/* Per-kernel-class device time, measured with CUDA events recorded on the
+ * engine's compute stream around each class of launches. */
+#define FGLSGPU_PROF_GENOTYPES 0  /* genotype widening / BF16 operand build     */
+#define FGLSGPU_PROF_SPLIT_GEMM 1 /* tcgen05 split-precision GEMM               */
+#define FGLSGPU_PROF_SELFGRAM 2   /* quadratic Gram terms (double-FP32)         */
+#define FGLSGPU_PROF_SOLVE 3      /* batched p x p solves + B/V emission        */
+#define FGLSGPU_PROF_FP64_GEMM 4  /* FP64 path: Z^T XR                          */
+#define FGLSGPU_PROF_TRSM 5       /* FP64 path: L^-1 XR                         */
+#define FGLSGPU_PROF_GRAM 6       /* FP64 path: Gram terms                      */
+#define FGLSGPU_PROF_CLASSES 8
+/* Turns timing on (enable != 0) or off and zeroes the accumulators. */
+int fglsgpu_profile(fglsgpu_engine *e, int enable);
+/* Milliseconds and number of timed sections per class (FGLSGPU_PROF_CLASSES
+ * entries each); waits for the recorded events. */
+int fglsgpu_profile_read(fglsgpu_engine *e, double *ms, long long *count);
+
 /* The CUDA stream the engine computes on (a cudaStream_t). */
 void *fglsgpu_stream(fglsgpu_engine *e);
 
@@ -156,6 +172,14 @@ const char *fglsgpu_last_error(const fglsgpu_engine *e);
 
 /* Library version, major*10000 + minor*100 + patch. */
 int fglsgpu_version(void);
+
+/* Diagnostic: runs the split-precision tensor-core GEMM used by
+ * FGLSGPU_PREC_SPLIT on caller data.  C = A * X^T with A M x K (row-major
+ * FP64, cut into `slices` BF16 slices, 1..6), X K x N (column-major, integer
+ * genotypes 0..2) and C M x N column-major, all host pointers; K <= 16383.
+ * No counterpart in the reference (its GEMMs are FP64 BLAS calls). */
+int fglsgpu_selftest_split_gemm(int M, int K, int N, int slices, const double *A, const double *X,
+                                double *C);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,75 @@
+"""Split-precision (BF16-slice tcgen05) path.
+
+* The raw split GEMM is bit-exact when A is representable in the chosen
+  number of 8-bit slices (this pins the exactness of FP32 accumulation of
+  integer slice products in TMEM, including sums near 2^22).
+* For general FP64 A, 6 slices give |error| <= 2^-44 * sum_k |A_rk| |X_kc|.
+* The split eigen path matches the FP64 oracle: beta relative error <= 1e-10
+  (normwise per trait and SNP, and on the SE scale), SE <= 1e-10.
+"""
+import numpy as np
+import pytest
+
+from oracle import fgls_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _exact_product(Aint, shift, X):
+    # A = Aint * 2^-shift exactly; product exact in int64 then scaled
+    P = Aint.astype(np.int64) @ X.astype(np.int64)
+    return np.ldexp(P.astype(np.float64), -shift)
+
+
+@pytest.mark.parametrize("M,K,N,S,bits", [(259, 1000, 300, 2, 15), (128, 64, 256, 1, 7), (300, 4097, 513, 3, 23)])
+def test_split_gemm_exact_when_representable(M, K, N, S, bits):
+    from fgls_gb300.engine import split_gemm_selftest
+    rng = np.random.default_rng(M + K)
+    Aint = rng.integers(-(2 ** bits) + 1, 2 ** bits, size=(M, K))
+    Aint[:, 0] = 2 ** bits - 1  # every row uses its full exponent range
+    X = rng.integers(0, 3, size=(K, N))
+    A = np.ldexp(Aint.astype(np.float64), -bits)
+    C = split_gemm_selftest(A, X, S)
+    assert np.array_equal(C, _exact_product(Aint, bits, X))
+
+
+def test_split_gemm_exact_at_accumulator_limit():
+    """Slice products near 2^22 (K = 16000, digits of magnitude 127-128,
+    genotypes 2) must still be exact."""
+    from fgls_gb300.engine import split_gemm_selftest
+    K, M, N = 16000, 128, 256
+    rng = np.random.default_rng(1)
+    Aint = np.where(rng.random((M, K)) < 0.5, -32767, 32767).astype(np.int64)
+    Aint[:64] = 32767    # same-sign rows: |slice product| = 128 * 2 * 16000 ~ 2^22
+    Aint[64:96] = -32767
+    Aint[:, 0] = 32767
+    X = np.full((K, N), 2)
+    X[:, 1::2] = rng.integers(0, 3, size=(K, N // 2))
+    C = split_gemm_selftest(np.ldexp(Aint.astype(np.float64), -15), X, 2)
+    assert np.array_equal(C, _exact_product(Aint, 15, X))
+
+
+def test_split_gemm_fp64_accuracy():
+    from fgls_gb300.engine import split_gemm_selftest
+    rng = np.random.default_rng(7)
+    M, K, N = 300, 2000, 700
+    A = rng.standard_normal((M, K)) * np.exp(rng.uniform(-5, 5, size=(M, 1)))
+    X = rng.integers(0, 3, size=(K, N)).astype(np.float64)
+    C = split_gemm_selftest(A, X, 6)
+    ref = A @ X
+    bound = np.abs(A) @ np.abs(X)
+    assert np.all(np.abs(C - ref) <= 2.0 ** -44 * bound + 1e-300)
+
+
+@pytest.mark.parametrize("n,m,t,xb", [(300, 700, 5, 256), (1000, 1100, 16, 512)])
+def test_split_eigen_vs_oracle(n, m, t, xb):
+    from fgls_gb300 import Engine, datagen
+    pb = datagen.make_problem(n, m, t, seed=n + t, hsig_uniform=True)
+    with Engine(n, 3, 1, t, xb, variant="eigen", precision="split", slices=6) as e:
+        e.set_problem(pb.Phi, pb.XL, pb.Y, pb.h, pb.sigma)
+        B, V = e.run_snps(pb.XR)
+    Br, Vr = O.fgls_eigen(pb)
+    d = O.compare(B, V, Br, Vr)
+    assert d["finite"] and d["upper_abs_max"] == 0.0
+    assert d["beta_se_scaled"] <= 1e-10, d
+    assert d["se_rel"] <= 1e-10, d
