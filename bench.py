@@ -1,0 +1,428 @@
+#!/usr/bin/env python3
+"""Headline benchmark: SNP x trait tests/s of the FGLS eigen association on
+one GB300 with the split-precision tensor-core path, beside the all-FP64
+device path and the CPU restatement of the reference.
+
+Workload (synthetic, seeded): n = 10,000 individuals, p = 4 (intercept + 2
+N(0,1) covariates + 1 SNP), t = 100 traits with h ~ U(0.1, 0.9),
+sigma ~ U(0.5, 2), kinship Phi = G G^T / 5000 + 1e-3 I, hard-call genotypes
+Binomial(2, f), f ~ U(0.05, 0.5).  The job is m = 1,000,000 SNPs; a step is
+one block of x_b SNPs x t traits through the hot path (genotype operand
+build, split GEMM, quadratic Gram, batched p x p solves, B/V emission).
+The one-off setup (device eigendecomposition of Phi, Z^T XL, Z^T Y, null
+models, slicing of [Z^T ; U^T]) is outside the timed region and reported as
+setup_s.  Every step reads a different resident genotype block of 1.3 GB
+(FP64, the reference's XR layout): inputs larger than L2.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "cugwas-proto_gb300"))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "SNP×trait tests/s on 1 GB300, split-prec vs FP64 path, β rel-err ≤1e-10"
+UNIT = "tests/s"
+N_IND, T_TRAITS, WXL, WXR, M_JOB = 10000, 100, 3, 1, 1_000_000
+FALLBACK_PEAKS = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d, "measured"
+    return dict(FALLBACK_PEAKS), "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the
+    timed region (our own child process, stopped by PID)."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id):
+        self.gpu_id = gpu_id
+        self.lines = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", self.gpu_id, f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.th = threading.Thread(target=self._read, daemon=True)
+        self.th.start()
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.th.join(timeout=2)
+        sm, mx, pw, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+                pw.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "power_w_max": max(pw) if pw else None, "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def make_problem_gpu(n, t, seed, dev):
+    """Phi, XL, Y, h, sigma (host numpy) drawn on the device (torch is the
+    data generator only)."""
+    import torch
+    g = torch.Generator(device=dev).manual_seed(seed)
+    k = 5000
+    f = torch.rand(k, generator=g, device=dev, dtype=torch.float64) * 0.45 + 0.05
+    G = ((torch.rand(n, k, generator=g, device=dev, dtype=torch.float64) < f).double()
+         + (torch.rand(n, k, generator=g, device=dev, dtype=torch.float64) < f).double())
+    G = (G - G.mean(0)) / G.std(0, unbiased=False).clamp_min(1e-12)
+    Phi = G @ G.T / k
+    Phi.diagonal().add_(1e-3)
+    h = torch.rand(t, generator=g, device=dev, dtype=torch.float64) * 0.8 + 0.1
+    s = torch.rand(t, generator=g, device=dev, dtype=torch.float64) * 1.5 + 0.5
+    XL = torch.ones(n, WXL, device=dev, dtype=torch.float64)
+    XL[:, 1:] = torch.randn(n, WXL - 1, generator=g, device=dev, dtype=torch.float64)
+    u = torch.randn(k, t, generator=g, device=dev, dtype=torch.float64)
+    v = torch.randn(n, t, generator=g, device=dev, dtype=torch.float64)
+    Y = (G @ u) / k ** 0.5 * torch.sqrt(h * s) + v * torch.sqrt(h * s * 1e-3 + (1 - h) * s)
+    out = [x.cpu().numpy() for x in (Phi, XL, Y, h, s)]
+    del G, Phi
+    torch.cuda.empty_cache()
+    return out
+
+
+def genotype_block(x, n, seed, dev):
+    """x SNPs of hard calls 0/1/2 as a (x, n) FP64 tensor = column-major n x x."""
+    import torch
+    g = torch.Generator(device=dev).manual_seed(seed)
+    f = torch.rand(x, 1, generator=g, device=dev) * 0.45 + 0.05
+    X = (torch.rand(x, n, generator=g, device=dev) < f).to(torch.uint8)
+    X += (torch.rand(x, n, generator=g, device=dev) < f).to(torch.uint8)
+    return X.double()
+
+
+def rel_errors(B, V, Br, Vr):
+    """beta error normwise per (trait, SNP) and on the SE scale; SE element-wise."""
+    p = B.shape[-1]
+    idx = np.arange(p)
+    se_r = Vr[..., idx, idx]
+    nb = np.linalg.norm(B - Br, axis=-1) / np.linalg.norm(Br, axis=-1)
+    bs = np.abs(B - Br) / (np.abs(Br) + se_r)
+    se = np.abs(V[..., idx, idx] - se_r) / se_r
+    return float(nb.max()), float(bs.max()), float(se.max())
+
+
+def cpu_port_throughput(Z, W, XL, Y, h, s, X_host, budget_s, min_reps=1, steps=None):
+    """The oracle's restatement of the reference's per-block eigen loop on the
+    host cores: tests/s over a bounded SNP sample.  Only this leg imports
+    oracle/ (the checker), and only to time it."""
+    from oracle import fgls_oracle as O
+    st = O.eigen_setup(Z, W, XL, Y, h, s, WXL)
+    x = X_host.shape[1]
+    times = []
+    if steps is None:
+        t0 = time.perf_counter()
+        while True:
+            a = time.perf_counter()
+            O.eigen_block(st, X_host, WXR)
+            times.append(time.perf_counter() - a)
+            if len(times) >= min_reps and time.perf_counter() - t0 > budget_s:
+                break
+    else:
+        w, k = steps
+        for _ in range(w):
+            O.eigen_block(st, X_host, WXR)
+        for _ in range(k):
+            a = time.perf_counter()
+            O.eigen_block(st, X_host, WXR)
+            times.append(time.perf_counter() - a)
+    tot = sum(times)
+    return len(times) * x * Y.shape[1] / tot, tot / len(times), len(times)
+
+
+def orthogonal_basis(n, seed):
+    """Dense orthogonal n x n matrix (three Householder reflectors), used by
+    the reference arm where no device eigensolver may run."""
+    rng = np.random.default_rng(seed)
+    Z = np.eye(n)
+    for _ in range(3):
+        v = rng.standard_normal(n)
+        v /= np.linalg.norm(v)
+        Z -= 2.0 * np.outer(v, v @ Z)
+    return Z
+
+
+def run_reference(args, rank, world):
+    """The reference's CPU algorithm (oracle restatement of fgls_eigen's
+    per-block loop, src/fgls_eigen.c:471-565) on the host cores."""
+    if rank != 0:
+        return
+    from oracle import fgls_oracle  # noqa: F401  (checker; timed here as the reference arm)
+    n, t = args.n, args.t
+    rng = np.random.default_rng(7)
+    xs = args.ref_snps
+    W = np.sort(rng.uniform(1e-3, 6.0, size=n))
+    Z = orthogonal_basis(n, 7)
+    XL = np.ones((n, WXL))
+    XL[:, 1:] = rng.standard_normal((n, WXL - 1))
+    Y = rng.standard_normal((n, t))
+    h = rng.uniform(0.1, 0.9, t)
+    s = rng.uniform(0.5, 2.0, t)
+    f = rng.uniform(0.05, 0.5, xs)
+    X = rng.binomial(2, f, size=(n, xs)).astype(np.float64)
+    val, sec, reps = cpu_port_throughput(Z, W, XL, Y, h, s, X, 0, steps=(args.warmup, args.steps))
+    cores = os.cpu_count()
+    sample = f"{xs} SNPs x {t} traits per step at n={n}: Z^T XR block + per-trait rescale + per-SNP solves"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"fgls_eigen per-block loop, n={n} p=4 t={t}, CPU restatement", "n": n, "t": t,
+                   "p": 4, "snps_per_step": xs},
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_IND)
+    ap.add_argument("--t", type=int, default=T_TRAITS)
+    ap.add_argument("--xb", type=int, default=16384)
+    ap.add_argument("--slices", type=int, default=6)
+    ap.add_argument("--pool", type=int, default=4)
+    ap.add_argument("--e2e-blocks", type=int, default=4)
+    ap.add_argument("--fp64-snps", type=int, default=2048)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--ref-snps", type=int, default=128)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from fgls_gb300 import Engine, launch_count
+
+    n, t, xb, p = args.n, args.t, args.xb, WXL + WXR
+    pk, pk_kind = peaks()
+    t0 = time.perf_counter()
+    Phi, XL, Y, h, s = make_problem_gpu(n, t, 1234, dev)
+    gen_s = time.perf_counter() - t0
+    eng = Engine(n, WXL, WXR, t, xb, variant="eigen", precision="split", slices=args.slices, device=local)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    eng.set_problem(Phi, XL, Y, h, s)
+    setup_s = time.perf_counter() - t0
+    log(f"[bench] rank {rank}: data {gen_s:.1f}s, setup (eigendecomposition + operands) {setup_s:.1f}s")
+
+    pool = [genotype_block(xb, n, 100 + rank * 1000 + i, dev) for i in range(args.pool)]
+    dB = torch.empty(t * xb * p, dtype=torch.float64, device=dev)
+    dV = torch.empty(t * xb * p * p, dtype=torch.float64, device=dev)
+    stream = torch.cuda.ExternalStream(eng.stream(), device=dev)
+
+    def step(k):
+        eng.run_block_device(pool[k % len(pool)].data_ptr(), xb, dB.data_ptr(), dV.data_ptr(), xb * p, xb * p * p)
+
+    for k in range(args.warmup):
+        step(k)
+    eng.sync()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    uuid = "GPU-" + str(torch.cuda.get_device_properties(local).uuid)
+    sampler = ClockSampler(uuid)
+    eng.profile(True)
+    l0 = launch_count()
+    sampler.start()
+    time.sleep(0.3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for k in range(args.steps):
+        step(args.warmup + k)
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = sampler.stop()
+    launches = launch_count() - l0
+    ms = e0.elapsed_time(e1)
+    eng.sync()
+    prof = eng.profile_read()
+    eng.profile(False)
+    if dist:
+        tt = torch.tensor([ms], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    tests = world * args.steps * xb * t
+    value = tests / (ms / 1e3)
+
+    # roofline of the dominant kernel: the tcgen05 split GEMM
+    M_A = n + t * (1 + WXL)
+    flops_launch = 2.0 * args.slices * M_A * n * xb  # sliced BF16 MMA operations per launch
+    gemm_ms, gemm_n = prof["split_gemm"]
+    gemm_ms_launch = gemm_ms / max(gemm_n, 1)
+    achieved = flops_launch / (gemm_ms_launch / 1e3) / 1e12
+    peak = float(pk.get("bf16_tflops_sustained", FALLBACK_PEAKS["bf16_tflops_sustained"]))
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "split_gemm_traffic.json")
+    if os.path.exists(tf):
+        try:
+            tj = json.load(open(tf))
+            traffic = float(tj["dram_bytes_per_snp"]) * xb
+        except Exception:
+            traffic = None
+
+    # all-FP64 device path on the same problem (same eigendecomposition)
+    eng.set_precision("fp64")
+    x64 = min(args.fp64_snps, xb)
+    Xp = pool[0][:x64].contiguous()
+    dB64 = torch.empty(t * x64 * p, dtype=torch.float64, device=dev)
+    dV64 = torch.empty(t * x64 * p * p, dtype=torch.float64, device=dev)
+    eng.run_block_device(Xp.data_ptr(), x64, dB64.data_ptr(), dV64.data_ptr(), x64 * p, x64 * p * p)
+    eng.sync()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    reps64 = 2
+    for _ in range(reps64):
+        eng.run_block_device(Xp.data_ptr(), x64, dB64.data_ptr(), dV64.data_ptr(), x64 * p, x64 * p * p)
+    f1.record(stream)
+    f1.synchronize()
+    eng.sync()
+    fp64_value = reps64 * x64 * t / (f0.elapsed_time(f1) / 1e3)
+    B64 = dB64.cpu().numpy().reshape(t, x64, p)
+    V64 = dV64.cpu().numpy().reshape(t, x64, p, p).transpose(0, 1, 3, 2)
+    eng.set_precision("split")
+    dBs = torch.empty_like(dB64)
+    dVs = torch.empty_like(dV64)
+    eng.run_block_device(Xp.data_ptr(), x64, dBs.data_ptr(), dVs.data_ptr(), x64 * p, x64 * p * p)
+    eng.sync()
+    Bs = dBs.cpu().numpy().reshape(t, x64, p)
+    Vs = dVs.cpu().numpy().reshape(t, x64, p, p).transpose(0, 1, 3, 2)
+    nb, bs, se = rel_errors(Bs, Vs, B64, V64)
+
+    # end to end through the public host API: pinned host genotypes in the
+    # reference XR layout, results back in the B.out / V.out layout
+    E = args.e2e_blocks
+    Xh = torch.empty((E * xb, n), dtype=torch.float64, pin_memory=True)
+    for i in range(E):
+        Xh[i * xb:(i + 1) * xb].copy_(pool[i % len(pool)])
+    Bh = torch.empty(t * E * xb * p, dtype=torch.float64, pin_memory=True)
+    Vh = torch.empty(t * E * xb * p * p, dtype=torch.float64, pin_memory=True)
+    eng.run_snps_ptr(Xh.data_ptr(), xb, Bh.data_ptr(), Vh.data_ptr())  # warm
+    if dist:
+        dist.barrier()
+    a = time.perf_counter()
+    eng.run_snps_ptr(Xh.data_ptr(), E * xb, Bh.data_ptr(), Vh.data_ptr())
+    e2e_s = time.perf_counter() - a
+    if dist:
+        tt = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    e2e_value = world * E * xb * t / e2e_s
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        W, Z = eng.eigen()
+        xs = 256
+        Xc = pool[0][:xs].cpu().numpy().T.copy()
+        cv, csec, creps = cpu_port_throughput(Z, W, XL, Y, h, s, Xc, args.cpu_seconds)
+        cpu = {"value": cv, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{creps} x ({xs} SNPs x {t} traits) at n={n}, oracle restatement of the reference's "
+                         f"per-block eigen loop (numpy/OpenBLAS, all host threads), {creps * csec:.1f} s"}
+    eng.close()
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+        "config": {
+            "workload": f"fgls_eigen split-precision, n={n} p=4 t={t}, job m={M_JOB} SNPs, "
+                        f"steps of x_b={xb} SNPs x {t} traits",
+            "n": n, "t": t, "p": 4, "m_job": M_JOB, "x_b": xb, "slices": args.slices,
+            "genotype_input": "FP64 reference layout, resident in HBM",
+            "l2": f"inputs larger than L2: {len(pool)} distinct {xb * n * 8 / 1e9:.2f} GB blocks cycled",
+            "setup_s": setup_s, "job_s_estimate": M_JOB * t / value + setup_s,
+            "fp64_path": {"value": fp64_value, "unit": UNIT, "snps": x64,
+                          "speedup_split_vs_fp64": value / fp64_value},
+            "split_vs_fp64_error": {"beta_normwise": nb, "beta_se_scaled": bs, "se_rel": se,
+                                    "snps": x64, "traits": t},
+            "kernel_ms": {k: v[0] for k, v in prof.items() if v[1]},
+        },
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "ozaki_gemm_kernel", "peak_source": f"{pk_kind} bf16_tflops_sustained",
+                     "work": f"2*{args.slices} slices*{M_A} rows*{n} K*{xb} SNPs per launch"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": xb * n * 8,
+                "d2h_bytes_per_step": t * xb * (p + p * p) * 8,
+                "api": "fglsgpu_run_snps (host pinned FP64 XR -> host B/V)", "blocks": E},
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

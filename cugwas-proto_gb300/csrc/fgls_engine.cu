@@ -530,6 +530,29 @@ int fglsgpu_run_snps(fglsgpu_engine* e, const double* XR, long long m, double* B
   return check_status(e, "block");
 }
 
+int fglsgpu_set_precision(fglsgpu_engine* e, int precision) {
+  if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
+  if (precision != FGLSGPU_PREC_FP64 && precision != FGLSGPU_PREC_SPLIT)
+    return fail(e, FGLSGPU_EINVAL, "unknown precision %d", precision);
+  fglsgpu_config& c = e->cfg;
+  if (precision == c.precision) return FGLSGPU_OK;
+  ENG_TRY(e, cudaSetDevice(c.device), "cudaSetDevice");
+  ENG_TRY(e, cudaStreamSynchronize(e->comp), "set_precision");
+  const long long n = c.n, xb = c.x_b, wXR = c.wXR;
+  if (precision == FGLSGPU_PREC_FP64 && c.variant == FGLSGPU_VARIANT_EIGEN) {
+    if (!e->dWork) ENG_TRY(e, dalloc(&e->dWork, n * xb * wXR), "FP64 buffers");
+    if (!e->dQ) ENG_TRY(e, dalloc(&e->dQ, n * xb * wXR * wXR), "FP64 buffers");
+  }
+  c.precision = precision;
+  if (precision == FGLSGPU_PREC_SPLIT && e->problem_set && c.variant == FGLSGPU_VARIANT_EIGEN) {
+    if (!e->oz) ENG_TRY(e, ozaki_create(&e->oz, c.n, c.t, c.wXL, c.wXR, c.x_b, c.slices, 1), "split plan");
+    ENG_TRY(e, ozaki_set_eigen(e->oz, e->comp, e->dZ, e->dAYL, e->ddinv), "split operands");
+    ENG_TRY(e, cudaStreamSynchronize(e->comp), "split operands");
+  }
+  if (c.variant == FGLSGPU_VARIANT_CHOL) e->trait_sel = -1;  // re-select: the operands differ per path
+  return FGLSGPU_OK;
+}
+
 int fglsgpu_profile(fglsgpu_engine* e, int enable) {
   if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
   ENG_TRY(e, cudaSetDevice(e->cfg.device), "cudaSetDevice");

@@ -36,8 +36,10 @@ EXPORTS = (
     "fglsgpu_set_problem", "fglsgpu_select_trait", "fglsgpu_run_block", "fglsgpu_run_snps",
     "fglsgpu_run_block_device", "fglsgpu_run_block_device_u8", "fglsgpu_sync",
     "fglsgpu_get_res_sigma", "fglsgpu_get_eigen", "fglsgpu_stream", "fglsgpu_launch_count",
-    "fglsgpu_last_error", "fglsgpu_version", "fglsgpu_selftest_split_gemm",
+    "fglsgpu_last_error", "fglsgpu_version", "fglsgpu_selftest_split_gemm", "fglsgpu_set_precision",
+    "fglsgpu_profile", "fglsgpu_profile_read",
 )
+PROF_CLASSES = ("genotypes", "split_gemm", "selfgram", "solve", "fp64_gemm", "trsm", "gram", "spare")
 
 
 class FGLSError(RuntimeError):
@@ -82,6 +84,9 @@ def lib():
     L.fglsgpu_last_error.restype = C.c_char_p
     L.fglsgpu_version.restype = I
     L.fglsgpu_selftest_split_gemm.argtypes = [I, I, I, I, P, P, P]
+    L.fglsgpu_set_precision.argtypes = [P, I]
+    L.fglsgpu_profile.argtypes = [P, I]
+    L.fglsgpu_profile_read.argtypes = [P, P, P]
     _lib = L
     return L
 
@@ -156,6 +161,19 @@ class Engine:
         f = self.L.fglsgpu_run_block_device_u8 if u8 else self.L.fglsgpu_run_block_device
         self._check(f(self._h, C.c_void_p(xr_ptr), int(x), C.c_void_p(b_ptr), C.c_void_p(v_ptr),
                       int(bstride), int(vstride)))
+
+    def set_precision(self, precision):
+        self._check(self.L.fglsgpu_set_precision(self._h, PRECISION[precision]))
+
+    def profile(self, enable=True):
+        self._check(self.L.fglsgpu_profile(self._h, 1 if enable else 0))
+
+    def profile_read(self):
+        """{class: (milliseconds, sections)} of device time since profile()."""
+        ms = np.zeros(len(PROF_CLASSES))
+        cnt = np.zeros(len(PROF_CLASSES), dtype=np.int64)
+        self._check(self.L.fglsgpu_profile_read(self._h, _ptr(ms), _ptr(cnt)))
+        return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(PROF_CLASSES)}
 
     def sync(self):
         self._check(self.L.fglsgpu_sync(self._h))

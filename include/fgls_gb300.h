@@ -144,6 +144,11 @@ int fglsgpu_get_res_sigma(fglsgpu_engine *e, double *out);
  * Phi computed by set_problem (eigen variant); either pointer may be NULL. */
 int fglsgpu_get_eigen(fglsgpu_engine *e, double *W, double *Z);
 
+/* Switches a live engine between FGLSGPU_PREC_FP64 and FGLSGPU_PREC_SPLIT
+ * without redoing set_problem (eigen keeps its eigendecomposition; chol
+ * needs select_trait again). */
+int fglsgpu_set_precision(fglsgpu_engine *e, int precision);
+
 /* Per-kernel-class device time, measured with CUDA events recorded on the
  * engine's compute stream around each class of launches. */
 #define FGLSGPU_PROF_GENOTYPES 0  /* genotype widening / BF16 operand build     */

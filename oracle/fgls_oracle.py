@@ -157,6 +157,39 @@ def fgls_eigen(pb, W=None, Z=None):
     return B, V
 
 
+def eigen_setup(Z, W, XL, Y, h, sigma, wXL):
+    """Per-problem state of the eigen variant given the basis (Z, W):
+    src/fgls_eigen.c:720-796 (Z^T XL, Z^T Y) and :998-1195 (res_sigma)."""
+    ZtXL = Z.T @ XL
+    ZtY = Z.T @ Y
+    rs = residual_sigma_eigen(Z, W, XL, ZtXL, Y, ZtY, h, sigma, wXL)
+    return {"Z": Z, "W": W, "ZtXL": ZtXL, "ZtY": ZtY, "rs": rs, "h": h, "sigma": sigma, "wXL": wXL}
+
+
+def eigen_block(st, XR_blk, wXR=1):
+    """One SNP block of fgls_eigen for all traits, as the reference's
+    ooc_loops does it: Z^T XR_blk (src/fgls_eigen.c:962), then per trait the
+    Winv rescale of the whole block (:505-507) and the per-SNP Gram and solve
+    (:512-565).  Returns B (t, x, p), V (t, x, p, p)."""
+    Z, W, wXL = st["Z"], st["W"], st["wXL"]
+    ZtXR = Z.T @ XR_blk
+    t = st["ZtY"].shape[1]
+    Bs, Vs = [], []
+    for j in range(t):
+        a = st["sigma"][j] * st["h"][j]
+        b = st["sigma"][j] * (1.0 - st["h"][j])
+        Winv = np.sqrt(1.0 / (a * W + b))
+        yc = st["ZtY"][:, j] * Winv
+        XLc = st["ZtXL"] * Winv[:, None]
+        B_t = XLc.T @ yc
+        V_tl = XLc.T @ XLc
+        Xc = ZtXR * Winv[:, None]
+        bb, vv = snp_solve(B_t, V_tl, XLc, yc, Xc, wXL, wXR, st["rs"][j])
+        Bs.append(bb)
+        Vs.append(vv)
+    return np.stack(Bs), np.stack(Vs)
+
+
 # ---------------------------------------------------------------------------
 # Comparators.  Element-wise relative error on beta is ill-posed for
 # coefficients near zero (the reference's own chol and eigen variants differ

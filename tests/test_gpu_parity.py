@@ -158,3 +158,20 @@ def test_u8_genotypes_match_fp64():
         e.sync()
     B2 = dB.cpu().numpy().reshape(2, 48, 4)
     assert np.array_equal(B, B2)
+
+
+def test_cli_driver_reference_interface():
+    """fgls-driver <variant> <dir> <nrep> with 'n p m t wXL x_b y_b threads' on
+    stdin (the reference's src/driver.c interface) writes dir/B.out, V.out."""
+    import subprocess
+    from fgls_gb300 import DRIVER_PATH, datagen
+    name = "chol_n128_m200_t2"
+    pb, var, xb, Bref, Vref = load_golden(name)
+    d = tempfile.mkdtemp()
+    datagen.write_problem(pb, d)
+    stdin = f"{pb.n}\n{pb.p}\n{pb.m}\n{pb.t}\n{pb.wXL}\n{xb}\n1\n2\n"
+    r = subprocess.run([DRIVER_PATH, "c", d, "2"], input=stdin, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.strip().isdigit()  # mean ms per repetition
+    B, V = datagen.read_outputs(d, pb.m, pb.t, pb.p)
+    check(O.compare(B, V, Bref, Vref), CHOL_TOL)

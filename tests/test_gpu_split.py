@@ -73,3 +73,52 @@ def test_split_eigen_vs_oracle(n, m, t, xb):
     assert d["finite"] and d["upper_abs_max"] == 0.0
     assert d["beta_se_scaled"] <= 1e-10, d
     assert d["se_rel"] <= 1e-10, d
+
+
+@pytest.mark.parametrize("n,m,t,xb", [(300, 500, 2, 256), (700, 300, 1, 300)])
+def test_split_chol_vs_oracle(n, m, t, xb):
+    from fgls_gb300 import Engine, datagen
+    pb = datagen.make_problem(n, m, t, seed=n + 3, hsig_uniform=True)
+    Bs, Vs = [], []
+    with Engine(n, 3, 1, t, xb, variant="chol", precision="split", slices=6) as e:
+        e.set_problem(pb.Phi, pb.XL, pb.Y, pb.h, pb.sigma)
+        for j in range(t):
+            e.select_trait(j)
+            B, V = e.run_snps(pb.XR)
+            Bs.append(B[0])
+            Vs.append(V[0])
+    Br, Vr = O.fgls_chol(pb, xb)
+    d = O.compare(np.stack(Bs), np.stack(Vs), Br, Vr)
+    assert d["finite"] and d["upper_abs_max"] == 0.0
+    assert d["beta_se_scaled"] <= 1e-10 and d["beta_normwise"] <= 1e-9, d
+    assert d["se_rel"] <= 1e-10, d
+
+
+def test_precision_switch_keeps_eigendecomposition():
+    from fgls_gb300 import Engine, datagen
+    pb = datagen.make_problem(400, 300, 4, seed=5, hsig_uniform=True)
+    with Engine(400, 3, 1, 4, 128, variant="eigen", precision="split") as e:
+        e.set_problem(pb.Phi, pb.XL, pb.Y, pb.h, pb.sigma)
+        B1, V1 = e.run_snps(pb.XR)
+        e.set_precision("fp64")
+        B2, V2 = e.run_snps(pb.XR)
+        e.set_precision("split")
+        B3, V3 = e.run_snps(pb.XR)
+    assert np.array_equal(B1, B3) and np.array_equal(V1, V3)  # deterministic
+    d = O.compare(B1, V1, B2, V2)
+    assert d["beta_se_scaled"] <= 1e-10 and d["se_rel"] <= 1e-10, d
+
+
+def test_split_u8_matches_fp64_genotype_input():
+    import torch
+    from fgls_gb300 import Engine, datagen
+    pb = datagen.make_problem(256, 200, 3, seed=6, hsig_uniform=True)
+    with Engine(256, 3, 1, 3, 200, variant="eigen", precision="split") as e:
+        e.set_problem(pb.Phi, pb.XL, pb.Y, pb.h, pb.sigma)
+        B, V = e.run_snps(pb.XR)
+        xu8 = torch.from_numpy(np.asfortranarray(pb.XR).T.astype(np.uint8).copy()).cuda()
+        dB = torch.empty(3 * 200 * 4, dtype=torch.float64, device="cuda")
+        dV = torch.empty(3 * 200 * 16, dtype=torch.float64, device="cuda")
+        e.run_block_device(xu8.data_ptr(), 200, dB.data_ptr(), dV.data_ptr(), 800, 3200, u8=True)
+        e.sync()
+    assert np.array_equal(B, dB.cpu().numpy().reshape(3, 200, 4))
