@@ -142,6 +142,27 @@ def genotype_block(x, n, seed, dev):
     return X.double()
 
 
+def rank_block_seeds(rank, pool):
+    """Genotype-block seeds of one rank: ranks shard the SNP blocks (weak
+    scaling), so no two ranks process the same block."""
+    return [100 + rank * 1000 + i for i in range(pool)]
+
+
+def max_over_ranks(value, dist, device):
+    """The job is as slow as its slowest rank: max of a per-rank time."""
+    if dist is None:
+        return value
+    import torch
+    tt = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def aggregate_throughput(world, blocks_per_rank, snps_per_block, traits, seconds):
+    """Whole-job tests/s: all ranks' SNP x trait tests over the slowest rank's time."""
+    return world * blocks_per_rank * snps_per_block * traits / seconds
+
+
 def rel_errors(B, V, Br, Vr):
     """beta error normwise per (trait, SNP) and on the SE scale; SE element-wise."""
     p = B.shape[-1]
@@ -271,7 +292,7 @@ def main():
     setup_s = time.perf_counter() - t0
     log(f"[bench] rank {rank}: data {gen_s:.1f}s, setup (eigendecomposition + operands) {setup_s:.1f}s")
 
-    pool = [genotype_block(xb, n, 100 + rank * 1000 + i, dev) for i in range(args.pool)]
+    pool = [genotype_block(xb, n, sd, dev) for sd in rank_block_seeds(rank, args.pool)]
     dB = torch.empty(t * xb * p, dtype=torch.float64, device=dev)
     dV = torch.empty(t * xb * p * p, dtype=torch.float64, device=dev)
     stream = torch.cuda.ExternalStream(eng.stream(), device=dev)
@@ -307,19 +328,14 @@ def main():
     eng.sync()
     prof = eng.profile_read()
     eng.profile(False)
-    if dist:
-        tt = torch.tensor([ms], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
-    tests = world * args.steps * xb * t
-    value = tests / (ms / 1e3)
+    ms = max_over_ranks(ms, dist, dev)
+    value = aggregate_throughput(world, args.steps, xb, t, ms / 1e3)
 
     # roofline of the dominant kernel: the tcgen05 split GEMM
     M_A = n + t * (1 + WXL)
-    flops_launch = 2.0 * args.slices * M_A * n * xb  # sliced BF16 MMA operations per launch
+    flops_snp = 2.0 * args.slices * M_A * n  # sliced BF16 MMA operations per SNP column
     gemm_ms, gemm_n = prof["split_gemm"]
-    gemm_ms_launch = gemm_ms / max(gemm_n, 1)
-    achieved = flops_launch / (gemm_ms_launch / 1e3) / 1e12
+    achieved = flops_snp * xb * args.steps / (gemm_ms / 1e3) / 1e12
     peak = float(pk.get("bf16_tflops_sustained", FALLBACK_PEAKS["bf16_tflops_sustained"]))
     traffic = None
     tf = os.path.join(ROOT, "profiles", "split_gemm_traffic.json")
@@ -372,11 +388,8 @@ def main():
     a = time.perf_counter()
     eng.run_snps_ptr(Xh.data_ptr(), E * xb, Bh.data_ptr(), Vh.data_ptr())
     e2e_s = time.perf_counter() - a
-    if dist:
-        tt = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
-    e2e_value = world * E * xb * t / e2e_s
+    e2e_s = max_over_ranks(e2e_s, dist, dev)
+    e2e_value = aggregate_throughput(world, E, xb, t, e2e_s)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -411,7 +424,8 @@ def main():
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "kernel": "ozaki_gemm_kernel", "peak_source": f"{pk_kind} bf16_tflops_sustained",
-                     "work": f"2*{args.slices} slices*{M_A} rows*{n} K*{xb} SNPs per launch"},
+                     "work": f"2*{args.slices} slices*{M_A} rows*{n} K per SNP; {gemm_n} launches, "
+                             f"{gemm_ms / max(gemm_n, 1):.3f} ms each"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": xb * n * 8,
                 "d2h_bytes_per_step": t * xb * (p + p * p) * 8,
                 "api": "fglsgpu_run_snps (host pinned FP64 XR -> host B/V)", "blocks": E},

@@ -8,14 +8,13 @@
 //     per column, rank-2 update).  Memory-bound: ~3 passes over the trailing
 //     matrix per column.
 //  2. Q = H_0 H_1 ... H_{n-3} formed explicitly by backward accumulation.
-//  3. Implicit QL with Wilkinson shifts on the tridiagonal (the EISPACK
-//     tql2 / tqli iteration) with an absolute deflation test |e_m| <= eps*|T|.
-//     The scalar recurrence of each sweep runs in one thread and records its
-//     Givens rotations; a second kernel applies the sweep's rotation chain to
-//     every row of Z in parallel (one thread per row, coalesced by column).
-//  4. Sort ascending, permuting the columns of Z.
+//  3. Eigenpairs of the tridiagonal by divide and conquer (fgls_dc.cu):
+//     eigenvalues ascending, eigenvectors V of T.
+//  4. Z = Q V (DGEMM).
 #include <algorithm>
 #include <cfloat>
+#include <cstdio>
+#include <cstdlib>
 
 #include "fgls_common.cuh"
 #include "fgls_kernels.cuh"
@@ -161,148 +160,13 @@ __global__ void load_v_kernel(int n, int k, const double* A, long long lda, doub
     vbuf[i] = (i == 0) ? 1.0 : A[(k + 1 + i) + (long long)k * lda];
 }
 
-struct QLState {
-  int l;      // first not yet converged index
-  int lo, hi; // rotation range of the last sweep (applied hi down to lo)
-  int nrot;   // rotations recorded by the last sweep (0: none)
-  int iter;   // sweeps spent on the current l
-  int done;
-  int fail;
-  int sweeps;
-  double anorm;
-};
-
-__global__ void ql_init_kernel(int n, const double* d, const double* e, QLState* q) {
-  double a = 0.0;
-  for (int i = 0; i < n; i++) {
-    double r = fabs(d[i]) + fabs(e[i]) + (i > 0 ? fabs(e[i - 1]) : 0.0);
-    a = fmax(a, r);
-  }
-  q->l = 0;
-  q->lo = q->hi = 0;
-  q->nrot = 0;
-  q->iter = 0;
-  q->done = (n <= 1);
-  q->fail = 0;
-  q->sweeps = 0;
-  q->anorm = a;
-}
-
-// One implicit QL sweep (scalar, single thread); records rotations in c/s.
-__global__ void ql_sweep_kernel(int n, double* d, double* e, double* cs, double* sn, QLState* q) {
-  q->nrot = 0;
-  if (q->done) return;
-  const double tol = DBL_EPSILON * q->anorm;
-  int l = q->l;
-  while (l < n) {
-    int m;
-    for (m = l; m < n - 1; m++)
-      if (fabs(e[m]) <= tol) break;
-    if (m == l) {
-      l++;
-      q->iter = 0;
-      continue;
-    }
-    if (q->iter >= 64) {
-      q->fail = 1;
-      q->done = 1;
-      q->l = l;
-      return;
-    }
-    q->iter++;
-    q->sweeps++;
-    double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
-    double r = hypot(g, 1.0);
-    g = d[m] - d[l] + e[l] / (g + copysign(r, g));
-    double s = 1.0, c = 1.0, p = 0.0;
-    int i;
-    int cnt = 0;
-    for (i = m - 1; i >= l; i--) {
-      double f = s * e[i];
-      double b = c * e[i];
-      r = hypot(f, g);
-      e[i + 1] = r;
-      if (r == 0.0) {
-        d[i + 1] -= p;
-        e[m] = 0.0;
-        break;
-      }
-      s = f / r;
-      c = g / r;
-      g = d[i + 1] - p;
-      r = (d[i] - g) * s + 2.0 * c * b;
-      p = s * r;
-      d[i + 1] = g + p;
-      g = c * r - b;
-      cs[i] = c;
-      sn[i] = s;
-      cnt++;
-    }
-    q->hi = m - 1;
-    q->lo = m - cnt;
-    q->nrot = cnt;
-    if (!(r == 0.0 && i >= l)) {
-      d[l] -= p;
-      e[l] = g;
-      e[m] = 0.0;
-    }
-    q->l = l;
-    return;
-  }
-  q->l = n;
-  q->done = 1;
-}
-
-// Apply the recorded rotation chain to every row of Z (column-major n x n).
-__global__ void ql_apply_kernel(int n, double* Z, long long ldz, const double* cs, const double* sn,
-                                const QLState* q) {
-  const int nrot = q->nrot;
-  if (nrot == 0) return;
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n) return;
-  const int hi = q->hi, lo = q->lo;
-  double carry = Z[r + (long long)(hi + 1) * ldz];
-  for (int i = hi; i >= lo; i--) {
-    const double zi = Z[r + (long long)i * ldz];
-    const double c = cs[i], s = sn[i];
-    Z[r + (long long)(i + 1) * ldz] = s * zi + c * carry;
-    carry = c * zi - s * carry;
-  }
-  Z[r + (long long)lo * ldz] = carry;
-}
-
-// rank of each eigenvalue (ascending, ties by index), then gather
-__global__ void rank_kernel(int n, const double* d, int* rank) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double di = d[i];
-  int rk = 0;
-  for (int j = 0; j < n; j++) {
-    const double dj = d[j];
-    rk += (dj < di) || (dj == di && j < i);
-  }
-  rank[i] = rk;
-}
-
-__global__ void permute_kernel(int n, const double* d, const int* rank, const double* Zin, long long ldi,
-                               double* W, double* Zout, long long ldo) {
-  const long long total = (long long)n * n;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
-       e += (long long)gridDim.x * blockDim.x) {
-    int r = (int)(e % n), c = (int)(e / n);
-    int rc = rank[c];
-    Zout[r + (long long)rc * ldo] = Zin[r + (long long)c * ldi];
-    if (r == 0) W[rc] = d[c];
-  }
-}
-
 int grid_for(long long total) { return (int)std::min<long long>((total + 255) / 256, 152LL * 32); }
 
 }  // namespace
 
 size_t eig_workspace_bytes(int n) {
-  // d, e, tau, vbuf, p, cs, sn (n each) + rank (n ints) + QLState
-  return sizeof(double) * (size_t)n * 7 + sizeof(int) * (size_t)n + 256;
+  // d, e, tau, vbuf, p (n each) + n ints of scratch
+  return sizeof(double) * (size_t)n * 5 + sizeof(int) * (size_t)n + 256;
 }
 
 cudaError_t dsyev_device(cudaStream_t s, int n, const double* Phi, long long ldp, double* A, double* Z,
@@ -312,12 +176,18 @@ cudaError_t dsyev_device(cudaStream_t s, int n, const double* Phi, long long ldp
   double* tau = e + n;
   double* vbuf = tau + n;
   double* p = vbuf + n;
-  double* cs = p + n;
-  double* sn = cs + n;
-  int* rank = (int*)(sn + n);
-  QLState* q = (QLState*)(((uintptr_t)(rank + n) + 63) & ~(uintptr_t)63);
+  int* rank = (int*)(p + n);
   long long nl = 0;
-  // A := Phi (lower) symmetrized; use Z as the scratch copy target first
+  // FGLS_EIG_TIMING=1 prints the phase times (CUDA events on s) to stderr
+  const bool timing = getenv("FGLS_EIG_TIMING") != nullptr;
+  cudaEvent_t ev[5];
+  if (timing)
+    for (auto& x : ev) cudaEventCreate(&x);
+  auto mark = [&](int i) {
+    if (timing) cudaEventRecord(ev[i], s);
+  };
+  mark(0);
+  // A := Phi (lower) symmetrized
   FGLS_CUDA_TRY(cudaMemcpy2DAsync(A, sizeof(double) * n, Phi, sizeof(double) * ldp, sizeof(double) * n, n,
                                   cudaMemcpyDeviceToDevice, s));
   symmetrize_kernel<<<grid_for((long long)n * n), 256, 0, s>>>(n, A, n);
@@ -337,6 +207,7 @@ cudaError_t dsyev_device(cudaStream_t s, int n, const double* Phi, long long ldp
   tridiag_tail_kernel<<<1, 1, 0, s>>>(n, A, n, d, e);
   nl++;
   FGLS_CUDA_TRY(cudaGetLastError());
+  mark(1);
   // 2. Q = H_0 ... H_{n-3}
   identity_kernel<<<grid_for((long long)n * n), 256, 0, s>>>(n, Z, n);
   nl++;
@@ -350,30 +221,34 @@ cudaError_t dsyev_device(cudaStream_t s, int n, const double* Phi, long long ldp
     nl += 3;
   }
   FGLS_CUDA_TRY(cudaGetLastError());
-  // 3. implicit QL with rotations applied to Z
-  ql_init_kernel<<<1, 1, 0, s>>>(n, d, e, q);
-  nl++;
-  QLState hq;
-  const long long max_sweeps = 64LL * n + 64;
-  long long it = 0;
-  for (;;) {
-    for (int b = 0; b < 128; b++, it++) {
-      ql_sweep_kernel<<<1, 1, 0, s>>>(n, d, e, cs, sn, q);
-      ql_apply_kernel<<<ceil_div(n, 128), 128, 0, s>>>(n, Z, n, cs, sn, q);
-      nl += 2;
-    }
-    FGLS_CUDA_TRY(cudaGetLastError());
-    FGLS_CUDA_TRY(cudaMemcpyAsync(&hq, q, sizeof(QLState), cudaMemcpyDeviceToHost, s));
-    FGLS_CUDA_TRY(cudaStreamSynchronize(s));
-    if (hq.done || it > max_sweeps) break;
+  mark(2);
+  // 3. eigenpairs of T by divide and conquer (fgls_dc.cu) into A (free now)
+  void* dcw = nullptr;
+  FGLS_CUDA_TRY(cudaMalloc(&dcw, dc_workspace_bytes(n)));
+  int* dfail = rank;  // n ints of scratch; first used as the failure flag
+  FGLS_CUDA_TRY(cudaMemsetAsync(dfail, 0, sizeof(int), s));
+  cudaError_t rc = dc_tridiag_eig(s, n, d, e, W, A, dcw, dfail, &nl);
+  mark(3);
+  // 4. Z = Q T-eigenvectors, through a scratch matrix of the workspace
+  double* T = (double*)dcw;
+  if (rc == cudaSuccess) rc = dgemm(s, false, false, n, n, n, 1.0, Z, n, A, n, 0.0, T, n);
+  if (rc == cudaSuccess)
+    rc = cudaMemcpyAsync(Z, T, sizeof(double) * (size_t)n * n, cudaMemcpyDeviceToDevice, s);
+  int hfail = 0;
+  if (rc == cudaSuccess) rc = cudaMemcpyAsync(&hfail, dfail, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (rc == cudaSuccess) rc = cudaStreamSynchronize(s);
+  cudaFree(dcw);
+  FGLS_CUDA_TRY(rc);
+  *fail_out = hfail;
+  mark(4);
+  if (timing) {
+    cudaEventSynchronize(ev[4]);
+    float t[4];
+    for (int i = 0; i < 4; i++) cudaEventElapsedTime(&t[i], ev[i], ev[i + 1]);
+    fprintf(stderr, "[fgls eig n=%d] tridiagonal %.1f ms, form Q %.1f ms, divide-and-conquer %.1f ms, back-transform %.1f ms\n",
+            n, t[0], t[1], t[2], t[3]);
+    for (auto& x : ev) cudaEventDestroy(x);
   }
-  *fail_out = (hq.fail || !hq.done) ? 1 : 0;
-  // 4. sort ascending; A is free again and receives the permuted Z, copied back
-  rank_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, d, rank);
-  permute_kernel<<<grid_for((long long)n * n), 256, 0, s>>>(n, d, rank, Z, n, W, A, n);
-  nl += 2;
-  FGLS_CUDA_TRY(cudaGetLastError());
-  FGLS_CUDA_TRY(cudaMemcpyAsync(Z, A, sizeof(double) * (size_t)n * n, cudaMemcpyDeviceToDevice, s));
   if (launches) *launches += nl;
   note_launch(nl);
   return cudaSuccess;

@@ -58,6 +58,7 @@ struct fglsgpu_engine {
   };
   bool prof = false;
   std::vector<PEv> pev_live, pev_pool;
+  PEv pending[FGLSGPU_PROF_CLASSES]{};
   double prof_ms[FGLSGPU_PROF_CLASSES] = {0};
   long long prof_cnt[FGLSGPU_PROF_CLASSES] = {0};
 };
@@ -150,8 +151,8 @@ struct Prof {
   cudaStream_t s;
   fglsgpu_engine::PEv ev{};
   bool on;
-  Prof(fglsgpu_engine* e_, int cls, cudaStream_t s_) : e(e_), s(s_), on(e_->prof) {
-    if (!on) return;
+  static fglsgpu_engine::PEv take(fglsgpu_engine* e, int cls) {
+    fglsgpu_engine::PEv ev{};
     if (e->pev_pool.empty()) {
       cudaEventCreate(&ev.a);
       cudaEventCreate(&ev.b);
@@ -160,6 +161,11 @@ struct Prof {
       e->pev_pool.pop_back();
     }
     ev.cls = cls;
+    return ev;
+  }
+  Prof(fglsgpu_engine* e_, int cls, cudaStream_t s_) : e(e_), s(s_), on(e_->prof) {
+    if (!on) return;
+    ev = take(e, cls);
     cudaEventRecord(ev.a, s);
   }
   ~Prof() {
@@ -168,6 +174,19 @@ struct Prof {
     e->pev_live.push_back(ev);
   }
 };
+
+// Stage hook of the split path: brackets each stage on the stream it runs on.
+void stage_hook(void* ctx, int cls, int begin, cudaStream_t st) {
+  fglsgpu_engine* e = (fglsgpu_engine*)ctx;
+  if (!e->prof) return;
+  if (begin) {
+    e->pending[cls] = Prof::take(e, cls);
+    cudaEventRecord(e->pending[cls].a, st);
+  } else {
+    cudaEventRecord(e->pending[cls].b, st);
+    e->pev_live.push_back(e->pending[cls]);
+  }
+}
 
 // Compute one block already in device memory (FP64 genotypes at dXin,
 // n x x*wXR) into dB/dV with the given trait strides, on e->comp.
@@ -181,18 +200,7 @@ int compute_block(fglsgpu_engine* e, const double* dXin, const unsigned char* dX
   if (c.variant == FGLSGPU_VARIANT_CHOL && e->trait_sel < 0)
     return fail(e, FGLSGPU_ESTATE, "fglsgpu_select_trait must precede run_block (chol)");
   if (split(e)) {
-    {
-      Prof pr(e, FGLSGPU_PROF_GENOTYPES, s);
-      ENG_TRY(e, dXu8 ? ozaki_genotypes_u8(e->oz, s, dXu8, x) : ozaki_genotypes(e->oz, s, dXin, x), "genotypes");
-    }
-    {
-      Prof pr(e, FGLSGPU_PROF_SPLIT_GEMM, s);
-      ENG_TRY(e, ozaki_product(e->oz, s, x), "split GEMM");
-    }
-    {
-      Prof pr(e, FGLSGPU_PROF_SELFGRAM, s);
-      ENG_TRY(e, ozaki_selfgram(e->oz, s, x, e->dGR), "quadratic Gram");
-    }
+    ENG_TRY(e, ozaki_block(e->oz, s, dXin, dXu8, x, e->dGR, stage_hook, e), "split block");
     long long ld = 0;
     const double* gyl = ozaki_gram_rows(e->oz, &ld);
     Prof pr(e, FGLSGPU_PROF_SOLVE, s);

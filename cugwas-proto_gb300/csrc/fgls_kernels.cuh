@@ -46,6 +46,13 @@ size_t eig_workspace_bytes(int n);
 cudaError_t dsyev_device(cudaStream_t s, int n, const double* Phi, long long ldp, double* A, double* Z,
                          double* W, void* work, int* fail_out, long long* launches);
 
+// Divide-and-conquer eigensolver of the tridiagonal (d, e) (fgls_dc.cu):
+// W ascending, V (n x n) eigenvectors; d, e are overwritten; fail_dev set
+// to 1 if a leaf iteration did not converge.
+size_t dc_workspace_bytes(int n);
+cudaError_t dc_tridiag_eig(cudaStream_t s, int n, double* d, double* e, double* W, double* V, void* work,
+                           int* fail_dev, long long* launches);
+
 // Genotype conversion: FP64 or u8 hard calls -> FP64 (device to device).
 cudaError_t u8_to_f64(cudaStream_t s, const unsigned char* in, double* out, long long count);
 

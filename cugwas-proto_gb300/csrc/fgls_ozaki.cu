@@ -178,10 +178,26 @@ struct GemmArgs {
   int tiles_m, tiles_n;
   int tri_rows;     // rows [0, tri_rows) of A are lower triangular in K (0: none)
   const double* row_scale;  // per row 2^(e_r - 15 - 16 (passes-1))
-  double* C;        // FP64 output, column-major, ld = ldc (int64 between passes)
+  double* C;        // output, column-major, ld = ldc (int64 between passes)
   long long ldc;
+  int col0;         // first genotype column of this launch (TMA row offset of G)
+  int sq_rows;      // rows [0, sq_rows): write (C^2) as an error-free float pair (hi, lo)
   int* err;         // first failing wait site (0 = ok)
 };
+
+// Exact int64 value V times a power-of-two scale, squared, as a float pair:
+// v = V*scale = vh + vl (|vl| <= 2^-24 |vh|), v^2 ~= ah + al with
+// ah = fl(vh^2), al = (vh^2 - ah) + 2 vh vl; relative error ~2^-47.  No FP64
+// arithmetic: the conversions run on the integer / conversion units.
+__device__ __forceinline__ float2 square_pair(long long V, float fscale) {
+  const float vh0 = __ll2float_rn(V);
+  const long long rem = V - __float2ll_rn(vh0);
+  const float vh = vh0 * fscale;
+  const float vl = __ll2float_rn(rem) * fscale;
+  const float ah = vh * vh;
+  const float al = fmaf(vh, vh, -ah) + 2.0f * vh * vl;
+  return make_float2(ah, al);
+}
 
 __global__ void __launch_bounds__(THREADS, 1)
     ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
@@ -250,7 +266,7 @@ __global__ void __launch_bounds__(THREADS, 1)
           mbar_expect_tx(&full[stage], (two ? 2 * A_TILE : A_TILE) + B_TILE);
           tma_load_2d(sb, &tmA, kb * BK, s0 * g.Mpad + m0, &full[stage]);
           if (two) tma_load_2d(sb + A_TILE, &tmA, kb * BK, s1 * g.Mpad + m0, &full[stage]);
-          tma_load_2d(sb + 2 * A_TILE, &tmB, kb * BK, n0, &full[stage]);
+          tma_load_2d(sb + 2 * A_TILE, &tmB, kb * BK, g.col0 + n0, &full[stage]);
           issued[stage] = 1;
           issued_phase[stage] = phase;
           if (++stage == STAGES) { stage = 0; phase ^= 1; }
@@ -305,6 +321,8 @@ __global__ void __launch_bounds__(THREADS, 1)
     const int r = m0 + row;
     const bool rvalid = r < g.M;
     const double scale = rvalid ? g.row_scale[r] : 0.0;
+    const bool sq = r < g.sq_rows;
+    const float fscale = (float)scale;  // power of two: exact while >= 2^-149
     for (int p = 0; p < passes; p++) {
       const bool two = 2 * p + 1 < g.S;
       const bool last = p == passes - 1;
@@ -327,12 +345,14 @@ __global__ void __launch_bounds__(THREADS, 1)
           if (col >= g.N) break;
           int qv = __float2int_rn(__uint_as_float(v0[j])) * 256;
           if (two) qv += __float2int_rn(__uint_as_float(v1[j]));
-          long long* cp = (long long*)(g.C + (long long)r + (long long)col * g.ldc);
+          long long* cp = (long long*)(g.C + (long long)r + (long long)(g.col0 + col) * g.ldc);
           long long V = (p == 0) ? (long long)qv : (*cp) * 65536LL + (long long)qv;
-          if (last)
-            *(double*)cp = (double)V * scale;
-          else
+          if (!last)
             *cp = V;
+          else if (sq)
+            *(float2*)cp = square_pair(V, fscale);
+          else
+            *(double*)cp = (double)V * scale;
         }
       }
       tc_fence_before();
@@ -420,109 +440,162 @@ __global__ void transpose_kernel(int n, const double* __restrict__ A, double* __
   }
 }
 
-__global__ void fill_pairs_kernel(int count, float* hi, float* lo) {
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < count; e += gridDim.x * blockDim.x) {
-    hi[e] = 1.0f;
-    lo[e] = 0.0f;
-  }
+// ---------------------------------------------------------------------------
+// Quadratic Gram terms in double-FP32:
+//   GR[i + j*ldg] = sum_l A[l,i] * D[l,j],   A = R^2 as float pairs written by
+//   the GEMM epilogue (C rows [0, n), 8 bytes each), D = d_j as float pairs.
+// All terms are non-negative (no cancellation).  Each product is error-free
+// (p + pe = ah*dh exactly, by fma) and its cross terms ah*dl + al*dh go to the
+// low accumulator.  The high accumulator starts at a power of two B_ij no
+// smaller than any term (max_l ah[l,i] * max_l dh[l,j], rounded up), so every
+// addition satisfies |s| >= |p| and Fast2Sum (3 ops) is exact.  Every 64 rows
+// the chunk (offset removed exactly) is folded into an outer (H, L) pair by
+// TwoSum, so the FP32 low parts never sum more than 64 rounding errors of one
+// chunk: relative error ~1e-14 at n = 10^4 (a single running pair reaches
+// ~1e-11 there).  9 FP32 operations per term.
+// CTA tile 64 SNPs x 112 traits (16 x 16 threads, 4 x 7 each), 32-row chunks.
+// ---------------------------------------------------------------------------
+constexpr int QG_I = 64, QG_J = 112, QG_L = 32, QG_RI = 4, QG_RJ = 7, QG_FOLD = 64;
+
+// Knuth's TwoSum: s + e == a + b exactly
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bp = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
 }
 
-// d (FP64, n x t) -> float pair (hi, lo)
-__global__ void split_pairs_kernel(long long count, const double* __restrict__ d, float* __restrict__ hi,
-                                   float* __restrict__ lo) {
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < count;
-       e += (long long)gridDim.x * blockDim.x) {
-    const double v = d[e];
-    const float h = (float)v;
-    hi[e] = h;
-    lo[e] = (float)(v - (double)h);
-  }
+__device__ __forceinline__ float pow2_ceil(float v) {
+  // smallest power of two >= v (v > 0, finite)
+  return __int_as_float((__float_as_int(v) + 0x007FFFFF) & 0x7F800000);
 }
 
-// ---------------------------------------------------------------------------
-// Quadratic Gram terms in double-FP32:  GR[i + j*x] = sum_l R[l,i]^2 * D[l,j]
-// with D = (Dh + Dl) float pairs.  Error-free products (fma) and sums
-// (TwoSum) keep ~2^-44 relative accuracy; all terms are non-negative so there
-// is no cancellation.  Tile 64 SNPs x 64 traits, 256 threads, 4 x 4 each.
-// ---------------------------------------------------------------------------
-constexpr int QG_I = 64, QG_J = 64, QG_L = 32;
-__global__ void __launch_bounds__(256) selfgram_kernel(int n, int x, int t, const double* __restrict__ R,
-                                                       long long ldr, const float* __restrict__ Dh,
-                                                       const float* __restrict__ Dl, long long ldd,
-                                                       double* __restrict__ GR, long long ldg) {
-  __shared__ float Ah[QG_L][QG_I + 1], Al[QG_L][QG_I + 1];
-  __shared__ float Bh[QG_L][QG_J + 1], Bl[QG_L][QG_J + 1];
+// amax[i] = max_l A[l, i].x  (one warp per column)
+__global__ void colmax_kernel(int n, int x, const float2* __restrict__ A, long long lda, float* __restrict__ amax) {
+  const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (i >= x) return;
+  float m = 0.0f;
+  for (int l = lane; l < n; l += 32) m = fmaxf(m, A[l + (long long)i * lda].x);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (lane == 0) amax[i] = m;
+}
+
+__global__ void __launch_bounds__(256) selfgram_kernel(int n, int x, int t, const float2* __restrict__ A,
+                                                       long long lda, const float* __restrict__ amax,
+                                                       const float2* __restrict__ D, long long ldd,
+                                                       const float* __restrict__ dmax, double* __restrict__ GR,
+                                                       long long ldg) {
+  __shared__ float2 As[QG_L][QG_I];
+  __shared__ float2 Bs[QG_L][QG_J];
   const int i0 = blockIdx.x * QG_I, j0 = blockIdx.y * QG_J;
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-  float sh[4][4], sl[4][4];
+  // inner (sh, sl): one 64-row chunk from the offset; outer (H, L): the fold
+  float sh[QG_RI][QG_RJ], sl[QG_RI][QG_RJ], H[QG_RI][QG_RJ], L[QG_RI][QG_RJ];
+  auto offset = [&](int a, int b) {
+    const int i = i0 + ty + 16 * a, j = j0 + tx + 16 * b;
+    const float bound = ((i < x) ? amax[i] : 0.0f) * ((j < t) ? dmax[j] : 0.0f);
+    return bound > 0.0f ? pow2_ceil(bound) : 0.0f;
+  };
 #pragma unroll
-  for (int a = 0; a < 4; a++)
+  for (int a = 0; a < QG_RI; a++)
 #pragma unroll
-    for (int b = 0; b < 4; b++) sh[a][b] = sl[a][b] = 0.0f;
+    for (int b = 0; b < QG_RJ; b++) {
+      sh[a][b] = offset(a, b);
+      sl[a][b] = H[a][b] = L[a][b] = 0.0f;
+    }
   for (int l0 = 0; l0 < n; l0 += QG_L) {
     __syncthreads();
     for (int e = threadIdx.x; e < QG_L * QG_I; e += 256) {
       const int l = e % QG_L, i = e / QG_L;
-      float h = 0.0f, lo = 0.0f;
-      if (l0 + l < n && i0 + i < x) {
-        const double r = R[(l0 + l) + (long long)(i0 + i) * ldr];
-        const float rh = (float)r;
-        const float rl = (float)(r - (double)rh);
-        h = rh * rh;
-        lo = fmaf(rh, rh, -h) + 2.0f * rh * rl;
-      }
-      Ah[l][i] = h;
-      Al[l][i] = lo;
+      float2 v = make_float2(0.f, 0.f);
+      if (l0 + l < n && i0 + i < x) v = A[(l0 + l) + (long long)(i0 + i) * lda];
+      As[l][i] = v;
     }
     for (int e = threadIdx.x; e < QG_L * QG_J; e += 256) {
       const int l = e % QG_L, j = e / QG_L;
-      float h = 0.0f, lo = 0.0f;
-      if (l0 + l < n && j0 + j < t) {
-        h = Dh[(l0 + l) + (long long)(j0 + j) * ldd];
-        lo = Dl[(l0 + l) + (long long)(j0 + j) * ldd];
-      }
-      Bh[l][j] = h;
-      Bl[l][j] = lo;
+      float2 v = make_float2(0.f, 0.f);
+      if (l0 + l < n && j0 + j < t) v = D[(l0 + l) + (long long)(j0 + j) * ldd];
+      Bs[l][j] = v;
     }
     __syncthreads();
 #pragma unroll 4
     for (int l = 0; l < QG_L; l++) {
-      float ah[4], al[4], bh[4], bl[4];
+      float2 av[QG_RI], bv[QG_RJ];
 #pragma unroll
-      for (int a = 0; a < 4; a++) {
-        ah[a] = Ah[l][ty + 16 * a];
-        al[a] = Al[l][ty + 16 * a];
-      }
+      for (int a = 0; a < QG_RI; a++) av[a] = As[l][ty + 16 * a];
 #pragma unroll
-      for (int b = 0; b < 4; b++) {
-        bh[b] = Bh[l][tx + 16 * b];
-        bl[b] = Bl[l][tx + 16 * b];
-      }
+      for (int b = 0; b < QG_RJ; b++) bv[b] = Bs[l][tx + 16 * b];
 #pragma unroll
-      for (int a = 0; a < 4; a++)
+      for (int a = 0; a < QG_RI; a++)
 #pragma unroll
-        for (int b = 0; b < 4; b++) {
-          const float p = ah[a] * bh[b];
-          const float pe = fmaf(ah[a], bh[b], -p);
-          const float low = fmaf(ah[a], bl[b], fmaf(al[a], bh[b], pe));
-          const float s = sh[a][b] + p;
-          const float bp = s - sh[a][b];
-          const float err = (sh[a][b] - (s - bp)) + (p - bp);
-          sh[a][b] = s;
-          sl[a][b] += err + low;
+        for (int b = 0; b < QG_RJ; b++) {
+          const float p = __fmul_rn(av[a].x, bv[b].x);
+          const float pe = fmaf(av[a].x, bv[b].x, -p);
+          float lo = fmaf(av[a].x, bv[b].y, sl[a][b]);
+          lo = fmaf(av[a].y, bv[b].x, lo);
+          const float s2 = __fadd_rn(sh[a][b], p);
+          const float err = __fsub_rn(p, __fsub_rn(s2, sh[a][b]));
+          sh[a][b] = s2;
+          sl[a][b] = __fadd_rn(__fadd_rn(lo, pe), err);
+        }
+    }
+    // fold the chunk into (H, L) every QG_FOLD rows (and at the end)
+    if (((l0 + QG_L) % QG_FOLD) == 0 || l0 + QG_L >= n) {
+#pragma unroll
+      for (int a = 0; a < QG_RI; a++)
+#pragma unroll
+        for (int b = 0; b < QG_RJ; b++) {
+          const float off = offset(a, b);
+          float hs, he, h2, e1;
+          two_sum(sh[a][b], -off, hs, he);
+          two_sum(H[a][b], hs, h2, e1);
+          H[a][b] = h2;
+          L[a][b] = __fadd_rn(L[a][b], __fadd_rn(__fadd_rn(e1, he), sl[a][b]));
+          sh[a][b] = off;
+          sl[a][b] = 0.0f;
         }
     }
   }
 #pragma unroll
-  for (int a = 0; a < 4; a++) {
+  for (int a = 0; a < QG_RI; a++) {
     const int i = i0 + ty + 16 * a;
     if (i >= x) continue;
 #pragma unroll
-    for (int b = 0; b < 4; b++) {
+    for (int b = 0; b < QG_RJ; b++) {
       const int j = j0 + tx + 16 * b;
       if (j >= t) continue;
-      GR[i + (long long)j * ldg] = (double)sh[a][b] + (double)sl[a][b];
+      GR[i + (long long)j * ldg] = (double)H[a][b] + (double)L[a][b];
     }
+  }
+}
+
+// unit weights (chol: |x~|^2)
+__global__ void unit_pairs_kernel(int n, float2* D, float* dmax) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) D[e] = make_float2(1.f, 0.f);
+  if (blockIdx.x == 0 && threadIdx.x == 0) dmax[0] = 1.f;
+}
+
+// D (FP64 n x t) -> interleaved float pairs, and dmax[j] = max_l hi
+__global__ void split_pairs_kernel(int n, int t, const double* __restrict__ d, float2* __restrict__ D,
+                                   float* __restrict__ dmax) {
+  const int j = blockIdx.x;
+  float m = 0.0f;
+  for (int l = threadIdx.x; l < n; l += blockDim.x) {
+    const double v = d[l + (long long)j * n];
+    const float h = (float)v;
+    D[l + (long long)j * n] = make_float2(h, (float)(v - (double)h));
+    m = fmaxf(m, h);
+  }
+  __shared__ float red[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) m = fmaxf(m, red[w]);
+    m = fmaxf(m, red[0]);
+    dmax[j] = m;
   }
 }
 
@@ -574,12 +647,15 @@ struct OzakiPlan {
   double* scale = nullptr;      // Mpad
   double* C = nullptr;          // Mpad x Ncap (ld Mpad)
   double* U = nullptr;          // n x nU
-  float *Dh = nullptr, *Dl = nullptr;  // n x t (eigen weights; chol: ones)
+  float2* D = nullptr;          // n x t weights as float pairs (eigen d_j; chol: ones)
+  float* dmax = nullptr;        // t: max_l of the high part of D[:, j]
+  float* amax = nullptr;        // Ncap: per-SNP max_l of the high part of R^2
   double* Linv = nullptr;       // chol: n x n, L^-1
   double* LinvT = nullptr;      // chol: n x n, (L^-1)^T (rows of L^-1 contiguous)
   int* err = nullptr;
   CUtensorMap mapA, mapB;
   bool maps = false;
+  int sub = 0;                      // SNPs per pipelined sub-block (multiple of BN)
 };
 
 cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_b, int slices, int eigen) {
@@ -608,8 +684,9 @@ cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_
   chk(cudaMalloc(&p->scale, sizeof(double) * p->Mpad));
   chk(cudaMalloc(&p->C, sizeof(double) * (size_t)p->Mpad * p->Ncap));
   chk(cudaMalloc(&p->U, sizeof(double) * (size_t)n * p->nU));
-  chk(cudaMalloc(&p->Dh, sizeof(float) * (size_t)n * t));
-  chk(cudaMalloc(&p->Dl, sizeof(float) * (size_t)n * t));
+  chk(cudaMalloc(&p->D, sizeof(float2) * (size_t)n * t));
+  chk(cudaMalloc(&p->dmax, sizeof(float) * (size_t)t));
+  chk(cudaMalloc(&p->amax, sizeof(float) * (size_t)p->Ncap));
   chk(cudaMalloc(&p->err, sizeof(int)));
   if (!eigen) chk(cudaMalloc(&p->Linv, sizeof(double) * (size_t)n * n));
   if (!eigen) chk(cudaMalloc(&p->LinvT, sizeof(double) * (size_t)n * n));
@@ -621,6 +698,7 @@ cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_
   if (r == cudaSuccess) chk(make_map(&p->mapB, p->G, p->Kpad, p->Ncap, BN));
   if (r == cudaSuccess) chk(cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                  SMEM_BYTES));
+  p->sub = p->Ncap;  // one GEMM launch per block
   if (r != cudaSuccess) {
     ozaki_destroy(p);
     return r;
@@ -632,7 +710,7 @@ cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_
 
 void ozaki_destroy(OzakiPlan* p) {
   if (!p) return;
-  void* ptrs[] = {p->A, p->G, p->scale, p->C, p->U, p->Dh, p->Dl, p->Linv, p->LinvT, p->err};
+  void* ptrs[] = {p->A, p->G, p->scale, p->C, p->U, p->D, p->dmax, p->amax, p->Linv, p->LinvT, p->err};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   delete p;
@@ -650,11 +728,13 @@ cudaError_t slice_operands(OzakiPlan* p, cudaStream_t s, const double* top, long
   return cudaGetLastError();
 }
 
-cudaError_t run_gemm(OzakiPlan* p, cudaStream_t s, int x, int tri_rows) {
+cudaError_t run_gemm(OzakiPlan* p, cudaStream_t s, int col0, int x, int tri_rows, int sq_rows) {
   GemmArgs g;
   g.M = p->M;
   g.Mpad = p->Mpad;
   g.N = x;
+  g.col0 = col0;
+  g.sq_rows = sq_rows;
   g.Kpad = p->Kpad;
   g.S = p->S;
   g.tiles_m = p->Mpad / BM;
@@ -676,9 +756,12 @@ cudaError_t load_genotypes(OzakiPlan* p, cudaStream_t s, const T* X, int x) {
   return cudaGetLastError();
 }
 
-cudaError_t selfgram(OzakiPlan* p, cudaStream_t s, int x, int t, double* GR) {
-  dim3 grid((x + QG_I - 1) / QG_I, (t + QG_J - 1) / QG_J);
-  selfgram_kernel<<<grid, 256, 0, s>>>(p->n, x, t, p->C, p->Mpad, p->Dh, p->Dl, p->n, GR, x);
+cudaError_t selfgram(OzakiPlan* p, cudaStream_t s, int col0, int xq, int t, double* GR, long long ldg) {
+  dim3 grid((xq + QG_I - 1) / QG_I, (t + QG_J - 1) / QG_J);
+  const float2* A = (const float2*)(p->C + (long long)col0 * p->Mpad);
+  colmax_kernel<<<(xq + 7) / 8, 256, 0, s>>>(p->n, xq, A, p->Mpad, p->amax + col0);
+  selfgram_kernel<<<grid, 256, 0, s>>>(p->n, xq, t, A, p->Mpad, p->amax + col0, p->D, p->n, p->dmax, GR + col0, ldg);
+  note_launch();
   note_launch();
   return cudaGetLastError();
 }
@@ -690,7 +773,7 @@ cudaError_t ozaki_set_eigen(OzakiPlan* p, cudaStream_t s, const double* Z, const
   FGLS_CUDA_TRY(dgemm(s, false, false, p->n, p->nU, p->n, 1.0, Z, p->n, AYL, p->n, 0.0, p->U, p->n));
   // rows of Z^T are the columns of Z (contiguous): ld n
   FGLS_CUDA_TRY(slice_operands(p, s, Z, p->n, p->n));
-  split_pairs_kernel<<<grid_for((long long)p->n * p->t), 256, 0, s>>>((long long)p->n * p->t, dinv, p->Dh, p->Dl);
+  split_pairs_kernel<<<p->t, 256, 0, s>>>(p->n, p->t, dinv, p->D, p->dmax);
   note_launch();
   return cudaGetLastError();
 }
@@ -708,25 +791,31 @@ cudaError_t ozaki_set_chol(OzakiPlan* p, cudaStream_t s, const double* L, const 
   note_launch();
   FGLS_CUDA_TRY(slice_operands(p, s, p->LinvT, n, n));
   // unit weights for the quadratic term |x~|^2
-  fill_pairs_kernel<<<grid_for(n), 256, 0, s>>>(n, p->Dh, p->Dl);
+  unit_pairs_kernel<<<grid_for(n), 256, 0, s>>>(n, p->D, p->dmax);
   note_launch();
   return cudaGetLastError();
 }
 
-cudaError_t ozaki_genotypes(OzakiPlan* p, cudaStream_t s, const double* X, int x) {
-  return load_genotypes<double>(p, s, X, x);
-}
-
-cudaError_t ozaki_genotypes_u8(OzakiPlan* p, cudaStream_t s, const unsigned char* X, int x) {
-  return load_genotypes<unsigned char>(p, s, X, x);
-}
-
-cudaError_t ozaki_product(OzakiPlan* p, cudaStream_t s, int x) {
-  return run_gemm(p, s, x, p->eigen ? 0 : p->n);
-}
-
-cudaError_t ozaki_selfgram(OzakiPlan* p, cudaStream_t s, int x, double* GR) {
-  return selfgram(p, s, x, p->eigen ? p->t : 1, GR);
+cudaError_t ozaki_block(OzakiPlan* p, cudaStream_t s, const double* X, const unsigned char* Xu8, int x,
+                        double* GR, StageHook hook, void* ctx) {
+  const int t = p->eigen ? p->t : 1;
+  const int tri = p->eigen ? 0 : p->n;
+  auto mark = [&](int cls, int begin, cudaStream_t st) {
+    if (hook) hook(ctx, cls, begin, st);
+  };
+  mark(FGLSGPU_PROF_GENOTYPES, 1, s);
+  FGLS_CUDA_TRY(Xu8 ? load_genotypes<unsigned char>(p, s, Xu8, x) : load_genotypes<double>(p, s, X, x));
+  mark(FGLSGPU_PROF_GENOTYPES, 0, s);
+  for (int x0 = 0; x0 < x; x0 += p->sub) {
+    const int xq = std::min(p->sub, x - x0);
+    mark(FGLSGPU_PROF_SPLIT_GEMM, 1, s);
+    FGLS_CUDA_TRY(run_gemm(p, s, x0, xq, tri, p->n));
+    mark(FGLSGPU_PROF_SPLIT_GEMM, 0, s);
+    mark(FGLSGPU_PROF_SELFGRAM, 1, s);
+    FGLS_CUDA_TRY(selfgram(p, s, x0, xq, t, GR, x));
+    mark(FGLSGPU_PROF_SELFGRAM, 0, s);
+  }
+  return cudaSuccess;
 }
 
 double ozaki_flops_per_snp(const OzakiPlan* p) {
@@ -795,7 +884,7 @@ extern "C" int fglsgpu_selftest_split_gemm(int M, int K, int N, int S, const dou
     chk(cudaGetLastError());
   }
   if (r == cudaSuccess) chk(load_genotypes<double>(&p, s, dX, N));
-  if (r == cudaSuccess) chk(run_gemm(&p, s, N, 0));
+  if (r == cudaSuccess) chk(run_gemm(&p, s, 0, N, 0, 0));
   if (r == cudaSuccess) chk(cudaStreamSynchronize(s));
   int herr = 0;
   if (r == cudaSuccess) chk(cudaMemcpy(&herr, p.err, sizeof(int), cudaMemcpyDeviceToHost));
@@ -810,3 +899,4 @@ extern "C" int fglsgpu_selftest_split_gemm(int M, int K, int N, int S, const dou
   if (r != cudaSuccess) return FGLSGPU_ECUDA;
   return herr ? FGLSGPU_ETIMEOUT : FGLSGPU_OK;
 }
+

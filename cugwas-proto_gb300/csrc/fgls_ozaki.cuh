@@ -18,14 +18,14 @@ void ozaki_destroy(OzakiPlan* p);
 cudaError_t ozaki_set_eigen(OzakiPlan* p, cudaStream_t s, const double* Z, const double* AYL, const double* dinv);
 // chol: L (n x n lower), WY = [y~ | XL~] (n x (1+wXL)) of the selected trait
 cudaError_t ozaki_set_chol(OzakiPlan* p, cudaStream_t s, const double* L, const double* WY);
-// Per-block stages:
-//  1. genotypes (FP64 or bytes, n x x) -> BF16 operand
-cudaError_t ozaki_genotypes(OzakiPlan* p, cudaStream_t s, const double* X, int x);
-cudaError_t ozaki_genotypes_u8(OzakiPlan* p, cudaStream_t s, const unsigned char* X, int x);
-//  2. the tcgen05 split GEMM: C = [Z^T ; U^T] X  (chol: [L^-1 ; U^T] X)
-cudaError_t ozaki_product(OzakiPlan* p, cudaStream_t s, int x);
-//  3. quadratic Gram terms GR[i + j*x] = sum_l C[l,i]^2 d_j(l)  (chol: d = 1)
-cudaError_t ozaki_selfgram(OzakiPlan* p, cudaStream_t s, int x, double* GR);
+// One genotype block (FP64 X or byte Xu8, n x x): BF16 operand build, the
+// tcgen05 split GEMM C = [Z^T ; U^T] X (chol: [L^-1 ; U^T] X), and the
+// quadratic Gram terms GR[i + j*x] = sum_l C[l,i]^2 d_j(l) (chol: d = 1),
+// all on stream s.  `hook(ctx, class, begin, stream)`
+// brackets each stage (FGLSGPU_PROF_* classes) for timing; may be null.
+typedef void (*StageHook)(void* ctx, int cls, int begin, cudaStream_t s);
+cudaError_t ozaki_block(OzakiPlan* p, cudaStream_t s, const double* X, const unsigned char* Xu8, int x,
+                        double* GR, StageHook hook, void* ctx);
 // sliced MMA operations per genotype column (2 * slices * rows * K)
 double ozaki_flops_per_snp(const OzakiPlan* p);
 
