@@ -900,3 +900,119 @@ extern "C" int fglsgpu_selftest_split_gemm(int M, int K, int N, int S, const dou
   return herr ? FGLSGPU_ETIMEOUT : FGLSGPU_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Split GEMM that allocates nothing.
+//
+// For callers that may not allocate device memory themselves: code that runs
+// inside a framework which owns every byte of the device through its own
+// pool (a raw cudaMalloc would bypass its accounting and can fail once the
+// pool has reserved the memory), and code that must not change the device's
+// memory footprint between steps.  They pass device buffers for the inputs
+// and the output; the kernel's scratch (BF16 slices of A, the BF16 genotype
+// operand, per-row scales, an error word) lives in the file-scope array below,
+// which every GPU that loads this library holds until the process exits.
+//
+// Limits (the array's size, 8.4 MB): M <= 256, K <= 2048, N <= 512,
+// slices <= 6.  Every call shares the array and leaves its contents behind;
+// calls that overlap on the GPU (several streams or threads at once) race on
+// it and must be serialised by the caller.  The first call on a device looks
+// up the array's device address (cudaGetSymbolAddress) with that device
+// current; make that first call before any stream capture.
+// ---------------------------------------------------------------------------
+namespace fgls {
+namespace oz {
+constexpr int NA_MAX_M = 256, NA_MAX_K = 2048, NA_MAX_N = 512, NA_MAX_S = MAX_SLICES;
+constexpr size_t NA_A_BYTES = (size_t)NA_MAX_S * NA_MAX_M * NA_MAX_K * 2;   // BF16 slices
+constexpr size_t NA_G_BYTES = (size_t)NA_MAX_N * NA_MAX_K * 2;              // BF16 genotypes
+constexpr size_t NA_SCALE_BYTES = (size_t)NA_MAX_M * 8;                     // row scales
+constexpr size_t NA_BYTES = NA_A_BYTES + NA_G_BYTES + NA_SCALE_BYTES + 256;  // + error word
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
+
+constexpr int NA_MAX_DEVICES = 64;
+static void* g_noalloc_addr[NA_MAX_DEVICES];
+}  // namespace oz
+}  // namespace fgls
+
+extern "C" int fglsgpu_split_gemm_noalloc(int M, int K, int N, int slices, const double* dA, const double* dX,
+                                          double* dC, void* stream) {
+  using namespace fgls;
+  using namespace fgls::oz;
+  if (M <= 0 || M > NA_MAX_M || K <= 0 || K > NA_MAX_K || N <= 0 || N > NA_MAX_N || slices < 1 ||
+      slices > NA_MAX_S || !dA || !dX || !dC)
+    return FGLSGPU_EINVAL;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NA_MAX_DEVICES) return FGLSGPU_ENODEV;
+  if (!g_noalloc_addr[dev]) {
+    // set-up, once per device, with the device current: the host-side name of
+    // the array is not a device address
+    void* ptr = nullptr;
+    if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) return FGLSGPU_ECUDA;
+    if (cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) !=
+        cudaSuccess)
+      return FGLSGPU_ECUDA;
+    g_noalloc_addr[dev] = ptr;
+  }
+  unsigned char* base = (unsigned char*)g_noalloc_addr[dev];
+  OzakiPlan p;
+  p.n = K;
+  p.S = slices;
+  p.M = M;
+  p.Mpad = (M + BM - 1) / BM * BM;
+  p.Kpad = (K + BK - 1) / BK * BK;
+  p.Ncap = (N + BN - 1) / BN * BN;
+  p.A = (__nv_bfloat16*)base;
+  p.G = (__nv_bfloat16*)(base + NA_A_BYTES);
+  p.scale = (double*)(base + NA_A_BYTES + NA_G_BYTES);
+  p.err = (int*)(base + NA_A_BYTES + NA_G_BYTES + NA_SCALE_BYTES);
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t r = cudaSuccess;
+  auto chk = [&](cudaError_t e) {
+    if (r == cudaSuccess) r = e;
+  };
+  // the array keeps the previous call's contents: zero what must start at zero
+  // (slice and genotype padding, scales of padding rows, the error word)
+  chk(cudaMemsetAsync(p.A, 0, sizeof(__nv_bfloat16) * (size_t)slices * p.Mpad * p.Kpad, s));
+  chk(cudaMemsetAsync(p.G, 0, sizeof(__nv_bfloat16) * (size_t)p.Ncap * p.Kpad, s));
+  chk(cudaMemsetAsync(p.scale, 0, sizeof(double) * p.Mpad, s));
+  chk(cudaMemsetAsync(p.err, 0, sizeof(int), s));
+  if (r == cudaSuccess) chk(make_map(&p.mapA, p.A, p.Kpad, (long long)slices * p.Mpad, BM));
+  if (r == cudaSuccess) chk(make_map(&p.mapB, p.G, p.Kpad, p.Ncap, BN));
+  if (r == cudaSuccess) {
+    slice_rows_kernel<<<M, 256, 0, s>>>(K, M, dA, K, 0, slices, p.Mpad, p.Kpad, p.A, p.scale);
+    note_launch();
+    chk(cudaGetLastError());
+  }
+  if (r == cudaSuccess) chk(load_genotypes<double>(&p, s, dX, N));
+  if (r == cudaSuccess) {
+    // the output doubles as the int64 accumulator between passes
+    p.C = dC;
+    GemmArgs g;
+    g.M = M;
+    g.Mpad = p.Mpad;
+    g.N = N;
+    g.Kpad = p.Kpad;
+    g.S = slices;
+    g.tiles_m = p.Mpad / BM;
+    g.tiles_n = (N + BN - 1) / BN;
+    g.tri_rows = 0;
+    g.row_scale = p.scale;
+    g.C = dC;
+    g.ldc = M;
+    g.col0 = 0;
+    g.sq_rows = 0;
+    g.err = p.err;
+    ozaki_gemm_kernel<<<g.tiles_m * g.tiles_n, THREADS, SMEM_BYTES, s>>>(p.mapA, p.mapB, g);
+    note_launch();
+    chk(cudaGetLastError());
+  }
+  int herr = 0;
+  if (r == cudaSuccess) chk(cudaMemcpyAsync(&herr, p.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  if (r == cudaSuccess) chk(cudaStreamSynchronize(s));
+  p.A = nullptr;
+  p.G = nullptr;
+  p.scale = nullptr;
+  p.C = nullptr;
+  p.err = nullptr;
+  if (r != cudaSuccess) return FGLSGPU_ECUDA;
+  return herr ? FGLSGPU_ETIMEOUT : FGLSGPU_OK;
+}

@@ -37,7 +37,7 @@ EXPORTS = (
     "fglsgpu_run_block_device", "fglsgpu_run_block_device_u8", "fglsgpu_sync",
     "fglsgpu_get_res_sigma", "fglsgpu_get_eigen", "fglsgpu_stream", "fglsgpu_launch_count",
     "fglsgpu_last_error", "fglsgpu_version", "fglsgpu_selftest_split_gemm", "fglsgpu_set_precision",
-    "fglsgpu_profile", "fglsgpu_profile_read",
+    "fglsgpu_profile", "fglsgpu_profile_read", "fglsgpu_split_gemm_noalloc",
 )
 PROF_CLASSES = ("genotypes", "split_gemm", "selfgram", "solve", "fp64_gemm", "trsm", "gram", "spare")
 
@@ -87,6 +87,7 @@ def lib():
     L.fglsgpu_set_precision.argtypes = [P, I]
     L.fglsgpu_profile.argtypes = [P, I]
     L.fglsgpu_profile_read.argtypes = [P, P, P]
+    L.fglsgpu_split_gemm_noalloc.argtypes = [I, I, I, I, P, P, P, P]
     _lib = L
     return L
 

@@ -186,6 +186,21 @@ int fglsgpu_version(void);
 int fglsgpu_selftest_split_gemm(int M, int K, int N, int slices, const double *A, const double *X,
                                 double *C);
 
+/* The same split-precision GEMM for callers that may not allocate device
+ * memory (code running under a framework that owns the device through its
+ * own memory pool, or that must keep the device's footprint fixed).  All
+ * pointers are DEVICE pointers owned by the caller: A (M x K, row-major
+ * FP64), X (K x N, column-major genotypes), C (M x N, column-major FP64 out).
+ * The kernel's scratch lives in a fixed 8.4 MB array inside the library
+ * (held by every GPU that loads it): M <= 256, K <= 2048, N <= 512,
+ * slices <= 6, else FGLSGPU_EINVAL.  Runs on `stream` (a cudaStream_t, NULL
+ * for the default stream) and returns after it finished.  Calls share the
+ * array: calls that overlap on the GPU race; serialise them.  The first call
+ * on a device sets up the array's address and should come before any stream
+ * capture.  No counterpart in the reference. */
+int fglsgpu_split_gemm_noalloc(int M, int K, int N, int slices, const double *A, const double *X,
+                               double *C, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
