@@ -163,6 +163,19 @@ def aggregate_throughput(world, blocks_per_rank, snps_per_block, traits, seconds
     return world * blocks_per_rank * snps_per_block * traits / seconds
 
 
+def gemm_traffic(n, t, xb):
+    """DRAM bytes (read + write) of one split-GEMM launch of this workload, from
+    the committed ncu summary profiles/ozaki_gemm_n{n}_t{t}_xb{xb}.txt (its
+    line 'dram_bytes_per_launch: <bytes>'); None when no capture exists."""
+    f = os.path.join(ROOT, "profiles", f"ozaki_gemm_n{n}_t{t}_xb{xb}.txt")
+    if not os.path.exists(f):
+        return None
+    for line in open(f):
+        if line.startswith("dram_bytes_per_launch:"):
+            return float(line.split(":", 1)[1])
+    return None
+
+
 def rel_errors(B, V, Br, Vr):
     """beta error normwise per (trait, SNP) and on the SE scale; SE element-wise."""
     p = B.shape[-1]
@@ -337,14 +350,7 @@ def main():
     gemm_ms, gemm_n = prof["split_gemm"]
     achieved = flops_snp * xb * args.steps / (gemm_ms / 1e3) / 1e12
     peak = float(pk.get("bf16_tflops_sustained", FALLBACK_PEAKS["bf16_tflops_sustained"]))
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "split_gemm_traffic.json")
-    if os.path.exists(tf):
-        try:
-            tj = json.load(open(tf))
-            traffic = float(tj["dram_bytes_per_snp"]) * xb
-        except Exception:
-            traffic = None
+    traffic = gemm_traffic(n, t, xb)
 
     # all-FP64 device path on the same problem (same eigendecomposition)
     eng.set_precision("fp64")
@@ -373,6 +379,14 @@ def main():
     Bs = dBs.cpu().numpy().reshape(t, x64, p)
     Vs = dVs.cpu().numpy().reshape(t, x64, p, p).transpose(0, 1, 3, 2)
     nb, bs, se = rel_errors(Bs, Vs, B64, V64)
+    # p-values of the SNP coefficient from both paths (device kernel)
+    dP64 = torch.empty(t * x64 * WXR, dtype=torch.float64, device=dev)
+    dPs = torch.empty_like(dP64)
+    eng.pvalues_device(dB64.data_ptr(), dV64.data_ptr(), x64, x64 * p, x64 * p * p, dP64.data_ptr(), x64 * WXR)
+    eng.pvalues_device(dBs.data_ptr(), dVs.data_ptr(), x64, x64 * p, x64 * p * p, dPs.data_ptr(), x64 * WXR)
+    eng.sync()
+    P64, Ps = dP64.cpu().numpy(), dPs.cpu().numpy()
+    pv_rel = float(np.max(np.abs(Ps - P64) / np.maximum(P64, 1e-300)))
 
     # end to end through the public host API: pinned host genotypes in the
     # reference XR layout, results back in the B.out / V.out layout
@@ -418,7 +432,7 @@ def main():
             "fp64_path": {"value": fp64_value, "unit": UNIT, "snps": x64,
                           "speedup_split_vs_fp64": value / fp64_value},
             "split_vs_fp64_error": {"beta_normwise": nb, "beta_se_scaled": bs, "se_rel": se,
-                                    "snps": x64, "traits": t},
+                                    "pvalue_rel": pv_rel, "snps": x64, "traits": t},
             "kernel_ms": {k: v[0] for k, v in prof.items() if v[1]},
         },
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",

@@ -61,6 +61,11 @@ struct fglsgpu_engine {
   PEv pending[FGLSGPU_PROF_CLASSES]{};
   double prof_ms[FGLSGPU_PROF_CLASSES] = {0};
   long long prof_cnt[FGLSGPU_PROF_CLASSES] = {0};
+  // adjoint state (eigen, FP64): allocated by fglsgpu_adjoint_reset
+  double *aWc = nullptr, *aAYLc = nullptr, *aAYLs = nullptr, *atopc = nullptr, *atops = nullptr, *areml = nullptr;
+  double *aGYLc = nullptr, *aGYLs = nullptr, *aGRc = nullptr, *aGRs = nullptr, *acontrib = nullptr, *ag = nullptr;
+  double *agR = nullptr, *aacc = nullptr, *aU = nullptr, *aV2 = nullptr;
+  bool adj_ready = false;
 };
 
 namespace {
@@ -122,7 +127,9 @@ int reset_status(fglsgpu_engine* e) {
 void free_all(fglsgpu_engine* e) {
   void* ptrs[] = {e->dPhi, e->dL,   e->dZ,    e->dW,    e->dXL,   e->dY,    e->dh,    e->dsig, e->dWY,
                   e->dZtXL, e->dZtY, e->ddinv, e->dAYL, e->dtop, e->deigwork, e->dX[0], e->dX[1], e->dWork,
-                  e->dQ,   e->dGYL, e->dGR,  e->dB[0], e->dB[1], e->dV[0], e->dV[1], e->dU8, e->dst};
+                  e->dQ,   e->dGYL, e->dGR,  e->dB[0], e->dB[1], e->dV[0], e->dV[1], e->dU8, e->dst,
+                  e->aWc, e->aAYLc, e->aAYLs, e->atopc, e->atops, e->areml, e->aGYLc, e->aGYLs, e->aGRc,
+                  e->aGRs, e->acontrib, e->ag, e->agR, e->aacc, e->aU, e->aV2};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (e->hst) cudaFreeHost(e->hst);
@@ -558,6 +565,131 @@ int fglsgpu_set_precision(fglsgpu_engine* e, int precision) {
     ENG_TRY(e, cudaStreamSynchronize(e->comp), "split operands");
   }
   if (c.variant == FGLSGPU_VARIANT_CHOL) e->trait_sel = -1;  // re-select: the operands differ per path
+  return FGLSGPU_OK;
+}
+
+int fglsgpu_pvalues_device(fglsgpu_engine* e, const double* dB, const double* dV, int x_inc, long long b_trait_stride,
+                           long long v_trait_stride, double* dP, long long p_trait_stride) {
+  if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
+  if (!dB || !dV || !dP || x_inc <= 0) return fail(e, FGLSGPU_EINVAL, "invalid p-value arguments");
+  ENG_TRY(e, cudaSetDevice(e->cfg.device), "cudaSetDevice");
+  const int nt = e->cfg.variant == FGLSGPU_VARIANT_EIGEN ? e->cfg.t : 1;
+  ENG_TRY(e, snp_pvalues(e->comp, x_inc, nt, e->p, e->cfg.wXL, dB, b_trait_stride, dV, v_trait_stride, dP,
+                         p_trait_stride),
+          "p-values");
+  return FGLSGPU_OK;
+}
+
+// ---------------------------------------------------------------- adjoint
+int fglsgpu_adjoint_reset(fglsgpu_engine* e) {
+  if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
+  const fglsgpu_config& c = e->cfg;
+  if (c.variant != FGLSGPU_VARIANT_EIGEN || c.wXR != 1)
+    return fail(e, FGLSGPU_EINVAL, "the adjoint is defined for the eigen variant with wXR = 1");
+  if (!e->problem_set) return fail(e, FGLSGPU_ESTATE, "set_problem must precede the adjoint");
+  ENG_TRY(e, cudaSetDevice(c.device), "cudaSetDevice");
+  const long long n = c.n, t = c.t, xb = c.x_b, wXL = c.wXL, p = e->p;
+  if (!e->dWork) ENG_TRY(e, dalloc(&e->dWork, n * xb), "adjoint buffers");
+  if (!e->dQ) ENG_TRY(e, dalloc(&e->dQ, n * xb), "adjoint buffers");
+  if (!e->adj_ready) {
+    cudaError_t r = cudaSuccess;
+    auto chk = [&](cudaError_t x) {
+      if (r == cudaSuccess) r = x;
+    };
+    chk(dalloc(&e->aWc, n * 2 * t));
+    chk(dalloc(&e->aAYLc, n * t * (1 + wXL)));
+    chk(dalloc(&e->aAYLs, n * t * (1 + wXL)));
+    chk(dalloc(&e->atopc, t * (wXL + wXL * wXL)));
+    chk(dalloc(&e->atops, t * (wXL + wXL * wXL)));
+    chk(dalloc(&e->areml, 2 * t));
+    chk(dalloc(&e->aGYLc, xb * t * (1 + wXL)));
+    chk(dalloc(&e->aGYLs, xb * t * (1 + wXL)));
+    chk(dalloc(&e->aGRc, xb * t));
+    chk(dalloc(&e->aGRs, xb * t));
+    chk(dalloc(&e->acontrib, 2 * t * xb));
+    chk(dalloc(&e->ag, t * xb * p));
+    chk(dalloc(&e->agR, xb * t));
+    chk(dalloc(&e->aacc, 2 * t + t * wXL));
+    chk(dalloc(&e->aU, n * t));
+    chk(dalloc(&e->aV2, n * t));
+    if (r != cudaSuccess) return cuda_fail(e, r, "adjoint buffers");
+    e->adj_ready = true;
+  }
+  cudaStream_t s = e->comp;
+  ENG_TRY(e, cudaMemsetAsync(e->aacc, 0, sizeof(double) * (2 * t + t * wXL), s), "adjoint reset");
+  ENG_TRY(e, cudaMemsetAsync(e->aU, 0, sizeof(double) * n * t, s), "adjoint reset");
+  ENG_TRY(e, adjoint_traits(s, c.n, c.t, c.wXL, e->dW, e->dh, e->dsig, e->dZtXL, e->dZtY, e->ddinv, e->aWc,
+                            e->aAYLc, e->aAYLs, e->atopc, e->atops, e->areml),
+          "adjoint weights");
+  ENG_TRY(e, cudaStreamSynchronize(s), "adjoint reset");
+  return FGLSGPU_OK;
+}
+
+int fglsgpu_adjoint_block_device(fglsgpu_engine* e, const double* dXR, int x, const double* dBbar, long long bstr) {
+  if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
+  if (!e->adj_ready) return fail(e, FGLSGPU_ESTATE, "fglsgpu_adjoint_reset must precede adjoint blocks");
+  const fglsgpu_config& c = e->cfg;
+  if (x <= 0 || x > c.x_b || !dXR || !dBbar) return fail(e, FGLSGPU_EINVAL, "invalid adjoint block");
+  ENG_TRY(e, cudaSetDevice(c.device), "cudaSetDevice");
+  const int n = c.n, t = c.t, wXL = c.wXL, p = e->p, nq = t * (1 + wXL);
+  cudaStream_t s = e->comp;
+  // recompute R = Z^T X and the d-, c- and s-weighted Gram blocks (never stored per SNP)
+  ENG_TRY(e, dgemm(s, true, false, n, x, n, 1.0, e->dZ, n, dXR, n, 0.0, e->dWork, n), "Z^T XR");
+  ENG_TRY(e, quad_products(s, n, x, 1, e->dWork, n, e->dQ, n), "quad");
+  ENG_TRY(e, dgemm(s, true, false, x, nq, n, 1.0, e->dWork, n, e->dAYL, n, 0.0, e->dGYL, x), "gram");
+  ENG_TRY(e, dgemm(s, true, false, x, t, n, 1.0, e->dQ, n, e->ddinv, n, 0.0, e->dGR, x), "gram");
+  ENG_TRY(e, dgemm(s, true, false, x, nq, n, 1.0, e->dWork, n, e->aAYLc, n, 0.0, e->aGYLc, x), "gram c");
+  ENG_TRY(e, dgemm(s, true, false, x, t, n, 1.0, e->dQ, n, e->aWc, n, 0.0, e->aGRc, x), "gram c");
+  ENG_TRY(e, dgemm(s, true, false, x, nq, n, 1.0, e->dWork, n, e->aAYLs, n, 0.0, e->aGYLs, x), "gram s");
+  ENG_TRY(e, dgemm(s, true, false, x, t, n, 1.0, e->dQ, n, e->aWc + (long long)n * t, n, 0.0, e->aGRs, x),
+          "gram s");
+  ENG_TRY(e, adjoint_snps(s, p, x, t, wXL, e->dtop, e->dGYL, e->dGR, e->atopc, e->aGYLc, e->aGRc, e->atops,
+                          e->aGYLs, e->aGRs, dBbar, bstr, e->acontrib, e->ag, e->dst),
+          "adjoint solve");
+  ENG_TRY(e, adjoint_reduce(s, x, t, p, wXL, e->acontrib, e->ag, e->aacc, e->agR), "adjoint reduce");
+  // U += R gR  (the SNP part of sum_i V_i g_i, accumulated over blocks)
+  ENG_TRY(e, dgemm(s, false, false, n, t, x, 1.0, e->dWork, n, e->agR, x, 1.0, e->aU, n), "dy accumulate");
+  return FGLSGPU_OK;
+}
+
+int fglsgpu_adjoint_read(fglsgpu_engine* e, double* dh, double* dsigma, double* dY) {
+  if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
+  if (!e->adj_ready) return fail(e, FGLSGPU_ESTATE, "no adjoint accumulated");
+  const fglsgpu_config& c = e->cfg;
+  ENG_TRY(e, cudaSetDevice(c.device), "cudaSetDevice");
+  const int n = c.n, t = c.t;
+  cudaStream_t s = e->comp;
+  int rc = check_status(e, "adjoint");
+  if (rc) return rc;
+  if (dY) {
+    ENG_TRY(e, adjoint_ybar(s, n, t, c.wXL, e->ddinv, e->dZtXL, e->aacc, e->aU, e->aV2), "dy");
+    // dY = Z V2 (original basis), through dQ as scratch (n x t <= n x x_b when t <= x_b)
+    double* out = e->dQ;
+    if ((long long)t > (long long)c.x_b) return fail(e, FGLSGPU_EINVAL, "dy needs t <= x_b");
+    ENG_TRY(e, dgemm(s, false, false, n, t, n, 1.0, e->dZ, n, e->aV2, n, 0.0, out, n), "dy");
+    ENG_TRY(e, cudaMemcpyAsync(dY, out, sizeof(double) * (size_t)n * t, cudaMemcpyDeviceToHost, s), "dy");
+  }
+  std::vector<double> acc(2 * t);
+  ENG_TRY(e, cudaMemcpyAsync(acc.data(), e->aacc, sizeof(double) * 2 * t, cudaMemcpyDeviceToHost, s), "dh");
+  ENG_TRY(e, cudaStreamSynchronize(s), "adjoint read");
+  for (int j = 0; j < t; j++) {
+    if (dh) dh[j] = acc[j];
+    if (dsigma) dsigma[j] = acc[t + j];
+  }
+  return FGLSGPU_OK;
+}
+
+int fglsgpu_reml(fglsgpu_engine* e, double* loglik, double* dloglik_dh) {
+  if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
+  if (!e->adj_ready) return fail(e, FGLSGPU_ESTATE, "fglsgpu_adjoint_reset computes the REML terms first");
+  const int t = e->cfg.t;
+  ENG_TRY(e, cudaSetDevice(e->cfg.device), "cudaSetDevice");
+  std::vector<double> r(2 * t);
+  ENG_TRY(e, cudaMemcpy(r.data(), e->areml, sizeof(double) * 2 * t, cudaMemcpyDeviceToHost), "reml");
+  for (int j = 0; j < t; j++) {
+    if (loglik) loglik[j] = r[j];
+    if (dloglik_dh) dloglik_dh[j] = r[t + j];
+  }
   return FGLSGPU_OK;
 }
 

@@ -53,6 +53,23 @@ size_t dc_workspace_bytes(int n);
 cudaError_t dc_tridiag_eig(cudaStream_t s, int n, double* d, double* e, double* W, double* V, void* work,
                            int* fail_dev, long long* launches);
 
+// Two-sided normal p-values of the SNP coefficients from B and V (fgls_snp.cu).
+cudaError_t snp_pvalues(cudaStream_t s, int x, int t, int p, int wXL, const double* B, long long bstride,
+                        const double* V, long long vstride, double* P, long long pstride);
+
+// Adjoint of the eigen variant (fgls_adjoint.cu); layouts in that file.
+cudaError_t adjoint_traits(cudaStream_t s, int n, int t, int wXL, const double* W, const double* h,
+                           const double* sigma, const double* ZtXL, const double* ZtY, const double* dinv,
+                           double* Wc, double* AYLc, double* AYLs, double* topc, double* tops, double* reml);
+cudaError_t adjoint_snps(cudaStream_t s, int p, int x, int t, int wXL, const double* top, const double* GYL,
+                         const double* GR, const double* topc, const double* GYLc, const double* GRc,
+                         const double* tops, const double* GYLs, const double* GRs, const double* Bbar,
+                         long long bstride, double* contrib, double* g, DevStatus* st);
+cudaError_t adjoint_reduce(cudaStream_t s, int x, int t, int p, int wXL, const double* contrib, const double* g,
+                           double* acc, double* gR);
+cudaError_t adjoint_ybar(cudaStream_t s, int n, int t, int wXL, const double* dinv, const double* ZtXL,
+                         const double* acc, const double* U, double* V2);
+
 // Genotype conversion: FP64 or u8 hard calls -> FP64 (device to device).
 cudaError_t u8_to_f64(cudaStream_t s, const unsigned char* in, double* out, long long count);
 

@@ -11,13 +11,13 @@
 // P_s = d_s G^T is an integer with |P_s| <= 128 * 2 * K < 2^22 for K <= 16383,
 // so FP32 accumulation in TMEM is exact and the result is bit-reproducible.
 //
-// Kernel ozaki_gemm_kernel (one 128 x 256 output tile per CTA, 6 warps):
+// Kernel ozaki_gemm_kernel (one 128 x 256 output tile per CTA, 10 warps):
 //   warp 0      TMA producer: per K-step of 64, two A-slice tiles (128 x 64)
 //               and one genotype tile (256 x 64), 128B-swizzled, 3 stages.
 //   warp 1      allocates 512 TMEM columns and issues tcgen05.mma
 //               (kind::f16, BF16 x BF16 -> F32, M=128 N=256 K=16): slice 2p
 //               into columns [0,256), slice 2p+1 into [256,512).
-//   warps 2-5   epilogue: tcgen05.ld the two accumulators, combine them
+//   warps 2-9   epilogue: tcgen05.ld the two accumulators, combine them
 //               exactly in int32 (q = P_2p * 256 + P_2p+1), Horner-accumulate
 //               the passes in int64 in the output buffer (V = V * 2^16 + q),
 //               and on the last pass write V * 2^(e_r - 15 - 16 (passes-1))
@@ -54,7 +54,7 @@ constexpr int A_TILE = BM * BK * 2;               // 16 KB
 constexpr int B_TILE = BN * BK * 2;               // 32 KB
 constexpr int STAGE_BYTES = 2 * A_TILE + B_TILE;  // 64 KB
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
-constexpr int THREADS = 192;
+constexpr int THREADS = 320;  // producer, MMA, 8 epilogue warps
 constexpr int MAX_SLICES = 6;
 constexpr int GROUP_M = 8;
 
@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       mbar_init(&empty[s], 1);
     }
     mbar_init(tfull, 1);
-    mbar_init(tempty, 128);
+    mbar_init(tempty, THREADS - 64);
     mbar_init(drain, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -315,38 +315,53 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
     __syncwarp();
   } else {
-    // epilogue: warps 2..5 -> TMEM lane quarter (warp % 4)
+    // epilogue: warps 2..9.  Warp w reads TMEM lane quarter w % 4 (the
+    // quarter a warp may access is fixed by its rank modulo 4) and column
+    // half (w - 2) / 4; thread = one output row.
     const int q = warp & 3;
+    const int cbeg = ((warp - 2) >> 2) * (BN / 2);
     const int row = q * 32 + lane;
     const int r = m0 + row;
     const bool rvalid = r < g.M;
     const double scale = rvalid ? g.row_scale[r] : 0.0;
     const bool sq = r < g.sq_rows;
     const float fscale = (float)scale;  // power of two: exact while >= 2^-149
+    const int ncols = rvalid ? min(BN, g.N - n0) : 0;  // valid columns of this tile for this row
+    long long* crow = (long long*)(g.C + (long long)r + (long long)(g.col0 + n0) * g.ldc);
+    const int cend = min(cbeg + BN / 2, ncols);
     for (int p = 0; p < passes; p++) {
       const bool two = 2 * p + 1 < g.S;
       const bool last = p == passes - 1;
+      // pull this row's partial sums into L2 while the pass's MMAs run
+      if (p > 0)
+        for (int c = cbeg; c < cend; c++)
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(crow + (long long)c * g.ldc));
       int ok = 1;
       if (lane == 0) ok = mbar_wait(tfull, p & 1, abort_flag, g.err, 4) ? 1 : 0;
       ok = __shfl_sync(0xffffffffu, ok, 0);  // warp-uniform: tcgen05.ld is .sync.aligned
       if (!ok) break;
       tc_fence_after();
 #pragma unroll 1
-      for (int ch = 0; ch < BN / 32; ch++) {
+      for (int ch = 0; ch < BN / 64; ch++) {
+        const int c0 = cbeg + ch * 32;
+        long long prev[32];
+        if (p > 0) {
+          // all 32 partial sums in flight at once, before the TMEM reads
+#pragma unroll
+          for (int j = 0; j < 32; j++) prev[j] = (c0 + j < cend) ? __ldcg(crow + (long long)(c0 + j) * g.ldc) : 0;
+        }
         uint32_t v0[32], v1[32];
-        const uint32_t ta = tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)(ch * 32);
+        const uint32_t ta = tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
         tmem_ld32(ta, v0);
         if (two) tmem_ld32(ta + 256, v1);
         tmem_ld_wait();
-        if (!rvalid) continue;
 #pragma unroll
         for (int j = 0; j < 32; j++) {
-          const int col = n0 + ch * 32 + j;
-          if (col >= g.N) break;
+          if (c0 + j >= cend) break;
           int qv = __float2int_rn(__uint_as_float(v0[j])) * 256;
           if (two) qv += __float2int_rn(__uint_as_float(v1[j]));
-          long long* cp = (long long*)(g.C + (long long)r + (long long)(g.col0 + col) * g.ldc);
-          long long V = (p == 0) ? (long long)qv : (*cp) * 65536LL + (long long)qv;
+          long long* cp = crow + (long long)(c0 + j) * g.ldc;
+          const long long V = (p == 0) ? (long long)qv : prev[j] * 65536LL + (long long)qv;
           if (!last)
             *cp = V;
           else if (sq)

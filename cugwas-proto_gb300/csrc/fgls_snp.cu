@@ -454,3 +454,40 @@ cudaError_t snp_solve(cudaStream_t s, int p, int x, int t, int wXL, const double
 }
 
 }  // namespace fgls
+
+// ---------------------------------------------------------------------------
+// p-values of the SNP coefficients (no counterpart in the reference, which
+// emits beta and V only): two-sided normal test on z = beta_k / SE_k,
+// p = erfc(|z| / sqrt 2), for the wXR SNP columns k = wXL .. p-1 of every
+// (trait, SNP).  B, V in the layouts written by snp_solve.
+// ---------------------------------------------------------------------------
+namespace fgls {
+namespace {
+__global__ void pvalues_kernel(int x, int t, int p, int wXL, const double* __restrict__ B, long long bstride,
+                               const double* __restrict__ V, long long vstride, double* __restrict__ P,
+                               long long pstride) {
+  const int wXR = p - wXL;
+  const long long total = (long long)x * t * wXR;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(e % wXR);
+    const long long r = e / wXR;
+    const int i = (int)(r % x), j = (int)(r / x);
+    const int k = wXL + c;
+    const double beta = B[(long long)j * bstride + (long long)i * p + k];
+    const double se = V[(long long)j * vstride + (long long)i * p * p + k + k * p];  // diagonal = SE
+    P[(long long)j * pstride + (long long)i * wXR + c] = erfc(fabs(beta / se) * 0.70710678118654752440);
+  }
+}
+}  // namespace
+
+cudaError_t snp_pvalues(cudaStream_t s, int x, int t, int p, int wXL, const double* B, long long bstride,
+                        const double* V, long long vstride, double* P, long long pstride) {
+  const long long total = (long long)x * t * (p - wXL);
+  const int blocks = (int)std::min<long long>((total + 255) / 256, 152LL * 32);
+  if (blocks <= 0) return cudaSuccess;
+  pvalues_kernel<<<blocks, 256, 0, s>>>(x, t, p, wXL, B, bstride, V, vstride, P, pstride);
+  note_launch();
+  return cudaGetLastError();
+}
+}  // namespace fgls

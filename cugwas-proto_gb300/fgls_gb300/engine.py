@@ -37,7 +37,8 @@ EXPORTS = (
     "fglsgpu_run_block_device", "fglsgpu_run_block_device_u8", "fglsgpu_sync",
     "fglsgpu_get_res_sigma", "fglsgpu_get_eigen", "fglsgpu_stream", "fglsgpu_launch_count",
     "fglsgpu_last_error", "fglsgpu_version", "fglsgpu_selftest_split_gemm", "fglsgpu_set_precision",
-    "fglsgpu_profile", "fglsgpu_profile_read", "fglsgpu_split_gemm_noalloc",
+    "fglsgpu_profile", "fglsgpu_profile_read", "fglsgpu_split_gemm_noalloc", "fglsgpu_adjoint_reset",
+    "fglsgpu_adjoint_block_device", "fglsgpu_adjoint_read", "fglsgpu_reml", "fglsgpu_pvalues_device",
 )
 PROF_CLASSES = ("genotypes", "split_gemm", "selfgram", "solve", "fp64_gemm", "trsm", "gram", "spare")
 
@@ -88,6 +89,11 @@ def lib():
     L.fglsgpu_profile.argtypes = [P, I]
     L.fglsgpu_profile_read.argtypes = [P, P, P]
     L.fglsgpu_split_gemm_noalloc.argtypes = [I, I, I, I, P, P, P, P]
+    L.fglsgpu_adjoint_reset.argtypes = [P]
+    L.fglsgpu_adjoint_block_device.argtypes = [P, P, I, P, LL]
+    L.fglsgpu_adjoint_read.argtypes = [P, P, P, P]
+    L.fglsgpu_reml.argtypes = [P, P, P]
+    L.fglsgpu_pvalues_device.argtypes = [P, P, P, I, LL, LL, P, LL]
     _lib = L
     return L
 
@@ -175,6 +181,30 @@ class Engine:
         cnt = np.zeros(len(PROF_CLASSES), dtype=np.int64)
         self._check(self.L.fglsgpu_profile_read(self._h, _ptr(ms), _ptr(cnt)))
         return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(PROF_CLASSES)}
+
+    def pvalues_device(self, b_ptr, v_ptr, x, bstride, vstride, p_ptr, pstride):
+        self._check(self.L.fglsgpu_pvalues_device(self._h, C.c_void_p(b_ptr), C.c_void_p(v_ptr), int(x), int(bstride),
+                                                  int(vstride), C.c_void_p(p_ptr), int(pstride)))
+
+    def adjoint_reset(self):
+        self._check(self.L.fglsgpu_adjoint_reset(self._h))
+
+    def adjoint_block_device(self, xr_ptr, x, bbar_ptr, bbar_trait_stride):
+        self._check(self.L.fglsgpu_adjoint_block_device(self._h, C.c_void_p(xr_ptr), int(x), C.c_void_p(bbar_ptr),
+                                                        int(bbar_trait_stride)))
+
+    def adjoint_read(self):
+        """(dL/dh (t), dL/dsigma (t), dL/dY (n x t))"""
+        dh, ds = np.empty(self.t), np.empty(self.t)
+        dY = np.empty((self.n, self.t), order="F")
+        self._check(self.L.fglsgpu_adjoint_read(self._h, _ptr(dh), _ptr(ds), _ptr(dY)))
+        return dh, ds, dY
+
+    def reml(self):
+        """(loglik (t), dloglik/dh (t)) of the null model."""
+        ll, dll = np.empty(self.t), np.empty(self.t)
+        self._check(self.L.fglsgpu_reml(self._h, _ptr(ll), _ptr(dll)))
+        return ll, dll
 
     def sync(self):
         self._check(self.L.fglsgpu_sync(self._h))

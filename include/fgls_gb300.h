@@ -144,6 +144,32 @@ int fglsgpu_get_res_sigma(fglsgpu_engine *e, double *out);
  * Phi computed by set_problem (eigen variant); either pointer may be NULL. */
 int fglsgpu_get_eigen(fglsgpu_engine *e, double *W, double *Z);
 
+/* Two-sided normal p-values p = erfc(|beta_k / SE_k| / sqrt 2) of the SNP
+ * coefficients (k = wXL .. p-1) of a block's results (device pointers in
+ * the B/V layouts above); P holds x_inc * wXR values per trait at
+ * P + j*p_trait_stride.  Runs on the engine stream.  No counterpart in the
+ * reference (it emits beta and V only). */
+int fglsgpu_pvalues_device(fglsgpu_engine *e, const double *dB, const double *dV, int x_inc,
+                           long long b_trait_stride, long long v_trait_stride, double *dP,
+                           long long p_trait_stride);
+
+/* ---- adjoint of fgls_eigen (FP64, wXR = 1) and the null-model REML ----
+ * No counterpart in the reference (it computes no derivatives).  With a
+ * cotangent Bbar for the betas (same layout as B), the vector-Jacobian
+ * products sum_ij Bbar_ij . dbeta_ij/dh_j, .../dsigma_j and .../dY are
+ * accumulated over blocks: reset, one call per block (device pointers, the
+ * block's genotypes and its Bbar slice with the given trait stride), read
+ * (host outputs; dY is n x t in the Y.in orientation, any pointer may be
+ * NULL).  Gram blocks are recomputed per block, never stored per SNP. */
+int fglsgpu_adjoint_reset(fglsgpu_engine *e);
+int fglsgpu_adjoint_block_device(fglsgpu_engine *e, const double *dXR, int x_inc, const double *dBbar,
+                                 long long bbar_trait_stride);
+int fglsgpu_adjoint_read(fglsgpu_engine *e, double *dh, double *dsigma, double *dY);
+/* Null-model REML log-likelihood per trait (sigma given, constants dropped)
+ *   l(h) = -1/2 [ log det M + log det(XL^T M^-1 XL) + r^T M^-1 r ]
+ * and dl/dh_j; valid after fglsgpu_adjoint_reset. */
+int fglsgpu_reml(fglsgpu_engine *e, double *loglik, double *dloglik_dh);
+
 /* Switches a live engine between FGLSGPU_PREC_FP64 and FGLSGPU_PREC_SPLIT
  * without redoing set_problem (eigen keeps its eigendecomposition; chol
  * needs select_trait again). */

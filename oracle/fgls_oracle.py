@@ -224,3 +224,65 @@ def compare(B, V, Bref, Vref):
         "upper_abs_max": upper_max,
         "finite": bool(np.isfinite(B).all() and np.isfinite(V).all()),
     }
+
+
+# ---------------------------------------------------------------------------
+# Derivatives (no counterpart in the reference): FP64 CPU reference for the
+# adjoint of the eigen variant and the null-model REML log-likelihood.
+# ---------------------------------------------------------------------------
+
+def eigen_betas(Z, W, XL, Y, h, sigma, XR):
+    """beta (t, m, p) of fgls_eigen for wXR = 1 in the d-weighted form
+    S = sum_l d_l v_l v_l^T, b = sum_l d_l v_l ytil_l."""
+    ZtXL, ZtY, R = Z.T @ XL, Z.T @ Y, Z.T @ XR
+    t, m, wXL = Y.shape[1], XR.shape[1], XL.shape[1]
+    out = np.zeros((t, m, wXL + 1))
+    for j in range(t):
+        d = 1.0 / (sigma[j] * h[j] * W + sigma[j] * (1 - h[j]))
+        V = np.concatenate([np.broadcast_to(ZtXL[None], (m,) + ZtXL.shape), R.T[:, :, None]], axis=2)  # m x n x p
+        S = np.einsum("mlp,l,mlq->mpq", V, d, V)
+        b = np.einsum("mlp,l,l->mp", V, d, ZtY[:, j])
+        out[j] = np.linalg.solve(S, b[..., None])[..., 0]
+    return out
+
+
+def eigen_adjoint(Z, W, XL, Y, h, sigma, XR, Bbar):
+    """(dL/dh (t), dL/dsigma (t), dL/dY (n x t)) for L = sum Bbar * beta."""
+    ZtXL, ZtY, R = Z.T @ XL, Z.T @ Y, Z.T @ XR
+    t, m, wXL = Y.shape[1], XR.shape[1], XL.shape[1]
+    dh, ds, dY = np.zeros(t), np.zeros(t), np.zeros((Z.shape[0], t))
+    V = np.concatenate([np.broadcast_to(ZtXL[None], (m,) + ZtXL.shape), R.T[:, :, None]], axis=2)
+    for j in range(t):
+        s, hj = sigma[j], h[j]
+        d = 1.0 / (s * hj * W + s * (1 - hj))
+        c = -s * (W - 1.0) * d * d
+        sg = -d / s
+        S = np.einsum("mlp,l,mlq->mpq", V, d, V)
+        b = np.einsum("mlp,l,l->mp", V, d, ZtY[:, j])
+        beta = np.linalg.solve(S, b[..., None])[..., 0]
+        g = np.linalg.solve(S, Bbar[j][..., None])[..., 0]
+        r = ZtY[:, j][None, :] - np.einsum("mlp,mp->ml", V, beta)       # m x n
+        Vg = np.einsum("mlp,mp->ml", V, g)                               # m x n
+        dh[j] = np.sum(Vg * r * c[None, :])
+        ds[j] = np.sum(Vg * r * sg[None, :])
+        dY[:, j] = Z @ (d * Vg.sum(0))
+    return dh, ds, dY
+
+
+def reml(Z, W, XL, Y, h, sigma):
+    """Null-model REML log-likelihood per trait (sigma given, constants
+    dropped) and its h-derivative, in the eigenbasis of Phi."""
+    ZtXL, ZtY = Z.T @ XL, Z.T @ Y
+    t = Y.shape[1]
+    ll, dll = np.zeros(t), np.zeros(t)
+    for j in range(t):
+        s, hj = sigma[j], h[j]
+        d = 1.0 / (s * hj * W + s * (1 - hj))
+        c = -s * (W - 1.0) * d * d
+        Vt = (ZtXL * d[:, None]).T @ ZtXL
+        bL = np.linalg.solve(Vt, (ZtXL * d[:, None]).T @ ZtY[:, j])
+        r0 = ZtY[:, j] - ZtXL @ bL
+        Vc = (ZtXL * c[:, None]).T @ ZtXL
+        ll[j] = -0.5 * (-np.sum(np.log(d)) + np.linalg.slogdet(Vt)[1] + np.sum(d * r0 * r0))
+        dll[j] = -0.5 * (-np.sum(c / d) + np.trace(np.linalg.solve(Vt, Vc)) + np.sum(c * r0 * r0))
+    return ll, dll

@@ -175,3 +175,25 @@ def test_cli_driver_reference_interface():
     assert r.stdout.strip().isdigit()  # mean ms per repetition
     B, V = datagen.read_outputs(d, pb.m, pb.t, pb.p)
     check(O.compare(B, V, Bref, Vref), CHOL_TOL)
+
+
+def test_pvalues_match_normal_tail():
+    import torch
+    from scipy.stats import norm
+    from fgls_gb300 import Engine, datagen
+    pb = datagen.make_problem(200, 64, 2, wXL=2, wXR=2, seed=4, hsig_uniform=True)
+    p, x = pb.p, pb.m
+    with Engine(pb.n, 2, 2, 2, x, variant="eigen") as e:
+        e.set_problem(pb.Phi, pb.XL, pb.Y, pb.h, pb.sigma)
+        dX = torch.from_numpy(np.asfortranarray(pb.XR).T.copy()).cuda()
+        dB = torch.empty(2 * x * p, dtype=torch.float64, device="cuda")
+        dV = torch.empty(2 * x * p * p, dtype=torch.float64, device="cuda")
+        dP = torch.empty(2 * x * 2, dtype=torch.float64, device="cuda")
+        e.run_block_device(dX.data_ptr(), x, dB.data_ptr(), dV.data_ptr(), x * p, x * p * p)
+        e.pvalues_device(dB.data_ptr(), dV.data_ptr(), x, x * p, x * p * p, dP.data_ptr(), x * 2)
+        e.sync()
+    B = dB.cpu().numpy().reshape(2, x, p)
+    V = dV.cpu().numpy().reshape(2, x, p, p).transpose(0, 1, 3, 2)
+    P = dP.cpu().numpy().reshape(2, x, 2)
+    z = B[..., 2:] / np.stack([V[..., 2, 2], V[..., 3, 3]], axis=-1)
+    assert np.allclose(P, 2 * norm.sf(np.abs(z)), rtol=1e-12, atol=1e-300)
