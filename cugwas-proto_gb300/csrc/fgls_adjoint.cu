@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(256) adj_trait_kernel(int n, int t, int wXL, c
   const int j = blockIdx.x;
   __shared__ double red[33];
   __shared__ double V[FGLS_MAX_P * FGLS_MAX_P], Vc[FGLS_MAX_P * FGLS_MAX_P], bt[FGLS_MAX_P], bl[FGLS_MAX_P];
-  const double h = hh[j], s = ss[j];
+  const double s = ss[j];  // dd/dh needs only sigma and w: d = 1/(s (h w + 1 - h))
   const double* y = ZtY + (long long)j * n;
   const double* d = dinv + (long long)j * n;
   const int tw = wXL + wXL * wXL;

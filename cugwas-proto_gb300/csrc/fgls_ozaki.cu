@@ -31,7 +31,7 @@
 //          Gram terms x~^T y~_j and x~^T XL~_j directly (one-sided: the exact
 //          genotypes are the other operand).  The quadratic terms
 //          sum_l R_l^2 d_j(l) run in double-FP32 (error-free products and
-//          sums) on the CUDA cores: selfgram_kernel.
+//          sums) on the CUDA cores: quad_gram (fgls_selfgram.cu).
 //   chol:  A = [L^-1 ; U^T], U = L^-T [y~ | XL~].
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -43,6 +43,7 @@
 #include "fgls_common.cuh"
 #include "fgls_kernels.cuh"
 #include "fgls_ozaki.cuh"
+#include "fgls_selfgram.cuh"
 
 namespace fgls {
 
@@ -456,135 +457,8 @@ __global__ void transpose_kernel(int n, const double* __restrict__ A, double* __
 }
 
 // ---------------------------------------------------------------------------
-// Quadratic Gram terms in double-FP32:
-//   GR[i + j*ldg] = sum_l A[l,i] * D[l,j],   A = R^2 as float pairs written by
-//   the GEMM epilogue (C rows [0, n), 8 bytes each), D = d_j as float pairs.
-// All terms are non-negative (no cancellation).  Each product is error-free
-// (p + pe = ah*dh exactly, by fma) and its cross terms ah*dl + al*dh go to the
-// low accumulator.  The high accumulator starts at a power of two B_ij no
-// smaller than any term (max_l ah[l,i] * max_l dh[l,j], rounded up), so every
-// addition satisfies |s| >= |p| and Fast2Sum (3 ops) is exact.  Every 64 rows
-// the chunk (offset removed exactly) is folded into an outer (H, L) pair by
-// TwoSum, so the FP32 low parts never sum more than 64 rounding errors of one
-// chunk: relative error ~1e-14 at n = 10^4 (a single running pair reaches
-// ~1e-11 there).  9 FP32 operations per term.
-// CTA tile 64 SNPs x 112 traits (16 x 16 threads, 4 x 7 each), 32-row chunks.
+// Weights of the quadratic Gram terms (fgls_selfgram.cu) as float pairs.
 // ---------------------------------------------------------------------------
-constexpr int QG_I = 64, QG_J = 112, QG_L = 32, QG_RI = 4, QG_RJ = 7, QG_FOLD = 64;
-
-// Knuth's TwoSum: s + e == a + b exactly
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-  s = __fadd_rn(a, b);
-  const float bp = __fsub_rn(s, a);
-  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
-}
-
-__device__ __forceinline__ float pow2_ceil(float v) {
-  // smallest power of two >= v (v > 0, finite)
-  return __int_as_float((__float_as_int(v) + 0x007FFFFF) & 0x7F800000);
-}
-
-// amax[i] = max_l A[l, i].x  (one warp per column)
-__global__ void colmax_kernel(int n, int x, const float2* __restrict__ A, long long lda, float* __restrict__ amax) {
-  const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (i >= x) return;
-  float m = 0.0f;
-  for (int l = lane; l < n; l += 32) m = fmaxf(m, A[l + (long long)i * lda].x);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if (lane == 0) amax[i] = m;
-}
-
-__global__ void __launch_bounds__(256) selfgram_kernel(int n, int x, int t, const float2* __restrict__ A,
-                                                       long long lda, const float* __restrict__ amax,
-                                                       const float2* __restrict__ D, long long ldd,
-                                                       const float* __restrict__ dmax, double* __restrict__ GR,
-                                                       long long ldg) {
-  __shared__ float2 As[QG_L][QG_I];
-  __shared__ float2 Bs[QG_L][QG_J];
-  const int i0 = blockIdx.x * QG_I, j0 = blockIdx.y * QG_J;
-  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-  // inner (sh, sl): one 64-row chunk from the offset; outer (H, L): the fold
-  float sh[QG_RI][QG_RJ], sl[QG_RI][QG_RJ], H[QG_RI][QG_RJ], L[QG_RI][QG_RJ];
-  auto offset = [&](int a, int b) {
-    const int i = i0 + ty + 16 * a, j = j0 + tx + 16 * b;
-    const float bound = ((i < x) ? amax[i] : 0.0f) * ((j < t) ? dmax[j] : 0.0f);
-    return bound > 0.0f ? pow2_ceil(bound) : 0.0f;
-  };
-#pragma unroll
-  for (int a = 0; a < QG_RI; a++)
-#pragma unroll
-    for (int b = 0; b < QG_RJ; b++) {
-      sh[a][b] = offset(a, b);
-      sl[a][b] = H[a][b] = L[a][b] = 0.0f;
-    }
-  for (int l0 = 0; l0 < n; l0 += QG_L) {
-    __syncthreads();
-    for (int e = threadIdx.x; e < QG_L * QG_I; e += 256) {
-      const int l = e % QG_L, i = e / QG_L;
-      float2 v = make_float2(0.f, 0.f);
-      if (l0 + l < n && i0 + i < x) v = A[(l0 + l) + (long long)(i0 + i) * lda];
-      As[l][i] = v;
-    }
-    for (int e = threadIdx.x; e < QG_L * QG_J; e += 256) {
-      const int l = e % QG_L, j = e / QG_L;
-      float2 v = make_float2(0.f, 0.f);
-      if (l0 + l < n && j0 + j < t) v = D[(l0 + l) + (long long)(j0 + j) * ldd];
-      Bs[l][j] = v;
-    }
-    __syncthreads();
-#pragma unroll 4
-    for (int l = 0; l < QG_L; l++) {
-      float2 av[QG_RI], bv[QG_RJ];
-#pragma unroll
-      for (int a = 0; a < QG_RI; a++) av[a] = As[l][ty + 16 * a];
-#pragma unroll
-      for (int b = 0; b < QG_RJ; b++) bv[b] = Bs[l][tx + 16 * b];
-#pragma unroll
-      for (int a = 0; a < QG_RI; a++)
-#pragma unroll
-        for (int b = 0; b < QG_RJ; b++) {
-          const float p = __fmul_rn(av[a].x, bv[b].x);
-          const float pe = fmaf(av[a].x, bv[b].x, -p);
-          float lo = fmaf(av[a].x, bv[b].y, sl[a][b]);
-          lo = fmaf(av[a].y, bv[b].x, lo);
-          const float s2 = __fadd_rn(sh[a][b], p);
-          const float err = __fsub_rn(p, __fsub_rn(s2, sh[a][b]));
-          sh[a][b] = s2;
-          sl[a][b] = __fadd_rn(__fadd_rn(lo, pe), err);
-        }
-    }
-    // fold the chunk into (H, L) every QG_FOLD rows (and at the end)
-    if (((l0 + QG_L) % QG_FOLD) == 0 || l0 + QG_L >= n) {
-#pragma unroll
-      for (int a = 0; a < QG_RI; a++)
-#pragma unroll
-        for (int b = 0; b < QG_RJ; b++) {
-          const float off = offset(a, b);
-          float hs, he, h2, e1;
-          two_sum(sh[a][b], -off, hs, he);
-          two_sum(H[a][b], hs, h2, e1);
-          H[a][b] = h2;
-          L[a][b] = __fadd_rn(L[a][b], __fadd_rn(__fadd_rn(e1, he), sl[a][b]));
-          sh[a][b] = off;
-          sl[a][b] = 0.0f;
-        }
-    }
-  }
-#pragma unroll
-  for (int a = 0; a < QG_RI; a++) {
-    const int i = i0 + ty + 16 * a;
-    if (i >= x) continue;
-#pragma unroll
-    for (int b = 0; b < QG_RJ; b++) {
-      const int j = j0 + tx + 16 * b;
-      if (j >= t) continue;
-      GR[i + (long long)j * ldg] = (double)H[a][b] + (double)L[a][b];
-    }
-  }
-}
-
 // unit weights (chol: |x~|^2)
 __global__ void unit_pairs_kernel(int n, float2* D, float* dmax) {
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) D[e] = make_float2(1.f, 0.f);
@@ -665,6 +539,8 @@ struct OzakiPlan {
   float2* D = nullptr;          // n x t weights as float pairs (eigen d_j; chol: ones)
   float* dmax = nullptr;        // t: max_l of the high part of D[:, j]
   float* amax = nullptr;        // Ncap: per-SNP max_l of the high part of R^2
+  float2* part = nullptr;       // quadratic Gram partial sums over row ranges
+  int sms = 0;                  // SM count of the device
   double* Linv = nullptr;       // chol: n x n, L^-1
   double* LinvT = nullptr;      // chol: n x n, (L^-1)^T (rows of L^-1 contiguous)
   int* err = nullptr;
@@ -702,6 +578,12 @@ cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_
   chk(cudaMalloc(&p->D, sizeof(float2) * (size_t)n * t));
   chk(cudaMalloc(&p->dmax, sizeof(float) * (size_t)t));
   chk(cudaMalloc(&p->amax, sizeof(float) * (size_t)p->Ncap));
+  chk(cudaMalloc(&p->part, sizeof(float2) * quad_gram_part_elems(p->Ncap, t)));
+  {
+    int dev = 0;
+    chk(cudaGetDevice(&dev));
+    chk(cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, dev));
+  }
   chk(cudaMalloc(&p->err, sizeof(int)));
   if (!eigen) chk(cudaMalloc(&p->Linv, sizeof(double) * (size_t)n * n));
   if (!eigen) chk(cudaMalloc(&p->LinvT, sizeof(double) * (size_t)n * n));
@@ -725,7 +607,7 @@ cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_
 
 void ozaki_destroy(OzakiPlan* p) {
   if (!p) return;
-  void* ptrs[] = {p->A, p->G, p->scale, p->C, p->U, p->D, p->dmax, p->amax, p->Linv, p->LinvT, p->err};
+  void* ptrs[] = {p->A, p->G, p->scale, p->C, p->U, p->D, p->dmax, p->amax, p->part, p->Linv, p->LinvT, p->err};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   delete p;
@@ -772,13 +654,8 @@ cudaError_t load_genotypes(OzakiPlan* p, cudaStream_t s, const T* X, int x) {
 }
 
 cudaError_t selfgram(OzakiPlan* p, cudaStream_t s, int col0, int xq, int t, double* GR, long long ldg) {
-  dim3 grid((xq + QG_I - 1) / QG_I, (t + QG_J - 1) / QG_J);
   const float2* A = (const float2*)(p->C + (long long)col0 * p->Mpad);
-  colmax_kernel<<<(xq + 7) / 8, 256, 0, s>>>(p->n, xq, A, p->Mpad, p->amax + col0);
-  selfgram_kernel<<<grid, 256, 0, s>>>(p->n, xq, t, A, p->Mpad, p->amax + col0, p->D, p->n, p->dmax, GR + col0, ldg);
-  note_launch();
-  note_launch();
-  return cudaGetLastError();
+  return quad_gram(s, p->n, xq, t, A, p->Mpad, p->amax + col0, p->D, p->n, p->dmax, p->part, GR + col0, ldg, p->sms);
 }
 
 }  // namespace

@@ -61,7 +61,8 @@ def test_split_gemm_fp64_accuracy():
     assert np.all(np.abs(C - ref) <= 2.0 ** -44 * bound + 1e-300)
 
 
-@pytest.mark.parametrize("n,m,t,xb", [(300, 700, 5, 256), (1000, 1100, 16, 512)])
+@pytest.mark.parametrize("n,m,t,xb", [(300, 700, 5, 256), (1000, 1100, 16, 512), (200, 300, 1, 256),
+                                      (260, 400, 40, 256), (300, 257, 100, 512), (150, 300, 130, 256)])
 def test_split_eigen_vs_oracle(n, m, t, xb):
     from fgls_gb300 import Engine, datagen
     pb = datagen.make_problem(n, m, t, seed=n + t, hsig_uniform=True)
