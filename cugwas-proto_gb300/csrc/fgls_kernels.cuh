@@ -53,6 +53,13 @@ size_t dc_workspace_bytes(int n);
 cudaError_t dc_tridiag_eig(cudaStream_t s, int n, double* d, double* e, double* W, double* V, void* work,
                            int* fail_dev, long long* launches);
 
+// Batched cohorts: solves of all problems with p predictors listed in plist
+// (device ints into probs), x_b SNPs per problem at most, one launch.
+struct SolveProblem;
+struct StepCohort;
+cudaError_t snp_solve_grouped(cudaStream_t s, int p, const SolveProblem* probs, const int* plist, int count, int x_b,
+                              const StepCohort* sc, DevStatus* st);
+
 // Two-sided normal p-values of the SNP coefficients from B and V (fgls_snp.cu).
 cudaError_t snp_pvalues(cudaStream_t s, int x, int t, int p, int wXL, const double* B, long long bstride,
                         const double* V, long long vstride, double* P, long long pstride);

@@ -39,11 +39,13 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <vector>
 
 #include "fgls_common.cuh"
 #include "fgls_kernels.cuh"
 #include "fgls_ozaki.cuh"
 #include "fgls_selfgram.cuh"
+#include "fgls_batch.cuh"
 
 namespace fgls {
 
@@ -186,6 +188,16 @@ struct GemmArgs {
   int* err;         // first failing wait site (0 = ok)
 };
 
+// Grouped launches: one problem per (cohort, trait), tiles listed by the host.
+struct GroupedProblem {
+  GemmArgs g;  // g.N is replaced by the cohort's columns of the launch
+  int cohort;
+  int pad;
+};
+struct GroupedTile {
+  int prob, m_tile, n_tile, pad;
+};
+
 // Exact int64 value V times a power-of-two scale, squared, as a float pair:
 // v = V*scale = vh + vl (|vl| <= 2^-24 |vh|), v^2 ~= ah + al with
 // ah = fl(vh^2), al = (vh^2 - ah) + 2 vh vl; relative error ~2^-47.  No FP64
@@ -200,9 +212,12 @@ __device__ __forceinline__ float2 square_pair(long long V, float fscale) {
   return make_float2(ah, al);
 }
 
-__global__ void __launch_bounds__(THREADS, 1)
-    ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                      const GemmArgs g) {
+// One 128 x 256 output tile (m_tile, n_tile) of problem g.  The tensor maps
+// are kernel parameters (single problem) or live in global memory (grouped
+// launch, written by the host before the launch: acquired through the
+// tensormap proxy before their first use).
+__device__ __forceinline__ void gemm_tile(const CUtensorMap* tmA, const CUtensorMap* tmB, const GemmArgs g,
+                                          const int m_tile, const int n_tile, const bool global_maps) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
@@ -214,14 +229,6 @@ __global__ void __launch_bounds__(THREADS, 1)
   volatile int* abort_flag = (volatile int*)(tbase_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // grouped rasterization: GROUP_M row tiles share the resident column tiles
-  const int tile = blockIdx.x;
-  const int per_group = GROUP_M * g.tiles_n;
-  const int group = tile / per_group;
-  const int first_m = group * GROUP_M;
-  const int gsz = min(g.tiles_m - first_m, GROUP_M);
-  const int m_tile = first_m + (tile % per_group) % gsz;
-  const int n_tile = (tile % per_group) / gsz;
   const int m0 = m_tile * BM, n0 = n_tile * BN;
   const int passes = (g.S + 1) / 2;
   int nk = g.Kpad / BK;
@@ -256,6 +263,10 @@ __global__ void __launch_bounds__(THREADS, 1)
       int issued[STAGES];
       uint32_t issued_phase[STAGES];
       for (int s = 0; s < STAGES; s++) issued[s] = 0;
+      if (global_maps) {
+        asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;" ::"l"((uint64_t)tmA) : "memory");
+        asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;" ::"l"((uint64_t)tmB) : "memory");
+      }
       bool ok = true;
       for (int p = 0; p < passes && ok; p++) {
         const int s0 = 2 * p, s1 = 2 * p + 1;
@@ -265,9 +276,9 @@ __global__ void __launch_bounds__(THREADS, 1)
           issued[stage] = 0;
           uint8_t* sb = smem + stage * STAGE_BYTES;
           mbar_expect_tx(&full[stage], (two ? 2 * A_TILE : A_TILE) + B_TILE);
-          tma_load_2d(sb, &tmA, kb * BK, s0 * g.Mpad + m0, &full[stage]);
-          if (two) tma_load_2d(sb + A_TILE, &tmA, kb * BK, s1 * g.Mpad + m0, &full[stage]);
-          tma_load_2d(sb + 2 * A_TILE, &tmB, kb * BK, g.col0 + n0, &full[stage]);
+          tma_load_2d(sb, tmA, kb * BK, s0 * g.Mpad + m0, &full[stage]);
+          if (two) tma_load_2d(sb + A_TILE, tmA, kb * BK, s1 * g.Mpad + m0, &full[stage]);
+          tma_load_2d(sb + 2 * A_TILE, tmB, kb * BK, g.col0 + n0, &full[stage]);
           issued[stage] = 1;
           issued_phase[stage] = phase;
           if (++stage == STAGES) { stage = 0; phase ^= 1; }
@@ -379,6 +390,33 @@ __global__ void __launch_bounds__(THREADS, 1)
   __syncthreads();
   tc_fence_after();
   if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(512) : "memory");
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+    ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                      const GemmArgs g) {
+  // grouped rasterization: GROUP_M row tiles share the resident column tiles
+  const int tile = blockIdx.x;
+  const int per_group = GROUP_M * g.tiles_n;
+  const int group = tile / per_group;
+  const int first_m = group * GROUP_M;
+  const int gsz = min(g.tiles_m - first_m, GROUP_M);
+  const int m_tile = first_m + (tile % per_group) % gsz;
+  const int n_tile = (tile % per_group) / gsz;
+  gemm_tile(&tmA, &tmB, g, m_tile, n_tile, false);
+}
+
+// Many independent problems in one launch: CTA b computes tiles[b] of
+// problem tiles[b].prob; its valid columns this launch are cols[cohort].
+// Tiles past a problem's valid columns exit before touching any resource.
+__global__ void __launch_bounds__(THREADS, 1)
+    ozaki_grouped_gemm_kernel(const GroupedTile* __restrict__ tiles, const GroupedProblem* __restrict__ probs,
+                              const CUtensorMap* __restrict__ maps, const int* __restrict__ cols) {
+  const GroupedTile tl = tiles[blockIdx.x];
+  GemmArgs g = probs[tl.prob].g;
+  g.N = cols[probs[tl.prob].cohort];
+  if (tl.n_tile * BN >= g.N) return;
+  gemm_tile(maps + 2 * tl.prob, maps + 2 * tl.prob + 1, g, tl.m_tile, tl.n_tile, true);
 }
 
 // ---------------------------------------------------------------------------
@@ -670,12 +708,25 @@ cudaError_t ozaki_set_eigen(OzakiPlan* p, cudaStream_t s, const double* Z, const
   return cudaGetLastError();
 }
 
+// L^-1 (lower, FP64) by blocked TRSM on the identity.  Column panel
+// [c0, c0 + w) of L^-1 is zero above row c0, so each panel solves only the
+// trailing system L[c0:, c0:] X = I[c0:, c0:c0+w]: n^3/3 flops instead of n^3.
+cudaError_t lower_inverse(cudaStream_t s, int n, const double* L, double* Linv) {
+  eye_kernel<<<grid_for((long long)n * n), 256, 0, s>>>(n, Linv);
+  note_launch();
+  constexpr int W = 512;
+  for (int c0 = 0; c0 < n; c0 += W) {
+    const int w = std::min(W, n - c0);
+    const long long off = (long long)c0 + (long long)c0 * n;
+    FGLS_CUDA_TRY(dtrsm_llnn(s, n - c0, w, L + off, n, Linv + off, n));
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t ozaki_set_chol(OzakiPlan* p, cudaStream_t s, const double* L, const double* WY) {
   const int n = p->n;
   // L^-1 by the FP64 blocked TRSM on the identity, then U = L^-T [y~ | XL~]
-  eye_kernel<<<grid_for((long long)n * n), 256, 0, s>>>(n, p->Linv);
-  note_launch();
-  FGLS_CUDA_TRY(dtrsm_llnn(s, n, n, L, n, p->Linv, n));
+  FGLS_CUDA_TRY(lower_inverse(s, n, L, p->Linv));
   FGLS_CUDA_TRY(dgemm(s, true, false, n, p->nU, n, 1.0, p->Linv, n, WY, n, 0.0, p->U, n));
   // rows of L^-1 contiguous: transpose, then slice
   dim3 tg((n + 31) / 32, (n + 31) / 32);
@@ -728,6 +779,161 @@ int ozaki_read_error(OzakiPlan* p) {
   int h = 0;
   cudaMemcpy(&h, p->err, sizeof(int), cudaMemcpyDeviceToHost);
   return h;
+}
+
+// ---------------------------------------------------------------------------
+// Batched cohorts: the split operand of one chol problem into caller buffers,
+// grouped genotype conversion and the grouped split GEMM.
+// ---------------------------------------------------------------------------
+int split_rows_padded(int rows) { return (rows + BM - 1) / BM * BM; }
+int split_k_padded(int n) { return (n + BK - 1) / BK * BK; }
+int split_cols_padded(int x) { return (x + BN - 1) / BN * BN; }
+
+cudaError_t split_chol_operand(cudaStream_t s, int n, int wXL, const double* L, const double* WY, int S, int Mpad,
+                               int Kpad, __nv_bfloat16* A, double* scale, double* Linv, double* LinvT, double* U) {
+  const int nU = 1 + wXL;
+  FGLS_CUDA_TRY(lower_inverse(s, n, L, Linv));
+  FGLS_CUDA_TRY(dgemm(s, true, false, n, nU, n, 1.0, Linv, n, WY, n, 0.0, U, n));
+  dim3 tg((n + 31) / 32, (n + 31) / 32);
+  transpose_kernel<<<tg, dim3(32, 8), 0, s>>>(n, Linv, LinvT);
+  note_launch();
+  slice_rows_kernel<<<n, 256, 0, s>>>(n, n, LinvT, n, 0, S, Mpad, Kpad, A, scale);
+  note_launch();
+  slice_rows_kernel<<<nU, 256, 0, s>>>(n, nU, U, n, n, S, Mpad, Kpad, A, scale);
+  note_launch();
+  return cudaGetLastError();
+}
+
+namespace {
+// per-row scale of an S-slice operand from that of the same digits cut at
+// S_built slices: 2^(e - 15 - 16 (passes - 1)) depends on the pass count only
+__global__ void rescale_rows_kernel(int rows, const double* __restrict__ built, int dpass, double* __restrict__ out) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < rows) out[r] = ldexp(built[r], 16 * dpass);
+}
+
+template <typename T>
+__global__ void grouped_genotypes_kernel(const GenoCohort* __restrict__ gc, const StepCohort* __restrict__ sc) {
+  const int c = blockIdx.y;
+  const int x = sc[c].x, n = gc[c].n, Kpad = gc[c].Kpad;
+  const T* __restrict__ src = (const T*)sc[c].X;
+  __nv_bfloat16* __restrict__ G = gc[c].G;
+  const long long total = (long long)x * n;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(e % n);
+    const long long col = e / n;
+    G[col * Kpad + k] = __float2bfloat16((float)src[col * n + k]);
+  }
+}
+}  // namespace
+
+cudaError_t split_rescale_rows(cudaStream_t s, int rows, const double* built_scale, int S_built, int S,
+                               double* scale) {
+  const int dpass = (S_built + 1) / 2 - (S + 1) / 2;
+  rescale_rows_kernel<<<(rows + 255) / 256, 256, 0, s>>>(rows, built_scale, dpass, scale);
+  note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t grouped_genotypes(cudaStream_t s, const GenoCohort* dgc, const StepCohort* dsc, int cohorts, bool u8) {
+  dim3 grid(96, cohorts);
+  if (u8)
+    grouped_genotypes_kernel<unsigned char><<<grid, 256, 0, s>>>(dgc, dsc);
+  else
+    grouped_genotypes_kernel<double><<<grid, 256, 0, s>>>(dgc, dsc);
+  note_launch();
+  return cudaGetLastError();
+}
+
+struct GroupedGemm {
+  int ntiles = 0, nprob = 0;
+  GroupedTile* tiles = nullptr;
+  GroupedProblem* probs = nullptr;
+  CUtensorMap* maps = nullptr;
+};
+
+cudaError_t grouped_gemm_create(GroupedGemm** out, const GroupedGemmDesc* d, int count, int x_b, int* err) {
+  *out = nullptr;
+  std::vector<GroupedProblem> probs(count);
+  std::vector<CUtensorMap> maps(2 * (size_t)count);
+  std::vector<int> order(count);
+  std::vector<long long> work(count);
+  for (int i = 0; i < count; i++) {
+    GemmArgs& g = probs[i].g;
+    g.M = d[i].M;
+    g.Mpad = d[i].Mpad;
+    g.N = x_b;
+    g.Kpad = d[i].Kpad;
+    g.S = d[i].S;
+    g.tiles_m = d[i].Mpad / BM;
+    g.tiles_n = (x_b + BN - 1) / BN;
+    g.tri_rows = d[i].tri_rows;
+    g.row_scale = d[i].scale;
+    g.C = d[i].C;
+    g.ldc = d[i].Mpad;
+    g.col0 = 0;
+    g.sq_rows = d[i].sq_rows;
+    g.err = err;
+    probs[i].cohort = d[i].cohort;
+    probs[i].pad = 0;
+    FGLS_CUDA_TRY(make_map(&maps[2 * i], d[i].A, d[i].Kpad, (long long)d[i].S_alloc * d[i].Mpad, BM));
+    FGLS_CUDA_TRY(make_map(&maps[2 * i + 1], d[i].G, d[i].Kpad, d[i].Ncap, BN));
+    order[i] = i;
+    work[i] = (long long)g.tiles_m * g.Kpad;
+  }
+  // longest problems first, so that the short ones fill the last waves
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return work[a] > work[b]; });
+  std::vector<GroupedTile> tiles;
+  for (int i : order) {
+    const GemmArgs& g = probs[i].g;
+    for (int first = 0; first < g.tiles_m; first += GROUP_M) {
+      const int gsz = std::min(GROUP_M, g.tiles_m - first);
+      for (int nt = 0; nt < g.tiles_n; nt++)
+        for (int m = 0; m < gsz; m++) tiles.push_back(GroupedTile{i, first + m, nt, 0});
+    }
+  }
+  GroupedGemm* gg = new GroupedGemm();
+  gg->ntiles = (int)tiles.size();
+  gg->nprob = count;
+  cudaError_t r = cudaSuccess;
+  auto chk = [&](cudaError_t e) {
+    if (r == cudaSuccess) r = e;
+  };
+  chk(cudaMalloc(&gg->tiles, sizeof(GroupedTile) * tiles.size()));
+  chk(cudaMalloc(&gg->probs, sizeof(GroupedProblem) * probs.size()));
+  chk(cudaMalloc(&gg->maps, sizeof(CUtensorMap) * maps.size()));  // 256-byte aligned: >= the 64 a map needs
+  if (r == cudaSuccess)
+    chk(cudaMemcpy(gg->tiles, tiles.data(), sizeof(GroupedTile) * tiles.size(), cudaMemcpyHostToDevice));
+  if (r == cudaSuccess)
+    chk(cudaMemcpy(gg->probs, probs.data(), sizeof(GroupedProblem) * probs.size(), cudaMemcpyHostToDevice));
+  if (r == cudaSuccess)
+    chk(cudaMemcpy(gg->maps, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice));
+  if (r == cudaSuccess)
+    chk(cudaFuncSetAttribute(ozaki_grouped_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+  if (r != cudaSuccess) {
+    grouped_gemm_destroy(gg);
+    return r;
+  }
+  *out = gg;
+  return cudaSuccess;
+}
+
+cudaError_t grouped_gemm_run(GroupedGemm* gg, cudaStream_t s, const int* dcols) {
+  if (gg->ntiles == 0) return cudaSuccess;
+  ozaki_grouped_gemm_kernel<<<gg->ntiles, THREADS, SMEM_BYTES, s>>>(gg->tiles, gg->probs, gg->maps, dcols);
+  note_launch();
+  return cudaGetLastError();
+}
+
+int grouped_gemm_tiles(const GroupedGemm* gg) { return gg ? gg->ntiles : 0; }
+
+void grouped_gemm_destroy(GroupedGemm* gg) {
+  if (!gg) return;
+  if (gg->tiles) cudaFree(gg->tiles);
+  if (gg->probs) cudaFree(gg->probs);
+  if (gg->maps) cudaFree(gg->maps);
+  delete gg;
 }
 
 }  // namespace fgls

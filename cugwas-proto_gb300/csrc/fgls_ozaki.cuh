@@ -6,6 +6,7 @@
 // epilogue recombines the slices in FP64.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 namespace fgls {
@@ -33,5 +34,40 @@ double ozaki_flops_per_snp(const OzakiPlan* p);
 // x~^T y~_j, x~^T XL~_j; element (SNP i, q) at ptr[q + i * ld].
 const double* ozaki_gram_rows(const OzakiPlan* p, long long* ld);
 int ozaki_read_error(OzakiPlan* p);
+
+// ---- batched cohorts (fgls_batch.cu) -------------------------------------
+struct StepCohort;
+struct GenoCohort;
+// padded sizes of a split operand with `rows` rows, K = n, x columns
+int split_rows_padded(int rows);
+int split_k_padded(int n);
+int split_cols_padded(int x);
+// [L^-1 ; (L^-T WY)^T] of one chol problem cut into S BF16 slices at A
+// (S x Mpad x Kpad) with row scales; Linv, LinvT (n x n) and U (n x (1+wXL))
+// are caller scratch.
+cudaError_t split_chol_operand(cudaStream_t s, int n, int wXL, const double* L, const double* WY, int S, int Mpad,
+                               int Kpad, __nv_bfloat16* A, double* scale, double* Linv, double* LinvT, double* U);
+// row scales of the first S slices of an operand cut into S_built slices
+cudaError_t split_rescale_rows(cudaStream_t s, int rows, const double* built_scale, int S_built, int S,
+                               double* scale);
+// genotype blocks of all cohorts (per-step table) -> their BF16 operands
+cudaError_t grouped_genotypes(cudaStream_t s, const GenoCohort* dgc, const StepCohort* dsc, int cohorts, bool u8);
+
+struct GroupedGemmDesc {
+  const __nv_bfloat16* A;  // slices, S_alloc x Mpad x Kpad
+  int S, S_alloc, M, Mpad, Kpad, tri_rows, sq_rows;
+  const double* scale;     // Mpad row scales for S slices
+  const __nv_bfloat16* G;  // cohort genotype operand, Ncap x Kpad
+  int Ncap;
+  double* C;               // Mpad x x_b output (ld Mpad)
+  int cohort;
+};
+struct GroupedGemm;
+// One launch over all problems' tiles (x_b columns each at most); the
+// columns of a launch come from dcols[cohort] (device ints).
+cudaError_t grouped_gemm_create(GroupedGemm** out, const GroupedGemmDesc* d, int count, int x_b, int* err);
+cudaError_t grouped_gemm_run(GroupedGemm* gg, cudaStream_t s, const int* dcols);
+int grouped_gemm_tiles(const GroupedGemm* gg);
+void grouped_gemm_destroy(GroupedGemm* gg);
 
 }  // namespace fgls

@@ -19,6 +19,7 @@
 
 #include "fgls_common.cuh"
 #include "fgls_kernels.cuh"
+#include "fgls_batch.cuh"
 
 namespace fgls {
 
@@ -260,15 +261,16 @@ __global__ void quad_products_kernel(int n, int x, int wXR, const double* __rest
 // ---------------------------------------------------------------------------
 // Batched p x p solve: one thread per (SNP, trait) test.
 // ---------------------------------------------------------------------------
+// 128 tests (SNPs i0 .. i0+127 of trait j) per CTA of 128 threads; `tag` is
+// added to the pivot index of a non-SPD report.
 template <int P>
-__global__ void __launch_bounds__(128) snp_solve_kernel(
-    int x, int t, int wXL, const double* __restrict__ top, const double* __restrict__ GYL, long long rsg,
-    long long ldg, const double* __restrict__ GR, long long ldr, double* __restrict__ Bout, long long bstride,
-    double* __restrict__ Vout, long long vstride, DevStatus* st, long long snp_base) {
+__device__ __forceinline__ void solve_block(int x, int t, int wXL, const int j, const int i0,
+                                            const double* __restrict__ top, const double* __restrict__ GYL,
+                                            long long rsg, long long ldg, const double* __restrict__ GR, long long ldr,
+                                            double* __restrict__ Bout, long long bstride, double* __restrict__ Vout,
+                                            long long vstride, DevStatus* st, long long snp_base, int tag) {
   extern __shared__ double stage[];  // [128][P + P*P]
   const int wXR = P - wXL;
-  const int j = blockIdx.y;
-  const int i0 = blockIdx.x * 128;
   const int i = i0 + threadIdx.x;
   const int tw = wXL + wXL * wXL + 1;
   const double* T = top + (long long)j * tw;
@@ -309,7 +311,7 @@ __global__ void __launch_bounds__(128) snp_solve_kernel(
         L[r][c] = v / lcc;
       }
     }
-    if (info) set_status(st, FGLSGPU_ENOTSPD, info, snp_base + i);
+    if (info) set_status(st, FGLSGPU_ENOTSPD, tag + info, snp_base + i);
     // two triangular solves: L z = b, L^T beta = z
     double z[P];
 #pragma unroll
@@ -365,6 +367,30 @@ __global__ void __launch_bounds__(128) snp_solve_kernel(
   for (int e = threadIdx.x; e < nv * P; e += 128) Bj[e] = stage[(e / P) * (P + P * P) + (e % P)];
   for (int e = threadIdx.x; e < nv * P * P; e += 128)
     Vj[e] = stage[(e / (P * P)) * (P + P * P) + P + (e % (P * P))];
+}
+
+template <int P>
+__global__ void __launch_bounds__(128) snp_solve_kernel(
+    int x, int t, int wXL, const double* __restrict__ top, const double* __restrict__ GYL, long long rsg,
+    long long ldg, const double* __restrict__ GR, long long ldr, double* __restrict__ Bout, long long bstride,
+    double* __restrict__ Vout, long long vstride, DevStatus* st, long long snp_base) {
+  solve_block<P>(x, t, wXL, blockIdx.y, blockIdx.x * 128, top, GYL, rsg, ldg, GR, ldr, Bout, bstride, Vout, vstride,
+                 st, snp_base, 0);
+}
+
+// Batched cohorts: CTA b solves SNPs [128 (b % bpp), +128) of problem
+// plist[b / bpp] (one trait of one cohort, wXR = 1); results go to the
+// cohort's step outputs.  A non-SPD report carries (cohort + 1) << 8 + pivot.
+template <int P>
+__global__ void __launch_bounds__(128) snp_solve_grouped_kernel(const SolveProblem* __restrict__ probs,
+                                                                const int* __restrict__ plist, int bpp,
+                                                                const StepCohort* __restrict__ sc, DevStatus* st) {
+  const SolveProblem pr = probs[plist[blockIdx.x / bpp]];
+  const StepCohort c = sc[pr.cohort];
+  const int i0 = (blockIdx.x % bpp) * 128;
+  if (i0 >= c.x) return;
+  solve_block<P>(c.x, 1, P - 1, 0, i0, pr.top, pr.gyl, pr.rsg, 1, pr.GR, 0, c.B + (long long)pr.trait * c.x * P, 0,
+                 c.V + (long long)pr.trait * c.x * P * P, 0, st, c.snp_base, (pr.cohort + 1) << 8);
 }
 
 template <int P>
@@ -431,6 +457,38 @@ cudaError_t quad_products(cudaStream_t s, int n, int x, int wXR, const double* R
   quad_products_kernel<<<blocks, 256, 0, s>>>(n, x, wXR, R, ldr, Q, ldq);
   note_launch();
   return cudaGetLastError();
+}
+
+template <int P>
+cudaError_t launch_solve_grouped(cudaStream_t s, const SolveProblem* probs, const int* plist, int count, int x_b,
+                                 const StepCohort* sc, DevStatus* st) {
+  const size_t smem = sizeof(double) * 128 * (P + P * P);
+  FGLS_CUDA_TRY(
+      cudaFuncSetAttribute(snp_solve_grouped_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int bpp = ceil_div(x_b, 128);
+  snp_solve_grouped_kernel<P><<<count * bpp, 128, smem, s>>>(probs, plist, bpp, sc, st);
+  note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t snp_solve_grouped(cudaStream_t s, int p, const SolveProblem* probs, const int* plist, int count, int x_b,
+                              const StepCohort* sc, DevStatus* st) {
+  if (count <= 0) return cudaSuccess;
+  switch (p) {
+#define FGLS_P_CASE(P) \
+  case P:              \
+    return launch_solve_grouped<P>(s, probs, plist, count, x_b, sc, st);
+    FGLS_P_CASE(2)
+    FGLS_P_CASE(3)
+    FGLS_P_CASE(4)
+    FGLS_P_CASE(5)
+    FGLS_P_CASE(6)
+    FGLS_P_CASE(7)
+    FGLS_P_CASE(8)
+#undef FGLS_P_CASE
+    default:
+      return cudaErrorInvalidValue;
+  }
 }
 
 cudaError_t snp_solve(cudaStream_t s, int p, int x, int t, int wXL, const double* top, const double* GYL,
