@@ -227,6 +227,167 @@ def orthogonal_basis(n, seed):
     return Z
 
 
+COHORT_BUCKETS = ((500, 1000), (1000, 2000), (2000, 4000), (4000, 8001))
+
+
+def make_cohorts(count, m, t, seed, dev):
+    """Uneven cohorts: n log-uniform in [500, 8000], p uniform in 3..8
+    (intercept + p-2 N(0,1) covariates + 1 SNP), t traits with h ~ U(0.1, 0.9),
+    sigma ~ U(0.5, 2); kinship G G^T / 5000 + 1e-3 I from standardised
+    genotypes G (n x 5000, FP32 product, symmetrised in FP64); seeds derived
+    from one master seed."""
+    import torch
+    rng = np.random.default_rng(seed)
+    out = []
+    for c in range(count):
+        n = int(round(np.exp(rng.uniform(np.log(500), np.log(8000)))))
+        p = int(rng.integers(3, 9))
+        g = torch.Generator(device=dev).manual_seed(int(rng.integers(1 << 31)))
+        k = 5000
+        f = torch.rand(k, generator=g, device=dev) * 0.45 + 0.05
+        G = (torch.rand(n, k, generator=g, device=dev) < f).float() + (torch.rand(n, k, generator=g, device=dev) < f).float()
+        G = (G - G.mean(0)) / G.std(0, unbiased=False).clamp_min(1e-6)
+        P = (G @ G.T / k).double()
+        Phi = 0.5 * (P + P.T)
+        Phi.diagonal().add_(1e-3)
+        h = torch.rand(t, generator=g, device=dev, dtype=torch.float64) * 0.8 + 0.1
+        sg = torch.rand(t, generator=g, device=dev, dtype=torch.float64) * 1.5 + 0.5
+        XL = torch.ones(n, p - 1, device=dev, dtype=torch.float64)
+        XL[:, 1:] = torch.randn(n, p - 2, generator=g, device=dev, dtype=torch.float64)
+        u = torch.randn(k, t, generator=g, device=dev, dtype=torch.float64)
+        v = torch.randn(n, t, generator=g, device=dev, dtype=torch.float64)
+        Y = (G.double() @ u) / k ** 0.5 * torch.sqrt(h * sg) + v * torch.sqrt(h * sg * 1e-3 + (1 - h) * sg)
+        out.append({"Phi": Phi.cpu().numpy(), "XL": XL.cpu().numpy(), "Y": Y.cpu().numpy(),
+                    "h": h.cpu().numpy(), "sigma": sg.cpu().numpy(), "n": n, "p": p, "t": t, "m": m,
+                    "seed": int(rng.integers(1 << 31))})
+        del G, P, Phi
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_cohorts(args):
+    """Batched uneven cohorts: 64 problems, m = 200000 SNPs and t = 4 traits
+    each, split precision, one grouped launch per stage, CUDA-graph steps,
+    x_b and slices from the autotuner unless given."""
+    import torch
+    from fgls_gb300 import Batch, launch_count
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    C, M, T = args.cohorts, 200_000, 4
+    t0 = time.perf_counter()
+    co = make_cohorts(C, M, T, 7, dev)
+    gen_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    b = Batch(co, x_b=args.xb if args.xb_set else 0, slices=args.slices if args.slices_set else 0,
+              use_graph=True, genotypes_u8=True, tol=1e-10)
+    setup_s = time.perf_counter() - t0
+    xb, S, perr = b.params()
+    log(f"[bench] cohorts: data {gen_s:.1f}s, setup {setup_s:.1f}s, x_b={xb}, slices={S}, probe err {perr:.2e}")
+    pool = 2
+    X = [[genotype_block(xb, c["n"], c["seed"] + i, dev).to(torch.uint8) for i in range(pool)] for c in co]
+    dB = [torch.empty(T * xb * c["p"], dtype=torch.float64, device=dev) for c in co]
+    dV = [torch.empty(T * xb * c["p"] ** 2, dtype=torch.float64, device=dev) for c in co]
+    stream = torch.cuda.ExternalStream(b.stream(), device=dev)
+    bp, vp = [d.data_ptr() for d in dB], [d.data_ptr() for d in dV]
+
+    def step(k, active=None):
+        xs = [xb if active is None or active(c) else 0 for c in co]
+        b.step([X[i][k % pool].data_ptr() for i in range(C)], xs, bp, vp)
+        return sum(x * c["t"] for x, c in zip(xs, co))
+
+    for k in range(args.warmup):
+        step(k)
+    b.sync()
+    uuid = "GPU-" + str(torch.cuda.get_device_properties(0).uuid)
+    sampler = ClockSampler(uuid)
+    l0 = launch_count()
+    sampler.start()
+    time.sleep(0.3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    tests = 0
+    for k in range(args.steps):
+        tests += step(args.warmup + k)
+    e1.record(stream)
+    e1.synchronize()
+    clocks = sampler.stop()
+    launches = launch_count() - l0
+    b.sync()
+    ms = e0.elapsed_time(e1)
+    value = tests / (ms / 1e3)
+    # per size bucket: the other cohorts idle (x = 0) within the same batch
+    buckets = {}
+    for lo, hi in COHORT_BUCKETS:
+        act = (lambda c, lo=lo, hi=hi: lo <= c["n"] < hi)
+        if not any(act(c) for c in co):
+            continue
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        tb = sum(step(k, act) for k in range(2))
+        f1.record(stream)
+        f1.synchronize()
+        buckets[f"n_{lo}_{hi - 1 if hi == 8001 else hi}"] = {
+            "cohorts": sum(1 for c in co if act(c)), "tests_per_s": tb / (f0.elapsed_time(f1) / 1e3)}
+    b.sync()
+    # stage times (profiled steps run without the graph)
+    b.profile(True)
+    for k in range(2):
+        step(k)
+    b.sync()
+    prof, nprof = b.profile_read()
+    b.profile(False)
+    # tensor-core work of the grouped split GEMM per step: 2 S (nU n + n^2/2) per SNP and trait
+    flops = sum(2.0 * S * ((c["p"]) * c["n"] + 0.5 * c["n"] ** 2) * xb * c["t"] for c in co)
+    gemm_ms = prof["split_gemm"] / max(nprof, 1)
+    pk, pk_kind = peaks()
+    peak = float(pk.get("bf16_tflops_sustained", FALLBACK_PEAKS["bf16_tflops_sustained"]))
+    # end to end: host pinned genotypes -> device, step, results -> host
+    Xh = [X[i][0].cpu().pin_memory() for i in range(C)]
+    Bh = [torch.empty_like(d, device="cpu").pin_memory() for d in dB]
+    Vh = [torch.empty_like(d, device="cpu").pin_memory() for d in dV]
+    Xd = [X[i][1] for i in range(C)]
+    E = 3
+    torch.cuda.synchronize()
+    a = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for k in range(E):
+            for i in range(C):
+                Xd[i].copy_(Xh[i], non_blocking=True)
+            b.step([Xd[i].data_ptr() for i in range(C)], [xb] * C, bp, vp)
+            for i in range(C):
+                Bh[i].copy_(dB[i], non_blocking=True)
+                Vh[i].copy_(dV[i], non_blocking=True)
+    stream.synchronize()
+    e2e_s = time.perf_counter() - a
+    b.sync()
+    e2e_tests = E * sum(xb * c["t"] for c in co)
+    b.close()
+    line = {
+        "metric": "SNP×trait tests/s, batched uneven cohorts (64 problems), split precision",
+        "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16", "data": "synthetic",
+        "config": {"workload": f"{C} cohorts, n log-uniform [500, 8000], p in 3..8, t={T}, m={M} each; "
+                               f"steps of x_b={xb} SNPs of every cohort",
+                   "cohorts": C, "n": [c["n"] for c in co], "p": [c["p"] for c in co], "t": T, "m": M,
+                   "x_b": xb, "slices": S, "probe_beta_err": perr, "setup_s": setup_s,
+                   "job_s_estimate": C * M * T / value + setup_s, "buckets": buckets,
+                   "stage_ms_per_step": {k: v / max(nprof, 1) for k, v in prof.items()},
+                   "l2": f"inputs larger than L2: {pool} blocks per cohort, "
+                         f"{pool * xb * sum(c['n'] for c in co) / 1e9:.2f} GB of genotypes cycled"},
+        "roofline": {"bound": "tensor", "achieved": flops / (gemm_ms / 1e3) / 1e12, "peak": peak,
+                     "unit": "TFLOP/s", "frac": flops / (gemm_ms / 1e3) / 1e12 / peak, "traffic": None,
+                     "kernel": "ozaki_grouped_gemm_kernel", "peak_source": f"{pk_kind} bf16_tflops_sustained"},
+        "e2e": {"value": e2e_tests / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": xb * sum(c["n"] for c in co),
+                "d2h_bytes_per_step": sum(T * xb * (c["p"] + c["p"] ** 2) * 8 for c in co),
+                "api": "fglsgpu_batch_step (host pinned u8 genotypes -> host B/V)", "steps": E},
+        "gpu_launches": launches, "clocks": clocks, "cpu_baseline": None,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, rank, world):
     """The reference's CPU algorithm (oracle restatement of fgls_eigen's
     per-block loop, src/fgls_eigen.c:471-565) on the host cores."""
@@ -276,6 +437,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-snps", type=int, default=128)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="eigen", choices=["eigen", "cohorts"])
+    ap.add_argument("--cohorts", type=int, default=64)
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -283,6 +446,10 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.workload == "cohorts":
+        args.xb_set = any(a.startswith("--xb") for a in sys.argv[1:])
+        args.slices_set = any(a.startswith("--slices") for a in sys.argv[1:])
+        return run_cohorts(args)
 
     import torch
     dist = None

@@ -1,0 +1,40 @@
+// Shared device-side tables of the batched-cohort path (fgls_batch.cu).
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+namespace fgls {
+
+// Per cohort, rewritten before every step (one host->device copy).
+struct StepCohort {
+  const void* X;       // genotype block, SNP-major (SNP i at X + i*n), u8 or FP64
+  double* B;           // results: trait j of SNP i at B + (j*x + i)*p
+  double* V;           //          and V + (j*x + i)*p*p
+  long long snp_base;  // index of the block's first SNP (error reports)
+  int x;               // SNPs of this step (0: cohort idle)
+  int pad;
+};
+
+// Per cohort, fixed: BF16 genotype operand of the split GEMM.
+struct GenoCohort {
+  __nv_bfloat16* G;  // Ncap x Kpad, column c at G + c*Kpad
+  int n, Kpad;
+};
+
+// Per (cohort, trait) problem, fixed.
+struct UnitGramProblem {
+  const float2* A;  // R^2 pairs, column i at A + i*lda, rows [0, n)
+  long long lda;
+  double* GR;       // x_b results
+  int n, cohort;
+};
+
+struct SolveProblem {
+  const double* top;  // null model of the trait: b_T, S_TL, res_sigma
+  const double* gyl;  // Gram rows of the split GEMM: SNP i at gyl + i*rsg, [x~'y~, x~'XL~]
+  long long rsg;
+  const double* GR;   // x~'x~ of SNP i at GR[i]
+  int cohort, trait;
+};
+
+}  // namespace fgls

@@ -39,6 +39,9 @@ EXPORTS = (
     "fglsgpu_last_error", "fglsgpu_version", "fglsgpu_selftest_split_gemm", "fglsgpu_set_precision",
     "fglsgpu_profile", "fglsgpu_profile_read", "fglsgpu_split_gemm_noalloc", "fglsgpu_adjoint_reset",
     "fglsgpu_adjoint_block_device", "fglsgpu_adjoint_read", "fglsgpu_reml", "fglsgpu_pvalues_device",
+    "fglsgpu_batch_create", "fglsgpu_batch_destroy", "fglsgpu_batch_params", "fglsgpu_batch_step",
+    "fglsgpu_batch_sync", "fglsgpu_batch_stream", "fglsgpu_batch_last_error", "fglsgpu_batch_profile",
+    "fglsgpu_batch_profile_read",
 )
 PROF_CLASSES = ("genotypes", "split_gemm", "selfgram", "solve", "fp64_gemm", "trsm", "gram", "spare")
 
@@ -52,6 +55,16 @@ class FGLSError(RuntimeError):
 class Config(C.Structure):
     _fields_ = [(f, C.c_int) for f in
                 ("n", "wXL", "wXR", "t", "x_b", "variant", "precision", "slices", "device", "reserved")]
+
+
+class CohortDesc(C.Structure):
+    _fields_ = [("n", C.c_int), ("wXL", C.c_int), ("t", C.c_int)] + \
+               [(f, C.c_void_p) for f in ("Phi", "XL", "Y", "h", "sigma")]
+
+
+class BatchConfig(C.Structure):
+    _fields_ = [(f, C.c_int) for f in ("x_b", "slices", "device", "use_graph", "genotypes_u8", "reserved")] + \
+               [("tol", C.c_double)]
 
 
 _lib = None
@@ -94,6 +107,17 @@ def lib():
     L.fglsgpu_adjoint_read.argtypes = [P, P, P, P]
     L.fglsgpu_reml.argtypes = [P, P, P]
     L.fglsgpu_pvalues_device.argtypes = [P, P, P, I, LL, LL, P, LL]
+    L.fglsgpu_batch_create.argtypes = [C.POINTER(CohortDesc), I, C.POINTER(BatchConfig), C.POINTER(P)]
+    L.fglsgpu_batch_destroy.argtypes = [P]
+    L.fglsgpu_batch_params.argtypes = [P, C.POINTER(I), C.POINTER(I), C.POINTER(C.c_double)]
+    L.fglsgpu_batch_step.argtypes = [P, P, P, P, P, P]
+    L.fglsgpu_batch_sync.argtypes = [P]
+    L.fglsgpu_batch_stream.argtypes = [P]
+    L.fglsgpu_batch_stream.restype = P
+    L.fglsgpu_batch_last_error.argtypes = [P]
+    L.fglsgpu_batch_last_error.restype = C.c_char_p
+    L.fglsgpu_batch_profile.argtypes = [P, I]
+    L.fglsgpu_batch_profile_read.argtypes = [P, P, C.POINTER(LL)]
     _lib = L
     return L
 
@@ -226,6 +250,89 @@ class Engine:
     def close(self):
         if self._h is not None:
             self.L.fglsgpu_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+class Batch:
+    """Batched uneven cohorts (fglsgpu_batch_*), chol variant, wXR = 1.
+
+    ``cohorts``: list of dicts with Phi (n x n), XL (n x wXL), Y (n x t), h, sigma
+    (numpy, natural orientation).  ``step`` takes per-cohort device pointers."""
+
+    def __init__(self, cohorts, x_b=0, slices=0, device=0, use_graph=True, genotypes_u8=True, tol=0.0):
+        self.L = lib()
+        self._keep = []
+        descs = (CohortDesc * len(cohorts))()
+        self.dims = []
+        for k, c in enumerate(cohorts):
+            Phi, XL = _f64(c["Phi"]), _f64(c["XL"])
+            Y = _f64(c["Y"])
+            h = np.ascontiguousarray(c["h"], dtype=np.float64)
+            s = np.ascontiguousarray(c["sigma"], dtype=np.float64)
+            self._keep += [Phi, XL, Y, h, s]
+            n, wXL = XL.shape
+            t = Y.shape[1]
+            descs[k] = CohortDesc(n, wXL, t, Phi.ctypes.data, XL.ctypes.data, Y.ctypes.data, h.ctypes.data,
+                                  s.ctypes.data)
+            self.dims.append((n, wXL + 1, t))
+        self.cfg = BatchConfig(int(x_b), int(slices), int(device), int(bool(use_graph)), int(bool(genotypes_u8)),
+                               0, float(tol))
+        h = C.c_void_p()
+        rc = self.L.fglsgpu_batch_create(descs, len(cohorts), C.byref(self.cfg), C.byref(h))
+        self._keep = None
+        if rc:
+            raise FGLSError(rc, self.L.fglsgpu_batch_last_error(None).decode())
+        self._h = h
+
+    def _check(self, rc):
+        if rc:
+            raise FGLSError(rc, self.L.fglsgpu_batch_last_error(self._h).decode())
+
+    def params(self):
+        xb, S, e = C.c_int(), C.c_int(), C.c_double()
+        self._check(self.L.fglsgpu_batch_params(self._h, C.byref(xb), C.byref(S), C.byref(e)))
+        return xb.value, S.value, e.value
+
+    def step(self, x_ptrs, xs, b_ptrs, v_ptrs, snp_base=None):
+        k = len(self.dims)
+        X = (C.c_void_p * k)(*x_ptrs)
+        xs = (C.c_int * k)(*xs)
+        B = (C.c_void_p * k)(*b_ptrs)
+        V = (C.c_void_p * k)(*v_ptrs)
+        base = None if snp_base is None else (C.c_longlong * k)(*snp_base)
+        self._check(self.L.fglsgpu_batch_step(self._h, X, xs, B, V, base))
+
+    def sync(self):
+        self._check(self.L.fglsgpu_batch_sync(self._h))
+
+    def stream(self):
+        return self.L.fglsgpu_batch_stream(self._h)
+
+    def profile(self, enable=True):
+        self._check(self.L.fglsgpu_batch_profile(self._h, int(bool(enable))))
+
+    def profile_read(self):
+        """{stage: summed ms} over the profiled steps, and the step count."""
+        ms = np.zeros(4)
+        n = C.c_longlong()
+        self._check(self.L.fglsgpu_batch_profile_read(self._h, _ptr(ms), C.byref(n)))
+        return dict(zip(("genotypes", "split_gemm", "selfgram", "solve"), ms.tolist())), n.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.L.fglsgpu_batch_destroy(self._h)
             self._h = None
 
     def __del__(self):

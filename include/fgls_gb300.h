@@ -227,6 +227,62 @@ int fglsgpu_selftest_split_gemm(int M, int K, int N, int slices, const double *A
 int fglsgpu_split_gemm_noalloc(int M, int K, int N, int slices, const double *A, const double *X,
                                double *C, void *stream);
 
+/* ---------------------------------------------------- batched cohorts ----
+ * Many independent chol-variant problems of uneven size (cohort c: n_c
+ * individuals, wXL_c covariates, t_c traits, wXR = 1) advanced together, one
+ * SNP block of every cohort per step: all cohorts' split GEMM tiles in one
+ * launch, the quadratic Gram terms and the p x p solves grouped likewise, the
+ * step replayed from a captured CUDA graph.  Per (cohort, trait) the FP64
+ * Cholesky of M_j, the null model and L_j^-1 are computed once at creation
+ * and the split operand stays resident in HBM.  The reference handles one
+ * problem per process (fgls_chol, src/fgls_chol.c:29); it has no batched
+ * counterpart.  Autotuning: x_b = 0 picks the SNP block (1024..8192) by
+ * measured tests/s, slices = 0 the smallest slice count whose probe-block
+ * beta is within tol/8 of the FP64 path for every problem. */
+typedef struct fglsgpu_batch fglsgpu_batch;
+
+typedef struct {
+  int n, wXL, t;       /* individuals, covariate columns, traits           */
+  const double *Phi;   /* host, n x n column-major (Phi.in layout)         */
+  const double *XL;    /* host, n x wXL column-major                       */
+  const double *Y;     /* host, t traits of n values (Y.in layout)         */
+  const double *h;     /* host, t heritabilities                           */
+  const double *sigma; /* host, t variance scales                          */
+} fglsgpu_cohort;
+
+typedef struct {
+  int x_b;          /* SNPs per cohort per step (0: autotune)             */
+  int slices;       /* BF16 slices 3..6 (0: autotune)                     */
+  int device;       /* CUDA device ordinal                                */
+  int use_graph;    /* 1: replay each step from a captured CUDA graph     */
+  int genotypes_u8; /* 1: genotype blocks are bytes, 0: FP64              */
+  int reserved;
+  double tol;       /* autotune target for beta vs FP64 (0: 1e-10)        */
+} fglsgpu_batch_config;
+
+int fglsgpu_batch_create(const fglsgpu_cohort *cohorts, int count, const fglsgpu_batch_config *cfg,
+                         fglsgpu_batch **out);
+int fglsgpu_batch_destroy(fglsgpu_batch *b);
+/* The tuned (or given) SNP block and slice count, and the probe error of
+ * the slice choice (-1 when slices were given). */
+int fglsgpu_batch_params(const fglsgpu_batch *b, int *x_b, int *slices, double *probe_err);
+/* One step (asynchronous; fglsgpu_batch_sync reports device failures).  Per
+ * cohort c: dX[c] = device genotype block of x[c] <= x_b SNPs (SNP i at
+ * dX[c] + i*n_c, bytes or doubles per the config; x[c] = 0 skips the
+ * cohort), results to device dB[c] (trait j of SNP i at (j*x[c] + i)*p_c)
+ * and dV[c] ((j*x[c] + i)*p_c*p_c, the V.out block layout); snp_base may be
+ * NULL (first SNP index per cohort, for error reports). */
+int fglsgpu_batch_step(fglsgpu_batch *b, const void *const *dX, const int *x, double *const *dB,
+                       double *const *dV, const long long *snp_base);
+int fglsgpu_batch_sync(fglsgpu_batch *b);
+void *fglsgpu_batch_stream(fglsgpu_batch *b);
+/* Per-stage timing: while enabled, steps run without the graph and CUDA
+ * events bracket the stages; read returns (and clears) the summed ms of
+ * [genotypes, split GEMM, quadratic Gram, solves] and the step count. */
+int fglsgpu_batch_profile(fglsgpu_batch *b, int enable);
+int fglsgpu_batch_profile_read(fglsgpu_batch *b, double *ms, long long *steps);
+const char *fglsgpu_batch_last_error(const fglsgpu_batch *b);
+
 #ifdef __cplusplus
 }
 #endif
