@@ -107,9 +107,10 @@ class ClockSampler:
                 "power_w_max": max(pw) if pw else None, "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def make_problem_gpu(n, t, seed, dev):
+def make_problem_gpu(n, t, seed, dev, h=None, sigma=None):
     """Phi, XL, Y, h, sigma (host numpy) drawn on the device (torch is the
-    data generator only)."""
+    data generator only); h, sigma fixed when given, else h ~ U(0.1, 0.9),
+    sigma ~ U(0.5, 2)."""
     import torch
     g = torch.Generator(device=dev).manual_seed(seed)
     k = 5000
@@ -119,8 +120,10 @@ def make_problem_gpu(n, t, seed, dev):
     G = (G - G.mean(0)) / G.std(0, unbiased=False).clamp_min(1e-12)
     Phi = G @ G.T / k
     Phi.diagonal().add_(1e-3)
-    h = torch.rand(t, generator=g, device=dev, dtype=torch.float64) * 0.8 + 0.1
-    s = torch.rand(t, generator=g, device=dev, dtype=torch.float64) * 1.5 + 0.5
+    hr = torch.rand(t, generator=g, device=dev, dtype=torch.float64) * 0.8 + 0.1
+    sr = torch.rand(t, generator=g, device=dev, dtype=torch.float64) * 1.5 + 0.5
+    h = hr if h is None else torch.full((t,), float(h), device=dev, dtype=torch.float64)
+    s = sr if sigma is None else torch.full((t,), float(sigma), device=dev, dtype=torch.float64)
     XL = torch.ones(n, WXL, device=dev, dtype=torch.float64)
     XL[:, 1:] = torch.randn(n, WXL - 1, generator=g, device=dev, dtype=torch.float64)
     u = torch.randn(k, t, generator=g, device=dev, dtype=torch.float64)
@@ -225,6 +228,174 @@ def orthogonal_basis(n, seed):
         v /= np.linalg.norm(v)
         Z -= 2.0 * np.outer(v, v @ Z)
     return Z
+
+
+def run_chol(args):
+    """The plain chol drop-in workload: n = 10000, p = 4, t = 1, h = 0.5,
+    sigma = 2, blocks of 4096 SNPs.  Device throughput of the all-FP64 path
+    (blocked TRSM, skinny Gram, solve) and of the split path, and end to end
+    through the fgls_chol file entry point (XR streamed from a local file
+    through the pinned ring) for a 16384-SNP file."""
+    import tempfile
+
+    import torch
+    from fgls_gb300 import Engine, fgls_chol, launch_count
+    from fgls_gb300.datagen import read_outputs
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    n, xb, t = args.n, 4096, 1
+    Phi, XL, Y, h, s = make_problem_gpu(n, t, 4321, dev, h=0.5, sigma=2.0)
+    pool = [genotype_block(xb, n, 500 + i, dev) for i in range(2)]
+    p = WXL + WXR
+    dB = torch.empty(xb * p, dtype=torch.float64, device=dev)
+    dV = torch.empty(xb * p * p, dtype=torch.float64, device=dev)
+    out = {}
+    for prec, steps in (("fp64", max(2, args.steps // 6)), ("split", args.steps)):
+        eng = Engine(n, WXL, WXR, t, xb, variant="chol", precision=prec, slices=args.slices)
+        eng.set_problem(Phi, XL, Y, h, s)
+        a = time.perf_counter()
+        eng.select_trait(0)
+        setup = time.perf_counter() - a
+        stream = torch.cuda.ExternalStream(eng.stream(), device=dev)
+
+        def step(k):
+            eng.run_block_device(pool[k % 2].data_ptr(), xb, dB.data_ptr(), dV.data_ptr(), xb * p, xb * p * p)
+
+        for k in range(max(1, min(args.warmup, 3))):
+            step(k)
+        eng.sync()
+        eng.profile(True)
+        l0 = launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(steps):
+            step(k)
+        e1.record(stream)
+        e1.synchronize()
+        eng.sync()
+        prof = eng.profile_read()
+        eng.profile(False)
+        ms = e0.elapsed_time(e1)
+        step0 = pool[0]
+        eng.run_block_device(step0.data_ptr(), xb, dB.data_ptr(), dV.data_ptr(), xb * p, xb * p * p)
+        eng.sync()
+        out[prec] = {"value": steps * xb * t / (ms / 1e3), "ms_per_step": ms / steps, "steps": steps,
+                     "setup_s": setup, "launches": launch_count() - l0,
+                     "kernel_ms_per_step": {k: v[0] / steps for k, v in prof.items() if v[1]},
+                     "B": dB.cpu().numpy().reshape(1, xb, p),
+                     "V": dV.cpu().numpy().reshape(1, xb, p, p).transpose(0, 1, 3, 2)}
+        eng.close()
+    nb, bs, se = rel_errors(out["split"]["B"], out["split"]["V"], out["fp64"]["B"], out["fp64"]["V"])
+    for v in out.values():
+        v.pop("B")
+        v.pop("V")
+    # end to end through the file entry point (reference layout files on local disk)
+    m_e2e = 4 * xb
+    e2e = {}
+    with tempfile.TemporaryDirectory() as d:
+        paths = {k: os.path.join(d, k) for k in ("Phi.in", "H.in", "Sig.in", "XL.in", "XR.in", "Y.in")}
+        Phi.T.astype("<f8").tofile(paths["Phi.in"])
+        h.astype("<f8").tofile(paths["H.in"])
+        s.astype("<f8").tofile(paths["Sig.in"])
+        np.asfortranarray(XL).T.astype("<f8").tofile(paths["XL.in"])
+        np.asfortranarray(Y).T.astype("<f8").tofile(paths["Y.in"])
+        with open(paths["XR.in"], "wb") as f:
+            for i in range(m_e2e // xb):
+                pool[i % 2].cpu().numpy().astype("<f8").tofile(f)
+        for prec in ("fp64", "split"):
+            a = time.perf_counter()
+            fgls_chol(n, p, m_e2e, t, WXL, WXR, xb, 1, 4, paths["Phi.in"], paths["H.in"], paths["Sig.in"],
+                      paths["XL.in"], paths["XR.in"], paths["Y.in"], os.path.join(d, "B.out"),
+                      os.path.join(d, "V.out"), env={"FGLS_PRECISION": prec})
+            wall = time.perf_counter() - a
+            B, _ = read_outputs(d, m_e2e, t, p)
+            e2e[prec] = {"value": m_e2e * t / wall, "unit": UNIT, "wall_s": wall, "snps": m_e2e,
+                         "finite": bool(np.isfinite(B).all())}
+    flops_trsm = float(n) * n * xb
+    trsm_ms = out["fp64"]["kernel_ms_per_step"].get("trsm")
+    line = {
+        "metric": "SNP tests/s, fgls_chol drop-in on 1 GB300 (n=10000, p=4, t=1)",
+        "value": out["fp64"]["value"], "unit": UNIT, "n_gpus": 1, "steps": out["fp64"]["steps"],
+        "warmup": args.warmup, "ms_per_step": out["fp64"]["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"fgls_chol, n={n} p={p} t=1 h=0.5 sigma=2, blocks of {xb} SNPs resident in HBM",
+                   "fp64_path": out["fp64"], "split_path": out["split"],
+                   "split_vs_fp64_error": {"beta_normwise": nb, "beta_se_scaled": bs, "se_rel": se},
+                   "l2": "inputs larger than L2: 2 distinct 0.33 GB blocks cycled"},
+        "roofline": {"bound": "fp64", "achieved": flops_trsm / (trsm_ms / 1e3) / 1e12 if trsm_ms else None,
+                     "peak": 1.25, "unit": "TFLOP/s", "peak_source": "nominal GB300 FP64 (no measured FP64 peak)",
+                     "frac": flops_trsm / (trsm_ms / 1e3) / 1e12 / 1.25 if trsm_ms else None,
+                     "kernel": "dtrsm_llnn (dgemm_kernel + diag_solve_kernel)", "traffic": None},
+        "e2e": {"value": e2e["fp64"]["value"], "unit": UNIT, "h2d_bytes_per_step": xb * n * 8,
+                "d2h_bytes_per_step": xb * (p + p * p) * 8,
+                "api": "fgls_chol file entry point, XR read from a local file through the pinned ring, "
+                       "setup included", "split": e2e["split"], "fp64": e2e["fp64"]},
+        "gpu_launches": out["fp64"]["launches"], "cpu_baseline": None,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_adjoint(args):
+    """Adjoint workload: n = 5000, p = 4, t = 16, FP64 forward and adjoint of
+    the eigen variant per block of 4096 SNPs (Gram blocks recomputed in the
+    backward pass), cotangent ~ N(0, 1)."""
+    import torch
+    from fgls_gb300 import Engine, launch_count
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    n, t, xb = 5000, 16, 4096
+    p = WXL + WXR
+    Phi, XL, Y, h, s = make_problem_gpu(n, t, 99, dev)
+    eng = Engine(n, WXL, WXR, t, xb, variant="eigen", precision="fp64")
+    a = time.perf_counter()
+    eng.set_problem(Phi, XL, Y, h, s)
+    setup = time.perf_counter() - a
+    eng.adjoint_reset()
+    pool = [genotype_block(xb, n, 700 + i, dev) for i in range(2)]
+    g = torch.Generator(device=dev).manual_seed(5)
+    bbar = torch.randn(t * xb * p, generator=g, device=dev, dtype=torch.float64)
+    dB = torch.empty(t * xb * p, dtype=torch.float64, device=dev)
+    dV = torch.empty(t * xb * p * p, dtype=torch.float64, device=dev)
+    stream = torch.cuda.ExternalStream(eng.stream(), device=dev)
+    res = {}
+    for name in ("forward", "adjoint"):
+        def step(k):
+            X = pool[k % 2].data_ptr()
+            if name == "forward":
+                eng.run_block_device(X, xb, dB.data_ptr(), dV.data_ptr(), xb * p, xb * p * p)
+            else:
+                eng.adjoint_block_device(X, xb, bbar.data_ptr(), xb * p)
+        for k in range(2):
+            step(k)
+        eng.sync()
+        l0 = launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(args.steps):
+            step(k)
+        e1.record(stream)
+        e1.synchronize()
+        eng.sync()
+        ms = e0.elapsed_time(e1)
+        res[name] = {"tests_per_s": args.steps * xb * t / (ms / 1e3), "ms_per_block": ms / args.steps,
+                     "launches": launch_count() - l0}
+    dh, ds, dY = eng.adjoint_read()
+    ll, dll = eng.reml()
+    eng.close()
+    both = 1.0 / (1.0 / res["forward"]["tests_per_s"] + 1.0 / res["adjoint"]["tests_per_s"])
+    line = {
+        "metric": "SNP×trait tests/s, fgls_eigen FP64 forward + adjoint on 1 GB300 (n=5000, t=16)",
+        "value": both, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": 2,
+        "ms_per_step": res["forward"]["ms_per_block"] + res["adjoint"]["ms_per_block"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"eigen forward + adjoint, n={n} p={p} t={t}, blocks of {xb} SNPs, m=100000 job",
+                   "setup_s": setup, "forward": res["forward"], "adjoint": res["adjoint"],
+                   "job_s_estimate": 100000 * t / both + setup,
+                   "grad_finite": bool(np.isfinite(dh).all() and np.isfinite(dY).all()),
+                   "reml_dll_dh": [float(v) for v in dll[:4]]},
+        "gpu_launches": res["forward"]["launches"] + res["adjoint"]["launches"], "cpu_baseline": None,
+    }
+    print(json.dumps(line), flush=True)
 
 
 COHORT_BUCKETS = ((500, 1000), (1000, 2000), (2000, 4000), (4000, 8001))
@@ -362,6 +533,11 @@ def run_cohorts(args):
     e2e_s = time.perf_counter() - a
     b.sync()
     e2e_tests = E * sum(xb * c["t"] for c in co)
+    # release every tensor that touched the batch's stream before the stream goes
+    del Xh, Bh, Vh, Xd, X, dB, dV, stream
+    import gc
+    gc.collect()
+    torch.cuda.synchronize()
     b.close()
     line = {
         "metric": "SNP×trait tests/s, batched uneven cohorts (64 problems), split precision",
@@ -437,7 +613,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-snps", type=int, default=128)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="eigen", choices=["eigen", "cohorts"])
+    ap.add_argument("--workload", default="eigen", choices=["eigen", "cohorts", "chol", "adjoint"])
     ap.add_argument("--cohorts", type=int, default=64)
     args = ap.parse_args()
 
@@ -450,6 +626,10 @@ def main():
         args.xb_set = any(a.startswith("--xb") for a in sys.argv[1:])
         args.slices_set = any(a.startswith("--slices") for a in sys.argv[1:])
         return run_cohorts(args)
+    if args.workload == "chol":
+        return run_chol(args)
+    if args.workload == "adjoint":
+        return run_adjoint(args)
 
     import torch
     dist = None

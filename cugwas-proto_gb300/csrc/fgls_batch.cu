@@ -92,6 +92,7 @@ struct fglsgpu_batch {
   int slot = 0;
   GroupedGemm* gg = nullptr;
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+  long long graph_launches = 0;  // kernels per replayed step
   double tune_err = -1.0;
   std::vector<double> tune_rates;
   std::string err;
@@ -236,6 +237,7 @@ cudaError_t enqueue_step(fglsgpu_batch* b, cudaStream_t s, const void* host_tabl
 int capture_graphs(fglsgpu_batch* b) {
   for (int k = 0; k < 2; k++) {
     cudaGraph_t g = nullptr;
+    const long long l0 = g_launches.load();
     B_TRY(b, cudaStreamBeginCapture(b->s, cudaStreamCaptureModeThreadLocal), "graph capture");
     const cudaError_t e1 = enqueue_step(b, b->s, b->hstep[k]);
     const cudaError_t e2 = cudaStreamEndCapture(b->s, &g);
@@ -243,6 +245,8 @@ int capture_graphs(fglsgpu_batch* b) {
       if (g) cudaGraphDestroy(g);
       return bfail(b, FGLSGPU_ECUDA, "graph capture: %s", cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
     }
+    b->graph_launches = g_launches.load() - l0;
+    g_launches.fetch_sub(b->graph_launches);  // counted when replayed
     const cudaError_t e3 = cudaGraphInstantiate(&b->gexec[k], g, 0);
     cudaGraphDestroy(g);
     B_TRY(b, e3, "graph instantiate");
@@ -273,6 +277,7 @@ int launch_step(fglsgpu_batch* b, const void* const* dX, const int* x, double* c
       if (rc) return rc;
     }
     B_TRY(b, cudaGraphLaunch(b->gexec[k], b->s), "graph launch");
+    g_launches.fetch_add(b->graph_launches);
   } else {
     B_TRY(b, enqueue_step(b, b->s, b->hstep[k]), "step");
   }

@@ -14,6 +14,15 @@
 // For chol with t > 1 the XR stream is cached in HBM during the first trait
 // when it fits (the reference re-reads the file for every trait).
 //
+// Block-granular resume (opt-in, FGLS_RESUME=1): every finished block is
+// appended to the journal <B_path>.done after its B/V bytes are on disk
+// (fdatasync), with a header of the run's dimensions.  A later run with the
+// same arguments and FGLS_RESUME=1 keeps the output files, skips the
+// journaled blocks and computes the rest; results are identical to an
+// uninterrupted run because every block lands at its deterministic offset
+// (src/fgls_chol.c:467,474).  FGLS_STOP_AFTER=k (host-side interruption for
+// tests) exits with status 3 after k newly journaled blocks.
+//
 // Errors print "[Error]: <msg>" and exit(EXIT_FAILURE) like the reference's
 // error_msg(msg, 1) (src/common.c:11-17).  Unlike the reference's sync_read,
 // which prints and continues on a short read (src/io.c:13-16), a short read
@@ -138,9 +147,45 @@ int run_variant(int variant, int n, int p, int m, int t, int wXL, int wXR, int x
 
   int xr_fd = open(XR_path, O_RDONLY);
   if (xr_fd < 0) die(std::string("cannot open XR file ") + XR_path + ": " + strerror(errno));
-  int b_fd = open(B_path, O_WRONLY | O_CREAT | O_TRUNC, 0644);
-  int v_fd = open(V_path, O_WRONLY | O_CREAT | O_TRUNC, 0644);
+  // resume journal: header line, then one "<trait> <first SNP>" line per finished block
+  const char* rs = getenv("FGLS_RESUME");
+  const bool resume = rs && atoi(rs) != 0;
+  const char* sa = getenv("FGLS_STOP_AFTER");
+  const long long stop_after = sa ? atoll(sa) : -1;
+  const std::string jpath = std::string(B_path) + ".done";
+  char header[256];
+  snprintf(header, sizeof header, "fgls-journal v1 variant=%d n=%d p=%d m=%d t=%d wXL=%d wXR=%d x_b=%d", variant, n, p,
+           m, t, wXL, wXR, x_b);
+  std::vector<std::pair<int, long long>> done;
+  bool have_journal = false;
+  if (resume) {
+    FILE* jf = fopen(jpath.c_str(), "r");
+    if (jf) {
+      char line[512];
+      if (!fgets(line, sizeof line, jf) || strncmp(line, header, strlen(header)) != 0) {
+        fclose(jf);
+        die("resume journal " + jpath + " was written for different arguments");
+      }
+      int tr;
+      long long ib;
+      while (fscanf(jf, "%d %lld", &tr, &ib) == 2) done.push_back({tr, ib});
+      fclose(jf);
+      have_journal = true;
+    }
+  }
+  const int oflags = O_WRONLY | O_CREAT | (have_journal ? 0 : O_TRUNC);
+  int b_fd = open(B_path, oflags, 0644);
+  int v_fd = open(V_path, oflags, 0644);
   if (b_fd < 0 || v_fd < 0) die("cannot open the output files");
+  FILE* journal = nullptr;
+  if (resume) {
+    journal = fopen(jpath.c_str(), have_journal ? "a" : "w");
+    if (!journal) die("cannot open the resume journal " + jpath);
+    if (!have_journal) {
+      fprintf(journal, "%s\n", header);
+      fflush(journal);
+    }
+  }
 
   const int nt = variant == FGLSGPU_VARIANT_EIGEN ? t : 1;
   const long long colb = (long long)n * wXR;  // doubles per SNP
@@ -151,7 +196,7 @@ int run_variant(int variant, int n, int p, int m, int t, int wXL, int wXR, int x
 
   // Keep XR resident in HBM across chol traits when it fits.
   double* dXall = nullptr;
-  if (variant == FGLSGPU_VARIANT_CHOL && t > 1) {
+  if (variant == FGLSGPU_VARIANT_CHOL && t > 1 && done.empty()) {
     size_t fr = 0, tot = 0;
     cudaMemGetInfo(&fr, &tot);
     const size_t need = sizeof(double) * (size_t)colb * m;
@@ -178,10 +223,19 @@ int run_variant(int variant, int n, int p, int m, int t, int wXL, int wXR, int x
 
   std::vector<Item> items;
   const int passes = variant == FGLSGPU_VARIANT_EIGEN ? 1 : t;
+  long long skipped = 0;
   for (int j = 0; j < passes; j++)
-    for (long long ib = 0; ib < m; ib += x_b)
-      items.push_back({variant == FGLSGPU_VARIANT_EIGEN ? -1 : j, ib, (int)std::min<long long>(x_b, m - ib),
-                       !(dXall && j > 0)});
+    for (long long ib = 0; ib < m; ib += x_b) {
+      const int tr = variant == FGLSGPU_VARIANT_EIGEN ? -1 : j;
+      if (std::find(done.begin(), done.end(), std::make_pair(tr, ib)) != done.end()) {
+        skipped++;
+        continue;
+      }
+      items.push_back({tr, ib, (int)std::min<long long>(x_b, m - ib), !(dXall && j > 0)});
+    }
+  if (resume && skipped)
+    fprintf(stderr, "[resume] %lld of %lld blocks already done\n", skipped, skipped + (long long)items.size());
+  long long journaled = 0;
 
   auto start_read = [&](int i) {
     Slot& s = sl2[i & 1];
@@ -203,6 +257,17 @@ int run_variant(int variant, int n, int p, int m, int t, int wXL, int wXR, int x
       if (!pwrite_full(b_fd, s.hB + (size_t)q * it.x * p, sizeof(double) * it.x * p, ob) ||
           !pwrite_full(v_fd, s.hV + (size_t)q * it.x * p * p, sizeof(double) * it.x * p * p, ov))
         die(std::string("write to ") + B_path + " / " + V_path + " failed: " + strerror(errno));
+    }
+    if (journal) {
+      if (fdatasync(b_fd) != 0 || fdatasync(v_fd) != 0)
+        die(std::string("flushing ") + B_path + " / " + V_path + " failed: " + strerror(errno));
+      fprintf(journal, "%d %lld\n", it.trait, it.ib);
+      if (fflush(journal) != 0 || fdatasync(fileno(journal)) != 0) die("writing the resume journal failed");
+      if (stop_after >= 0 && ++journaled >= stop_after) {
+        fprintf(stderr, "[resume] stopping after %lld blocks (FGLS_STOP_AFTER)\n", journaled);
+        cudaDeviceSynchronize();  // leave between blocks, with no work in flight
+        exit(3);
+      }
     }
   };
 
@@ -264,6 +329,7 @@ int run_variant(int variant, int n, int p, int m, int t, int wXL, int wXR, int x
   cudaStreamDestroy(h2d);
   cudaStreamDestroy(d2h);
   close(xr_fd);
+  if (journal) fclose(journal);
   if (close(b_fd) != 0 || close(v_fd) != 0) die("closing the output files failed");
   fglsgpu_destroy(e);
   return 0;

@@ -43,6 +43,7 @@ struct fglsgpu_engine {
   double* dQ = nullptr;     // eigen: self-product operand
   double *dGYL = nullptr, *dGR = nullptr;
   double *dB[2]{}, *dV[2]{};
+  double *dSE[2]{}, *dP[2]{};  // compact outputs (allocated on first use)
   unsigned char* dU8 = nullptr;
   DevStatus* dst = nullptr;
   DevStatus* hst = nullptr;
@@ -114,6 +115,8 @@ int check_status(fglsgpu_engine* e, const char* stage) {
     if (s.info < 0) return fail(e, FGLSGPU_ENOTSPD, "dpotrf(scoreV) failed (info: -1) - trait: %lld", s.idx);
     return fail(e, FGLSGPU_ENOTSPD, "dpotrf(V) failed (info: %d) - i: %lld", s.info, s.idx);
   }
+  if (s.code == FGLSGPU_EINVAL)
+    return fail(e, FGLSGPU_EINVAL, "missing genotype (2-bit code 01) at SNP %lld, individual %d", s.idx, s.info);
   if (s.code == FGLSGPU_ETIMEOUT)
     return fail(e, FGLSGPU_ETIMEOUT, "device wait expired in %s (site %d, item %lld)", stage, s.info, s.idx);
   return fail(e, s.code, "device status %d in %s (info %d, item %lld)", s.code, stage, s.info, s.idx);
@@ -129,7 +132,8 @@ void free_all(fglsgpu_engine* e) {
                   e->dZtXL, e->dZtY, e->ddinv, e->dAYL, e->dtop, e->deigwork, e->dX[0], e->dX[1], e->dWork,
                   e->dQ,   e->dGYL, e->dGR,  e->dB[0], e->dB[1], e->dV[0], e->dV[1], e->dU8, e->dst,
                   e->aWc, e->aAYLc, e->aAYLs, e->atopc, e->atops, e->areml, e->aGYLc, e->aGYLs, e->aGRc,
-                  e->aGRs, e->acontrib, e->ag, e->agR, e->aacc, e->aU, e->aV2};
+                  e->aGRs, e->acontrib, e->ag, e->agR, e->aacc, e->aU, e->aV2, e->dSE[0], e->dSE[1], e->dP[0],
+                  e->dP[1]};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (e->hst) cudaFreeHost(e->hst);
@@ -463,6 +467,19 @@ int fglsgpu_run_block_device_u8(fglsgpu_engine* e, const unsigned char* dXR, int
   return compute_block(e, nullptr, dXR, x_inc, dB, dV, bstr, vstr, 0);
 }
 
+int fglsgpu_run_block_device_packed(fglsgpu_engine* e, const unsigned char* dXR2, int x_inc, double* dB, double* dV,
+                                    long long bstr, long long vstr) {
+  if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
+  if (!e->problem_set) return fail(e, FGLSGPU_ESTATE, "set_problem must precede run_block");
+  if (x_inc <= 0 || x_inc > e->cfg.x_b) return fail(e, FGLSGPU_EINVAL, "x_inc=%d outside [1, %d]", x_inc, e->cfg.x_b);
+  if (!dXR2 || !dB || !dV) return fail(e, FGLSGPU_EINVAL, "null block pointer");
+  ENG_TRY(e, cudaSetDevice(e->cfg.device), "cudaSetDevice");
+  const long long cols = (long long)x_inc * e->cfg.wXR;
+  if (!e->dU8) ENG_TRY(e, dalloc(&e->dU8, (size_t)e->cfg.x_b * e->cfg.wXR * e->cfg.n), "genotype bytes");
+  ENG_TRY(e, unpack_2bit(e->comp, dXR2, e->cfg.n, cols, e->cfg.wXR, e->dU8, e->dst, 0), "unpack genotypes");
+  return compute_block(e, nullptr, e->dU8, x_inc, dB, dV, bstr, vstr, 0);
+}
+
 int fglsgpu_sync(fglsgpu_engine* e) {
   if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
   ENG_TRY(e, cudaSetDevice(e->cfg.device), "cudaSetDevice");
@@ -503,10 +520,13 @@ int fglsgpu_run_block(fglsgpu_engine* e, const double* XR, int x_inc, double* B,
 // traits (eigen: trait j at j*m*p; chol: the selected trait at 0).  Blocks
 // of x_b SNPs flow through two device slots: H2D on one stream, compute on
 // another, D2H on a third, so copies of block b+1 and b-1 overlap block b.
-int fglsgpu_run_snps(fglsgpu_engine* e, const double* XR, long long m, double* B, double* V) {
-  if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
-  if (!e->problem_set) return fail(e, FGLSGPU_ESTATE, "set_problem must precede run_snps");
-  if (m <= 0 || !XR || !B || !V) return fail(e, FGLSGPU_EINVAL, "invalid run_snps arguments");
+}  // extern "C"
+
+namespace {
+
+// Whole-job pipeline over host XR: full (V) or compact (SE, P) outputs.
+int run_snps_impl(fglsgpu_engine* e, const double* XR, long long m, double* B, double* V, double* SE, double* P) {
+  const bool compact = V == nullptr;
   const fglsgpu_config& c = e->cfg;
   if (c.variant == FGLSGPU_VARIANT_CHOL && e->trait_sel < 0)
     return fail(e, FGLSGPU_ESTATE, "fglsgpu_select_trait must precede run_snps (chol)");
@@ -530,19 +550,54 @@ int fglsgpu_run_snps(fglsgpu_engine* e, const double* XR, long long m, double* B
     const long long db = (long long)x * p, dv = (long long)x * p * p;
     rc = compute_block(e, e->dX[k], nullptr, x, e->dB[k], e->dV[k], db, dv, ib);
     if (rc) return rc;
+    if (compact)
+      ENG_TRY(e, snp_compact(e->comp, x, nt, p, e->dB[k], db, e->dV[k], dv, e->dSE[k], e->dP[k], db), "compact");
     ENG_TRY(e, cudaEventRecord(e->evC[k], e->comp), "event");
     ENG_TRY(e, cudaStreamWaitEvent(e->d2h, e->evC[k], 0), "wait");
     ENG_TRY(e, cudaMemcpy2DAsync(B + ib * p, sizeof(double) * m * p, e->dB[k], sizeof(double) * db,
                                  sizeof(double) * db, nt, cudaMemcpyDeviceToHost, e->d2h),
             "B download");
-    ENG_TRY(e, cudaMemcpy2DAsync(V + ib * p * p, sizeof(double) * m * p * p, e->dV[k], sizeof(double) * dv,
-                                 sizeof(double) * dv, nt, cudaMemcpyDeviceToHost, e->d2h),
-            "V download");
+    if (!compact) {
+      ENG_TRY(e, cudaMemcpy2DAsync(V + ib * p * p, sizeof(double) * m * p * p, e->dV[k], sizeof(double) * dv,
+                                   sizeof(double) * dv, nt, cudaMemcpyDeviceToHost, e->d2h),
+              "V download");
+    } else {
+      ENG_TRY(e, cudaMemcpy2DAsync(SE + ib * p, sizeof(double) * m * p, e->dSE[k], sizeof(double) * db,
+                                   sizeof(double) * db, nt, cudaMemcpyDeviceToHost, e->d2h),
+              "SE download");
+      ENG_TRY(e, cudaMemcpy2DAsync(P + ib * p, sizeof(double) * m * p, e->dP[k], sizeof(double) * db,
+                                   sizeof(double) * db, nt, cudaMemcpyDeviceToHost, e->d2h),
+              "P download");
+    }
     ENG_TRY(e, cudaEventRecord(e->evD[k], e->d2h), "event");
   }
   ENG_TRY(e, cudaStreamSynchronize(e->d2h), "run_snps");
   ENG_TRY(e, cudaStreamSynchronize(e->h2d), "run_snps");
   return check_status(e, "block");
+}
+
+}  // namespace
+
+extern "C" {
+
+int fglsgpu_run_snps(fglsgpu_engine* e, const double* XR, long long m, double* B, double* V) {
+  if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
+  if (!e->problem_set) return fail(e, FGLSGPU_ESTATE, "set_problem must precede run_snps");
+  if (m <= 0 || !XR || !B || !V) return fail(e, FGLSGPU_EINVAL, "invalid run_snps arguments");
+  return run_snps_impl(e, XR, m, B, V, nullptr, nullptr);
+}
+
+int fglsgpu_run_snps_compact(fglsgpu_engine* e, const double* XR, long long m, double* B, double* SE, double* P) {
+  if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
+  if (!e->problem_set) return fail(e, FGLSGPU_ESTATE, "set_problem must precede run_snps");
+  if (m <= 0 || !XR || !B || !SE || !P) return fail(e, FGLSGPU_EINVAL, "invalid run_snps_compact arguments");
+  ENG_TRY(e, cudaSetDevice(e->cfg.device), "cudaSetDevice");
+  const size_t per = (size_t)out_traits(e) * e->cfg.x_b * e->p;
+  for (int k = 0; k < 2; k++) {
+    if (!e->dSE[k]) ENG_TRY(e, dalloc(&e->dSE[k], per), "compact buffers");
+    if (!e->dP[k]) ENG_TRY(e, dalloc(&e->dP[k], per), "compact buffers");
+  }
+  return run_snps_impl(e, XR, m, B, nullptr, SE, P);
 }
 
 int fglsgpu_set_precision(fglsgpu_engine* e, int precision) {

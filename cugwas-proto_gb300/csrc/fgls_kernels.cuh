@@ -60,6 +60,14 @@ struct StepCohort;
 cudaError_t snp_solve_grouped(cudaStream_t s, int p, const SolveProblem* probs, const int* plist, int count, int x_b,
                               const StepCohort* sc, DevStatus* st);
 
+// compact outputs: SE and p-value of every coefficient (layout of B)
+cudaError_t snp_compact(cudaStream_t s, int x, int t, int p, const double* B, long long bstride, const double* V,
+                        long long vstride, double* SE, double* P, long long cstride);
+
+// 2-bit packed genotypes (PLINK .bed codes, ceil(n/4) bytes per column) -> bytes
+cudaError_t unpack_2bit(cudaStream_t s, const unsigned char* in, int n, long long cols, int wXR, unsigned char* out,
+                        DevStatus* st, long long snp_base);
+
 // Two-sided normal p-values of the SNP coefficients from B and V (fgls_snp.cu).
 cudaError_t snp_pvalues(cudaStream_t s, int x, int t, int p, int wXL, const double* B, long long bstride,
                         const double* V, long long vstride, double* P, long long pstride);

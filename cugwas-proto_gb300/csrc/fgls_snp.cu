@@ -416,9 +416,38 @@ __global__ void u8_to_f64_kernel(const unsigned char* __restrict__ in, double* _
     out[e] = (double)in[e];
 }
 
+// 2-bit packed hard calls, SNP-major like a PLINK .bed body: column c holds
+// ceil(n/4) bytes, individual k in bits 2(k%4)..2(k%4)+1 of byte k/4.  Codes:
+// 00 -> 2, 10 -> 1, 11 -> 0 (copies of the first allele), 01 = missing (status
+// FGLSGPU_EINVAL with the individual and the SNP, value 0).
+__global__ void unpack_2bit_kernel(const unsigned char* __restrict__ in, int n, long long cols, int wXR,
+                                   unsigned char* __restrict__ out, DevStatus* st, long long snp_base) {
+  const long long bpc = (n + 3) / 4;
+  const long long total = cols * n;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(e % n);
+    const long long c = e / n;
+    const unsigned code = (in[c * bpc + (k >> 2)] >> (2 * (k & 3))) & 3u;
+    unsigned char v = code == 0u ? 2 : (code == 2u ? 1 : 0);
+    if (code == 1u) set_status(st, FGLSGPU_EINVAL, k, snp_base + c / wXR);
+    out[e] = v;
+  }
+}
+
 }  // namespace
 
 std::atomic<long long> g_launches{0};
+
+cudaError_t unpack_2bit(cudaStream_t s, const unsigned char* in, int n, long long cols, int wXR, unsigned char* out,
+                        DevStatus* st, long long snp_base) {
+  const long long total = cols * n;
+  const int blocks = (int)std::min<long long>((total + 255) / 256, 152LL * 32);
+  if (blocks <= 0) return cudaSuccess;
+  unpack_2bit_kernel<<<blocks, 256, 0, s>>>(in, n, cols, wXR, out, st, snp_base);
+  note_launch();
+  return cudaGetLastError();
+}
 
 cudaError_t u8_to_f64(cudaStream_t s, const unsigned char* in, double* out, long long count) {
   int blocks = (int)std::min<long long>((count + 255) / 256, 152LL * 32);
@@ -538,6 +567,35 @@ __global__ void pvalues_kernel(int x, int t, int p, int wXL, const double* __res
   }
 }
 }  // namespace
+
+namespace {
+// SE_k = V_kk and p_k = erfc(|beta_k / SE_k| / sqrt 2) for every coefficient
+__global__ void compact_kernel(int x, int t, int p, const double* __restrict__ B, long long bstride,
+                               const double* __restrict__ V, long long vstride, double* __restrict__ SE,
+                               double* __restrict__ P, long long cstride) {
+  const long long total = (long long)x * t * p;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(e % p);
+    const long long r = e / p;
+    const int i = (int)(r % x), j = (int)(r / x);
+    const double beta = B[(long long)j * bstride + (long long)i * p + k];
+    const double se = V[(long long)j * vstride + (long long)i * p * p + k + k * p];
+    SE[(long long)j * cstride + (long long)i * p + k] = se;
+    P[(long long)j * cstride + (long long)i * p + k] = erfc(fabs(beta / se) * 0.70710678118654752440);
+  }
+}
+}  // namespace
+
+cudaError_t snp_compact(cudaStream_t s, int x, int t, int p, const double* B, long long bstride, const double* V,
+                        long long vstride, double* SE, double* P, long long cstride) {
+  const long long total = (long long)x * t * p;
+  const int blocks = (int)std::min<long long>((total + 255) / 256, 152LL * 32);
+  if (blocks <= 0) return cudaSuccess;
+  compact_kernel<<<blocks, 256, 0, s>>>(x, t, p, B, bstride, V, vstride, SE, P, cstride);
+  note_launch();
+  return cudaGetLastError();
+}
 
 cudaError_t snp_pvalues(cudaStream_t s, int x, int t, int p, int wXL, const double* B, long long bstride,
                         const double* V, long long vstride, double* P, long long pstride) {

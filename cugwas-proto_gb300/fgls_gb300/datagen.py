@@ -145,3 +145,16 @@ def read_outputs(d: str, m: int, t: int, p: int, bname="B.out", vname="V.out"):
     B = B[: t * m * p].reshape(t, m, p)
     V = V[: t * m * p * p].reshape(t, m, p, p).transpose(0, 1, 3, 2)
     return B, V
+
+
+def pack_2bit(X: np.ndarray) -> np.ndarray:
+    """Hard calls (columns x n, values 0/1/2, or -1 for missing) -> 2-bit
+    SNP-major bytes as in a PLINK .bed body: ceil(n/4) bytes per column,
+    individual k in bits 2(k%4).., codes 2 -> 00, 1 -> 10, 0 -> 11, missing -> 01."""
+    X = np.asarray(X)
+    cols, n = X.shape
+    code = np.select([X == 2, X == 1, X == 0], [0, 2, 3], default=1).astype(np.uint8)
+    pad = (-n) % 4
+    code = np.concatenate([code, np.full((cols, pad), 3, np.uint8)], axis=1).reshape(cols, -1, 4)
+    return (code[..., 0] | (code[..., 1] << 2) | (code[..., 2] << 4) | (code[..., 3] << 6)).astype(np.uint8)
+

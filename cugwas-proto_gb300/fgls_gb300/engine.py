@@ -41,7 +41,7 @@ EXPORTS = (
     "fglsgpu_adjoint_block_device", "fglsgpu_adjoint_read", "fglsgpu_reml", "fglsgpu_pvalues_device",
     "fglsgpu_batch_create", "fglsgpu_batch_destroy", "fglsgpu_batch_params", "fglsgpu_batch_step",
     "fglsgpu_batch_sync", "fglsgpu_batch_stream", "fglsgpu_batch_last_error", "fglsgpu_batch_profile",
-    "fglsgpu_batch_profile_read",
+    "fglsgpu_batch_profile_read", "fglsgpu_run_block_device_packed", "fglsgpu_run_snps_compact",
 )
 PROF_CLASSES = ("genotypes", "split_gemm", "selfgram", "solve", "fp64_gemm", "trsm", "gram", "spare")
 
@@ -85,8 +85,10 @@ def lib():
     L.fglsgpu_select_trait.argtypes = [P, I]
     L.fglsgpu_run_block.argtypes = [P, P, I, P, P, LL, LL]
     L.fglsgpu_run_snps.argtypes = [P, P, LL, P, P]
+    L.fglsgpu_run_snps_compact.argtypes = [P, P, LL, P, P, P]
     L.fglsgpu_run_block_device.argtypes = [P, P, I, P, P, LL, LL]
     L.fglsgpu_run_block_device_u8.argtypes = [P, P, I, P, P, LL, LL]
+    L.fglsgpu_run_block_device_packed.argtypes = [P, P, I, P, P, LL, LL]
     L.fglsgpu_sync.argtypes = [P]
     L.fglsgpu_get_res_sigma.argtypes = [P, P]
     L.fglsgpu_get_eigen.argtypes = [P, P, P]
@@ -183,13 +185,23 @@ class Engine:
         self._check(self.L.fglsgpu_run_snps(self._h, _ptr(XR), m, _ptr(B), _ptr(V)))
         return B, V.transpose(0, 1, 3, 2)
 
+    def run_snps_compact(self, XR):
+        """B, SE, P each (traits, m, p)."""
+        XR = _f64(XR)
+        m = XR.shape[1] // self.wXR
+        nt, p = self.out_traits, self.p
+        B, SE, P = (np.empty((nt, m, p)) for _ in range(3))
+        self._check(self.L.fglsgpu_run_snps_compact(self._h, _ptr(XR), m, _ptr(B), _ptr(SE), _ptr(P)))
+        return B, SE, P
+
     def run_snps_ptr(self, xr_ptr, m, b_ptr, v_ptr):
         """Host pointers (e.g. pinned torch tensors): XR, B, V."""
         self._check(self.L.fglsgpu_run_snps(self._h, C.c_void_p(xr_ptr), int(m), C.c_void_p(b_ptr),
                                             C.c_void_p(v_ptr)))
 
-    def run_block_device(self, xr_ptr, x, b_ptr, v_ptr, bstride, vstride, u8=False):
-        f = self.L.fglsgpu_run_block_device_u8 if u8 else self.L.fglsgpu_run_block_device
+    def run_block_device(self, xr_ptr, x, b_ptr, v_ptr, bstride, vstride, u8=False, packed=False):
+        f = (self.L.fglsgpu_run_block_device_packed if packed else
+             self.L.fglsgpu_run_block_device_u8 if u8 else self.L.fglsgpu_run_block_device)
         self._check(f(self._h, C.c_void_p(xr_ptr), int(x), C.c_void_p(b_ptr), C.c_void_p(v_ptr),
                       int(bstride), int(vstride)))
 

@@ -122,6 +122,14 @@ int fglsgpu_run_block(fglsgpu_engine *e, const double *XR, int x_inc, double *B,
  * buffering, src/fgls_chol.c:327-487). */
 int fglsgpu_run_snps(fglsgpu_engine *e, const double *XR, long long m, double *B, double *V);
 
+/* As fglsgpu_run_snps with a compact output: instead of V (p*p doubles per
+ * test) the standard errors SE and the two-sided normal p-values P of all p
+ * coefficients, both in the B layout (trait j, SNP i, coefficient k at
+ * (j*m + i)*p + k).  8x less output than B + V at p = 4.  No counterpart in
+ * the reference (it writes B and V only, src/fgls_chol.c:464-474). */
+int fglsgpu_run_snps_compact(fglsgpu_engine *e, const double *XR, long long m, double *B, double *SE,
+                             double *P);
+
 /* Same with DEVICE pointers (XR, B, V already in HBM); asynchronous with
  * respect to the host: call fglsgpu_sync before reading B/V. */
 int fglsgpu_run_block_device(fglsgpu_engine *e, const double *dXR, int x_inc, double *dB,
@@ -132,6 +140,16 @@ int fglsgpu_run_block_device(fglsgpu_engine *e, const double *dXR, int x_inc, do
 int fglsgpu_run_block_device_u8(fglsgpu_engine *e, const unsigned char *dXR, int x_inc,
                                 double *dB, double *dV, long long b_trait_stride,
                                 long long v_trait_stride);
+
+/* As run_block_device_u8 with genotypes packed 2 bits per individual, the
+ * body of a SNP-major PLINK .bed file: each of the x_inc*wXR columns holds
+ * ceil(n/4) bytes, individual k in bits 2(k%4)..2(k%4)+1 of byte k/4, codes
+ * 00 -> 2, 10 -> 1, 11 -> 0 copies of the first allele.  Code 01 (missing)
+ * is reported by fglsgpu_sync as FGLSGPU_EINVAL.  32x fewer bytes than FP64.
+ * No counterpart in the reference (it reads FP64 only, src/fgls_chol.c:333-337). */
+int fglsgpu_run_block_device_packed(fglsgpu_engine *e, const unsigned char *dXR2, int x_inc,
+                                    double *dB, double *dV, long long b_trait_stride,
+                                    long long v_trait_stride);
 
 /* Waits for the engine's device work and reports device-side failures
  * (non-SPD per-SNP systems, expired waits). */

@@ -74,3 +74,18 @@ def test_engine_without_gpu_fails_loudly(has_gpu):
     from fgls_gb300 import Engine, FGLSError
     with pytest.raises(FGLSError, match="no CUDA device"):
         Engine(100, 3, 1, 1, 16)
+
+
+def test_pack_2bit_layout():
+    """The packer follows the 2-bit SNP-major layout the device unpacker reads."""
+    import numpy as np
+    from fgls_gb300 import datagen
+    rng = np.random.default_rng(3)
+    X = rng.integers(-1, 3, size=(5, 13))
+    P = datagen.pack_2bit(X)
+    assert P.shape == (5, 4) and P.dtype == np.uint8
+    dec = {0: 2, 2: 1, 3: 0, 1: -1}
+    for c in range(5):
+        for k in range(13):
+            code = (int(P[c, k // 4]) >> (2 * (k % 4))) & 3
+            assert dec[code] == X[c, k]

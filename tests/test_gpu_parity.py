@@ -197,3 +197,84 @@ def test_pvalues_match_normal_tail():
     P = dP.cpu().numpy().reshape(2, x, 2)
     z = B[..., 2:] / np.stack([V[..., 2, 2], V[..., 3, 3]], axis=-1)
     assert np.allclose(P, 2 * norm.sf(np.abs(z)), rtol=1e-12, atol=1e-300)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_packed_2bit_genotypes_match_byte_input(precision):
+    import torch
+    from fgls_gb300 import Engine, FGLSError, datagen
+    pb = datagen.make_problem(301, 150, 3, seed=12, hsig_uniform=True)
+    p, x = pb.p, pb.m
+    G = np.ascontiguousarray(pb.XR.T.astype(np.uint8))           # (m, n)
+    packed = torch.from_numpy(datagen.pack_2bit(G)).cuda()
+    u8 = torch.from_numpy(G).cuda()
+    outs = []
+    with Engine(pb.n, 3, 1, 3, x, variant="eigen", precision=precision) as e:
+        e.set_problem(pb.Phi, pb.XL, pb.Y, pb.h, pb.sigma)
+        for src, kw in ((u8, {"u8": True}), (packed, {"packed": True})):
+            dB = torch.empty(3 * x * p, dtype=torch.float64, device="cuda")
+            dV = torch.empty(3 * x * p * p, dtype=torch.float64, device="cuda")
+            e.run_block_device(src.data_ptr(), x, dB.data_ptr(), dV.data_ptr(), x * p, x * p * p, **kw)
+            e.sync()
+            outs.append((dB.cpu().numpy(), dV.cpu().numpy()))
+        assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+        # a missing call is reported, not silently imputed
+        Gm = G.copy().astype(np.int16)
+        Gm[7, 5] = -1
+        bad = torch.from_numpy(datagen.pack_2bit(Gm)).cuda()
+        dB = torch.empty(3 * x * p, dtype=torch.float64, device="cuda")
+        dV = torch.empty(3 * x * p * p, dtype=torch.float64, device="cuda")
+        e.run_block_device(bad.data_ptr(), x, dB.data_ptr(), dV.data_ptr(), x * p, x * p * p, packed=True)
+        with pytest.raises(FGLSError, match="missing genotype .* SNP 7, individual 5"):
+            e.sync()
+
+
+@pytest.mark.parametrize("variant,t", [("chol", 2), ("eigen", 3)])
+def test_dropin_block_resume_after_interruption(variant, t):
+    """FGLS_RESUME=1: a run stopped on the host after 2 blocks (FGLS_STOP_AFTER)
+    and resumed computes only the missing blocks; B.out/V.out are identical to
+    an uninterrupted run."""
+    from fgls_gb300 import FGLSError, datagen, fgls_chol, fgls_eigen
+    pb = datagen.make_problem(200, 700, t, seed=31, hsig_uniform=True)
+    d = tempfile.mkdtemp()
+    paths = datagen.write_problem(pb, d)
+    fn = fgls_chol if variant == "chol" else fgls_eigen
+
+    def run(bname, env):
+        args = (pb.n, pb.p, pb.m, pb.t, pb.wXL, pb.wXR, 128, 1, 2, paths["Phi.in"], paths["H.in"], paths["Sig.in"],
+                paths["XL.in"], paths["XR.in"], paths["Y.in"], os.path.join(d, bname + ".B"),
+                os.path.join(d, bname + ".V"))
+        fn(*args, env=env)
+
+    run("full", {})
+    with pytest.raises(FGLSError) as ei:
+        run("part", {"FGLS_RESUME": "1", "FGLS_STOP_AFTER": "2"})
+    assert ei.value.code == 3
+    with open(os.path.join(d, "part.B.done")) as f:
+        assert len(f.read().splitlines()) == 1 + 2
+    run("part", {"FGLS_RESUME": "1"})
+    for ext in ("B", "V"):
+        a = np.fromfile(os.path.join(d, "full." + ext))
+        b = np.fromfile(os.path.join(d, "part." + ext))
+        assert a.size == b.size and np.array_equal(a, b)
+    # a journal from other arguments is refused
+    args = (pb.n, pb.p, pb.m, pb.t, pb.wXL, pb.wXR, 64, 1, 2, paths["Phi.in"], paths["H.in"], paths["Sig.in"],
+            paths["XL.in"], paths["XR.in"], paths["Y.in"], os.path.join(d, "part.B"), os.path.join(d, "part.V"))
+    with pytest.raises(FGLSError, match="different arguments"):
+        fn(*args, env={"FGLS_RESUME": "1"})
+
+
+@pytest.mark.parametrize("variant", ["chol", "eigen"])
+def test_run_snps_compact_matches_full_output(variant):
+    from scipy.special import erfc
+    from fgls_gb300 import Engine, datagen
+    pb = datagen.make_problem(180, 300, 2, seed=44, hsig_uniform=True)
+    with Engine(pb.n, 3, 1, 2, 128, variant=variant) as e:
+        e.set_problem(pb.Phi, pb.XL, pb.Y, pb.h, pb.sigma)
+        e.select_trait(1)
+        B, V = e.run_snps(pb.XR)
+        Bc, SE, P = e.run_snps_compact(pb.XR)
+    idx = np.arange(pb.p)
+    assert np.array_equal(B, Bc)
+    assert np.array_equal(SE, V[..., idx, idx])
+    assert np.allclose(P, erfc(np.abs(B / SE) / np.sqrt(2.0)), rtol=1e-13, atol=1e-300)
