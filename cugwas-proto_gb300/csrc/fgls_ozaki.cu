@@ -37,6 +37,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
 
 #include <algorithm>
 #include <vector>
@@ -197,6 +199,14 @@ struct GroupedProblem {
 struct GroupedTile {
   int prob, m_tile, n_tile, pad;
 };
+
+// An integer-valued float |f| < 2^22 as int without a conversion instruction:
+// f + 1.5 * 2^23 lies in [2^23, 2^24), where the float's mantissa bits are
+// the integer f + 2^22.  (Every slice product sum of the split GEMM is such an
+// integer: |P| <= 128 * 2 * K < 2^22 for K <= 16383.)
+__device__ __forceinline__ int exact_f2i(float f) {
+  return __float_as_int(__fadd_rn(f, 12582912.0f)) - 0x4B400000;
+}
 
 // Exact int64 value V times a power-of-two scale, squared, as a float pair:
 // v = V*scale = vh + vl (|vl| <= 2^-24 |vh|), v^2 ~= ah + al with
@@ -370,8 +380,8 @@ __device__ __forceinline__ void gemm_tile(const CUtensorMap* tmA, const CUtensor
 #pragma unroll
         for (int j = 0; j < 32; j++) {
           if (c0 + j >= cend) break;
-          int qv = __float2int_rn(__uint_as_float(v0[j])) * 256;
-          if (two) qv += __float2int_rn(__uint_as_float(v1[j]));
+          int qv = exact_f2i(__uint_as_float(v0[j])) * 256;
+          if (two) qv += exact_f2i(__uint_as_float(v1[j]));
           long long* cp = crow + (long long)(c0 + j) * g.ldc;
           const long long V = (p == 0) ? (long long)qv : prev[j] * 65536LL + (long long)qv;
           if (!last)
@@ -420,6 +430,301 @@ __global__ void __launch_bounds__(THREADS, 1)
 }
 
 // ---------------------------------------------------------------------------
+// Quadratic Gram terms on the tensor cores (eigen, many traits):
+//
+//   GR[i + j*ldg] = sum_l R2[l,i] d_j(l),  R2 >= 0, d > 0.
+//
+// Both operands are cut into signed base-64 digits (6 bits, |digit| <= 32):
+// a = R2 / sigma_i = sum_s alpha_s 64^-s, b = d / tau_j = sum_t delta_t 64^-t
+// with sigma_i, tau_j powers of two such that a, b <= 1/2.  A digit product
+// is at most 2^10, so a K-sum over K <= 16384 rows is an integer of at most
+// 2^24: exact in the FP32 TMEM accumulator.  Pairs with s + t <= L are kept
+// (L = 11: dropped terms below 2^-60 of sigma_i tau_j per row).  The epilogue
+// scales each exact pair sum by 64^-(s+t) (exact) and accumulates it in a
+// float pair by TwoSum (relative error ~2^-47), then multiplies by
+// sigma_i tau_j in FP64.
+//
+// quadtc_kernel: one CTA per 128 SNP rows, all traits (<= 112) as N.  A pass
+// holds one SNP digit s (A tile 128 x 64) and up to four trait digits t
+// (B tiles 112 x 64, two per MMA as N = 224); TMEM accumulators at columns
+// [0, 224) and [224, 448).  Same warp roles and bounded waits as
+// ozaki_gemm_kernel.  Threads keep the running (hi, lo) sums of 56 traits.
+// ---------------------------------------------------------------------------
+constexpr int QT_TP = 112;                          // trait rows of the digit operand
+constexpr int QT_BT = QT_TP * BK * 2;               // 14 KB trait tile
+constexpr int QT_STAGE = A_TILE + 4 * QT_BT;        // 72 KB
+constexpr int QT_SMEM = STAGES * QT_STAGE + 1024 + 256;
+constexpr int QT_MAXPASS = 40;
+constexpr uint32_t QT_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(224 >> 3) << 17) |
+                              ((uint32_t)(BM >> 4) << 24);
+
+struct QuadPasses {
+  int n;
+  signed char s[QT_MAXPASS];     // SNP digit (1-based)
+  signed char t[QT_MAXPASS][4];  // trait digits (1-based, 0 = empty slot)
+};
+
+struct QuadArgs {
+  int x;          // valid SNP rows
+  int t;          // valid traits
+  int Ncap;       // rows per SNP digit slice
+  int Kpad;
+  const int* aexp;  // per SNP: sigma_i = 2^aexp
+  const int* dexp;  // per trait: tau_j = 2^dexp
+  double* GR;
+  long long ldg;
+  int* err;
+};
+
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+}
+
+__device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bp = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+    quadtc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmD,
+                  const __grid_constant__ QuadPasses qp, const QuadArgs g) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + STAGES * QT_STAGE);
+  uint64_t* empty = full + STAGES;
+  uint64_t* tfull = empty + STAGES;
+  uint64_t* tempty = tfull + 1;
+  uint64_t* drain = tempty + 1;
+  uint32_t* tbase_slot = (uint32_t*)(drain + 1);
+  volatile int* abort_flag = (volatile int*)(tbase_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * BM;
+  const int nk = g.Kpad / BK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(tfull, 1);
+    mbar_init(tempty, THREADS - 64);
+    mbar_init(drain, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tbase_slot)),
+                 "r"(512)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = *tbase_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      int issued[STAGES];
+      uint32_t issued_phase[STAGES];
+      for (int s = 0; s < STAGES; s++) issued[s] = 0;
+      bool ok = true;
+      for (int p = 0; p < qp.n && ok; p++) {
+        int nt = 0;
+        for (int q = 0; q < 4; q++) nt += qp.t[p][q] > 0 ? 1 : 0;
+        for (int kb = 0; kb < nk; kb++) {
+          if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, g.err, 11)) { ok = false; break; }
+          issued[stage] = 0;
+          uint8_t* sb = smem + stage * QT_STAGE;
+          mbar_expect_tx(&full[stage], A_TILE + nt * QT_BT);
+          tma_load_2d(sb, &tmA, kb * BK, (qp.s[p] - 1) * g.Ncap + m0, &full[stage]);
+          for (int q = 0; q < 4; q++)
+            if (qp.t[p][q] > 0)
+              tma_load_2d(sb + A_TILE + q * QT_BT, &tmD, kb * BK, (qp.t[p][q] - 1) * QT_TP, &full[stage]);
+          issued[stage] = 1;
+          issued_phase[stage] = phase;
+          if (++stage == STAGES) { stage = 0; phase ^= 1; }
+        }
+      }
+      if (!ok)
+        for (int s = 0; s < STAGES; s++)
+          if (issued[s]) mbar_drain(&full[s], issued_phase[s]);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      bool ok = true, any = false;
+      for (int p = 0; p < qp.n && ok; p++) {
+        const bool second = qp.t[p][2] > 0;
+        if (!mbar_wait(tempty, (p & 1) ^ 1, abort_flag, g.err, 12)) { ok = false; break; }
+        tc_fence_after();
+        for (int kb = 0; kb < nk; kb++) {
+          if (!mbar_wait(&full[stage], phase, abort_flag, g.err, 13)) { ok = false; break; }
+          tc_fence_after();
+          uint8_t* sb = smem + stage * QT_STAGE;
+          const uint64_t a = desc_sw128(sb), b01 = desc_sw128(sb + A_TILE), b23 = desc_sw128(sb + A_TILE + 2 * QT_BT);
+#pragma unroll
+          for (int k = 0; k < BK / 16; k++) {
+            const uint64_t koff = (uint64_t)((k * 32) >> 4);
+            const uint32_t acc = (kb > 0 || k > 0) ? 1u : 0u;
+            mma_bf16(tbase, a + koff, b01 + koff, QT_IDESC, acc);
+            if (second) mma_bf16(tbase + 224, a + koff, b23 + koff, QT_IDESC, acc);
+          }
+          any = true;
+          mma_commit(&empty[stage]);
+          if (++stage == STAGES) { stage = 0; phase ^= 1; }
+        }
+        if (!ok) break;
+        mma_commit(tfull);
+      }
+      if (!ok && any) {
+        mma_commit(drain);
+        mbar_drain(drain, 0);
+      }
+    }
+    __syncwarp();
+  } else {
+    // epilogue: warp w reads TMEM lane quarter w % 4 (SNP rows) and the
+    // trait half (w - 2) / 4 (56 traits)
+    const int q = warp & 3;
+    const int jh = ((warp - 2) >> 2) * 56;
+    const int i = m0 + q * 32 + lane;
+    float H[56], L[56];
+#pragma unroll
+    for (int c = 0; c < 56; c++) H[c] = L[c] = 0.0f;
+    bool done = true;
+    for (int p = 0; p < qp.n; p++) {
+      int ok = 1;
+      if (lane == 0) ok = mbar_wait(tfull, p & 1, abort_flag, g.err, 14) ? 1 : 0;
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) { done = false; break; }
+      tc_fence_after();
+#pragma unroll 1
+      for (int slot = 0; slot < 4; slot++) {
+        const int tt = qp.t[p][slot];
+        if (tt <= 0) continue;  // uniform across the CTA
+        const float w = __int_as_float((127 - 6 * (qp.s[p] + tt)) << 23);  // 64^-(s+t)
+        const uint32_t col = (uint32_t)((slot >> 1) * 224 + (slot & 1) * QT_TP + jh);
+        const uint32_t ta = tbase + ((uint32_t)(q * 32) << 16) + col;
+#pragma unroll
+        for (int c8 = 0; c8 < 7; c8++) {
+          uint32_t v[8];
+          tmem_ld8(ta + c8 * 8, v);
+          tmem_ld_wait();
+#pragma unroll
+          for (int u = 0; u < 8; u++) {
+            const float x = __fmul_rn(__uint_as_float(v[u]), w);  // exact: integer times a power of two
+            float s2, e;
+            two_sum_f(H[c8 * 8 + u], x, s2, e);
+            H[c8 * 8 + u] = s2;
+            L[c8 * 8 + u] = __fadd_rn(L[c8 * 8 + u], e);
+          }
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(tempty);
+    }
+    if (done && i < g.x) {
+      const double si = ldexp(1.0, g.aexp[i]);
+#pragma unroll
+      for (int c = 0; c < 56; c++) {
+        const int j = jh + c;
+        if (j < g.t) g.GR[i + (long long)j * g.ldg] = ((double)H[c] + (double)L[c]) * si * ldexp(1.0, g.dexp[j]);
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(512) : "memory");
+}
+
+// SNP digits: CTA per SNP column i of the R2 float pairs (rows l < n):
+// sigma_i = 2^aexp[i] >= 2 max_l R2, then S signed base-64 digits of R2 / sigma_i
+// at Ad[(s*Ncap + i)*Kpad + l].  Digits from the exact float-pair value:
+// d = rint(hi), (hi, lo) = TwoSum(hi - d, lo), times 64.
+__global__ void __launch_bounds__(256) snp_digits_kernel(int n, const float2* __restrict__ A, long long lda, int S,
+                                                         int Ncap, int Kpad, __nv_bfloat16* __restrict__ Ad,
+                                                         int* __restrict__ aexp) {
+  const int i = blockIdx.x;
+  const float2* a = A + (long long)i * lda;
+  __shared__ float red[32];
+  float m = 0.0f;
+  for (int l = threadIdx.x; l < n; l += blockDim.x) m = fmaxf(m, a[l].x);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    float v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (threadIdx.x == 0) red[0] = v;
+  }
+  __syncthreads();
+  m = red[0];
+    int e = 0;  // 2^e >= 2 m, so that R2 / sigma <= (1 + 2^-23) / 2 and every digit is <= 32
+  if (m > 0.0f) {
+    int ex;
+    frexpf(m, &ex);  // m = f 2^ex, f in [0.5, 1)
+    e = ex + 1;
+  }
+  if (threadIdx.x == 0) aexp[i] = e;
+  for (int l = threadIdx.x; l < n; l += blockDim.x) {
+    const float2 v = a[l];
+    float vh = ldexpf(v.x, 6 - e), vl = ldexpf(v.y, 6 - e);
+    for (int s = 0; s < S; s++) {
+      const float d = rintf(vh);
+      Ad[((long long)s * Ncap + i) * Kpad + l] = __float2bfloat16(d);  // |d| <= 32: exact
+      float hs, he;
+      two_sum_f(__fsub_rn(vh, d), vl, hs, he);
+      vh = hs * 64.0f;
+      vl = he * 64.0f;
+    }
+  }
+}
+
+// Trait digits: CTA per trait j of d (FP64, d[l + j*n]): tau_j = 2^dexp[j] >=
+// 2 max_l d, digits of d / tau_j in FP64 at Dd[(s*QT_TP + j)*Kpad + l].
+__global__ void __launch_bounds__(256) trait_digits_kernel(int n, const double* __restrict__ d, int S, int Kpad,
+                                                           __nv_bfloat16* __restrict__ Dd, int* __restrict__ dexp) {
+  const int j = blockIdx.x;
+  const double* c = d + (long long)j * n;
+  __shared__ double red[32];
+  double m = 0.0;
+  for (int l = threadIdx.x; l < n; l += blockDim.x) m = fmax(m, c[l]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (threadIdx.x == 0) red[0] = v;
+  }
+  __syncthreads();
+  m = red[0];
+  const int e = m > 0.0 ? ilogb(m) + 2 : 0;  // 2^e >= 2 m
+  if (threadIdx.x == 0) dexp[j] = e;
+  for (int l = threadIdx.x; l < n; l += blockDim.x) {
+    double v = ldexp(c[l], 6 - e);
+    for (int s = 0; s < S; s++) {
+      const double dd = rint(v);
+      Dd[((long long)s * QT_TP + j) * Kpad + l] = __double2bfloat16(dd);
+      v = (v - dd) * 64.0;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Slicing: row r of A (K-contiguous source, element k at src[k + r*lds]) ->
 // S digit slices (BF16) at A[(s*Mpad + r)*Kpad + k], scale per row.
 // ---------------------------------------------------------------------------
@@ -460,6 +765,10 @@ __global__ void __launch_bounds__(256) slice_rows_kernel(int K, int rows, const 
 }
 
 // genotypes (FP64 or bytes, column c at src[c*lds + k]) -> BF16 [c*Kpad + k]
+// Genotype value -> BF16 (exact for hard calls 0/1/2).
+__device__ __forceinline__ __nv_bfloat16 geno_bf16(unsigned char v) { return __float2bfloat16((float)v); }
+__device__ __forceinline__ __nv_bfloat16 geno_bf16(double v) { return __float2bfloat16((float)v); }
+
 template <typename T>
 __global__ void genotypes_bf16_kernel(int K, int cols, const T* __restrict__ src, long long lds,
                                       __nv_bfloat16* __restrict__ G, int Kpad) {
@@ -468,7 +777,7 @@ __global__ void genotypes_bf16_kernel(int K, int cols, const T* __restrict__ src
        e += (long long)gridDim.x * blockDim.x) {
     const int k = (int)(e % K);
     const long long c = e / K;
-    G[c * Kpad + k] = __float2bfloat16((float)src[c * lds + k]);
+    G[c * Kpad + k] = geno_bf16(src[c * lds + k]);
   }
 }
 
@@ -579,6 +888,14 @@ struct OzakiPlan {
   float* amax = nullptr;        // Ncap: per-SNP max_l of the high part of R^2
   float2* part = nullptr;       // quadratic Gram partial sums over row ranges
   int sms = 0;                  // SM count of the device
+  // tensor-core quadratic Gram (eigen, 33 <= t <= 112): digit operands
+  bool tq = false;
+  int SQ = 10;                    // digits per side; pairs with s + t <= SQ + 1
+  __nv_bfloat16* Adig = nullptr;  // SQ x Ncap x Kpad SNP digits
+  __nv_bfloat16* Ddig = nullptr;  // SQ x QT_TP x Kpad trait digits
+  int *aexp = nullptr, *dexp = nullptr;
+  CUtensorMap mapAd, mapDd;
+  QuadPasses qp;
   double* Linv = nullptr;       // chol: n x n, L^-1
   double* LinvT = nullptr;      // chol: n x n, (L^-1)^T (rows of L^-1 contiguous)
   int* err = nullptr;
@@ -634,6 +951,32 @@ cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_
   if (r == cudaSuccess) chk(cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                  SMEM_BYTES));
   p->sub = p->Ncap;  // one GEMM launch per block
+  {
+    const char* qe = getenv("FGLS_QUAD_TC");
+    p->tq = eigen && t >= 33 && t <= QT_TP && !(qe && qe[0] == '0');
+  }
+  if (p->tq && r == cudaSuccess) {
+    const size_t na = (size_t)p->SQ * p->Ncap * p->Kpad, nd = (size_t)p->SQ * QT_TP * p->Kpad;
+    chk(cudaMalloc(&p->Adig, sizeof(__nv_bfloat16) * na));
+    chk(cudaMalloc(&p->Ddig, sizeof(__nv_bfloat16) * nd));
+    chk(cudaMalloc(&p->aexp, sizeof(int) * p->Ncap));
+    chk(cudaMalloc(&p->dexp, sizeof(int) * QT_TP));
+    if (r == cudaSuccess) chk(cudaMemset(p->Adig, 0, sizeof(__nv_bfloat16) * na));
+    if (r == cudaSuccess) chk(cudaMemset(p->Ddig, 0, sizeof(__nv_bfloat16) * nd));
+    if (r == cudaSuccess) chk(cudaMemset(p->dexp, 0, sizeof(int) * QT_TP));
+    if (r == cudaSuccess) chk(make_map(&p->mapAd, p->Adig, p->Kpad, (long long)p->SQ * p->Ncap, BM));
+    if (r == cudaSuccess) chk(make_map(&p->mapDd, p->Ddig, p->Kpad, (long long)p->SQ * QT_TP, QT_TP));
+    if (r == cudaSuccess)
+      chk(cudaFuncSetAttribute(quadtc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, QT_SMEM));
+    // passes: one SNP digit s with up to four trait digits t, s + t <= SQ + 1
+    memset(&p->qp, 0, sizeof(p->qp));
+    for (int sd = 1; sd <= p->SQ; sd++)
+      for (int t0 = 1; t0 <= p->SQ + 1 - sd; t0 += 4) {
+        const int k = p->qp.n++;
+        p->qp.s[k] = (signed char)sd;
+        for (int q = 0; q < 4; q++) p->qp.t[k][q] = (signed char)(t0 + q <= p->SQ + 1 - sd ? t0 + q : 0);
+      }
+  }
   if (r != cudaSuccess) {
     ozaki_destroy(p);
     return r;
@@ -645,7 +988,8 @@ cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_
 
 void ozaki_destroy(OzakiPlan* p) {
   if (!p) return;
-  void* ptrs[] = {p->A, p->G, p->scale, p->C, p->U, p->D, p->dmax, p->amax, p->part, p->Linv, p->LinvT, p->err};
+  void* ptrs[] = {p->A,    p->G,     p->scale, p->C,     p->U,    p->D,    p->dmax, p->amax,
+                  p->part, p->Linv,  p->LinvT, p->err,   p->Adig, p->Ddig, p->aexp, p->dexp};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   delete p;
@@ -693,7 +1037,24 @@ cudaError_t load_genotypes(OzakiPlan* p, cudaStream_t s, const T* X, int x) {
 
 cudaError_t selfgram(OzakiPlan* p, cudaStream_t s, int col0, int xq, int t, double* GR, long long ldg) {
   const float2* A = (const float2*)(p->C + (long long)col0 * p->Mpad);
-  return quad_gram(s, p->n, xq, t, A, p->Mpad, p->amax + col0, p->D, p->n, p->dmax, p->part, GR + col0, ldg, p->sms);
+  if (!p->tq || col0 != 0)
+    return quad_gram(s, p->n, xq, t, A, p->Mpad, p->amax + col0, p->D, p->n, p->dmax, p->part, GR + col0, ldg,
+                     p->sms);
+  snp_digits_kernel<<<xq, 256, 0, s>>>(p->n, A, p->Mpad, p->SQ, p->Ncap, p->Kpad, p->Adig, p->aexp);
+  note_launch();
+  QuadArgs g;
+  g.x = xq;
+  g.t = t;
+  g.Ncap = p->Ncap;
+  g.Kpad = p->Kpad;
+  g.aexp = p->aexp;
+  g.dexp = p->dexp;
+  g.GR = GR;
+  g.ldg = ldg;
+  g.err = p->err;
+  quadtc_kernel<<<(xq + BM - 1) / BM, THREADS, QT_SMEM, s>>>(p->mapAd, p->mapDd, p->qp, g);
+  note_launch();
+  return cudaGetLastError();
 }
 
 }  // namespace
@@ -705,6 +1066,10 @@ cudaError_t ozaki_set_eigen(OzakiPlan* p, cudaStream_t s, const double* Z, const
   FGLS_CUDA_TRY(slice_operands(p, s, Z, p->n, p->n));
   split_pairs_kernel<<<p->t, 256, 0, s>>>(p->n, p->t, dinv, p->D, p->dmax);
   note_launch();
+  if (p->tq) {
+    trait_digits_kernel<<<p->t, 256, 0, s>>>(p->n, dinv, p->SQ, p->Kpad, p->Ddig, p->dexp);
+    note_launch();
+  }
   return cudaGetLastError();
 }
 
@@ -823,7 +1188,7 @@ __global__ void grouped_genotypes_kernel(const GenoCohort* __restrict__ gc, cons
        e += (long long)gridDim.x * blockDim.x) {
     const int k = (int)(e % n);
     const long long col = e / n;
-    G[col * Kpad + k] = __float2bfloat16((float)src[col * n + k]);
+    G[col * Kpad + k] = geno_bf16(src[col * n + k]);
   }
 }
 }  // namespace

@@ -292,8 +292,10 @@ __device__ __forceinline__ void solve_block(int x, int t, int wXL, const int j, 
   double* out = stage + threadIdx.x * (P + P * P);
   if (valid) {
     const double rs = T[wXL + wXL * wXL];
-    // potrf (lower, unblocked)
-    double L[P][P];
+    // potrf (lower, unblocked).  One division per column (ri = 1 / L_cc),
+    // multiplications elsewhere: FP64 division is a multi-instruction
+    // sequence on GB300's narrow FP64 pipe, which bounds this kernel.
+    double L[P][P], ri[P];
     int info = 0;
 #pragma unroll
     for (int c = 0; c < P; c++) {
@@ -303,12 +305,13 @@ __device__ __forceinline__ void solve_block(int x, int t, int wXL, const int j, 
       if (!(a > 0.0) && info == 0) info = c + 1;
       const double lcc = sqrt(a);
       L[c][c] = lcc;
+      ri[c] = 1.0 / lcc;
 #pragma unroll
       for (int r = c + 1; r < P; r++) {
         double v = S[r][c];
 #pragma unroll
         for (int q = 0; q < c; q++) v -= L[r][q] * L[c][q];
-        L[r][c] = v / lcc;
+        L[r][c] = v * ri[c];
       }
     }
     if (info) set_status(st, FGLSGPU_ENOTSPD, tag + info, snp_base + i);
@@ -319,26 +322,26 @@ __device__ __forceinline__ void solve_block(int x, int t, int wXL, const int j, 
       double v = b[r];
 #pragma unroll
       for (int q = 0; q < r; q++) v -= L[r][q] * z[q];
-      z[r] = v / L[r][r];
+      z[r] = v * ri[r];
     }
 #pragma unroll
     for (int r = P - 1; r >= 0; r--) {
       double v = z[r];
 #pragma unroll
       for (int q = r + 1; q < P; q++) v -= L[q][r] * z[q];
-      z[r] = v / L[r][r];
+      z[r] = v * ri[r];
     }
     // potri: Li = L^-1 (lower), Sinv = Li^T Li (lower part)
     double Li[P][P];
 #pragma unroll
     for (int c = 0; c < P; c++) {
-      Li[c][c] = 1.0 / L[c][c];
+      Li[c][c] = ri[c];
 #pragma unroll
       for (int r = c + 1; r < P; r++) {
         double v = 0.0;
 #pragma unroll
         for (int q = c; q < r; q++) v -= L[r][q] * Li[q][c];
-        Li[r][c] = v / L[r][r];
+        Li[r][c] = v * ri[r];
       }
     }
 #pragma unroll
