@@ -208,15 +208,35 @@ __device__ __forceinline__ int exact_f2i(float f) {
   return __float_as_int(__fadd_rn(f, 12582912.0f)) - 0x4B400000;
 }
 
-// Exact int64 value V times a power-of-two scale, squared, as a float pair:
-// v = V*scale = vh + vl (|vl| <= 2^-24 |vh|), v^2 ~= ah + al with
-// ah = fl(vh^2), al = (vh^2 - ah) + 2 vh vl; relative error ~2^-47.  No FP64
-// arithmetic: the conversions run on the integer / conversion units.
+// An integer |x| < 2^22 as a float, exactly, without a conversion
+// instruction (the inverse of exact_f2i).
+__device__ __forceinline__ float exact_i2f(int x) { return __fsub_rn(__int_as_float(x + 0x4B400000), 12582912.0f); }
+
+__device__ __forceinline__ void two_sum_g(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bp = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+}
+
+// Exact int64 value V (|V| < 2^62) times a power-of-two scale, squared, as a
+// float pair.  V = a 2^42 + b 2^21 + c with b, c in [0, 2^21) and |a| < 2^20:
+// each part converts exactly by exact_i2f, two TwoSums give V = hi + lo to
+// ~2^-48 (GB300 runs 64-bit integer <-> float conversions on its narrow FP64
+// pipe, which made this the slowest step of the epilogue).  Then
+// v = V*scale = vh + vl and v^2 ~= ah + al with ah = fl(vh^2),
+// al = (vh^2 - ah) + 2 vh vl: relative error ~2^-47.
 __device__ __forceinline__ float2 square_pair(long long V, float fscale) {
-  const float vh0 = __ll2float_rn(V);
-  const long long rem = V - __float2ll_rn(vh0);
-  const float vh = vh0 * fscale;
-  const float vl = __ll2float_rn(rem) * fscale;
+  const float fa = __fmul_rn(exact_i2f((int)(V >> 42)), 4398046511104.0f);        // a 2^42
+  const float fb = __fmul_rn(exact_i2f((int)((V >> 21) & 0x1FFFFF)), 2097152.0f);  // b 2^21
+  const float fc = exact_i2f((int)(V & 0x1FFFFF));
+  float s, e1, t, e2;
+  two_sum_g(fa, fb, s, e1);
+  two_sum_g(s, fc, t, e2);
+  const float lo0 = __fadd_rn(e1, e2);
+  const float hi = __fadd_rn(t, lo0);  // Fast2Sum renormalisation (|t| >= |lo0|)
+  const float lo = __fsub_rn(lo0, __fsub_rn(hi, t));
+  const float vh = hi * fscale;
+  const float vl = lo * fscale;
   const float ah = vh * vh;
   const float al = fmaf(vh, vh, -ah) + 2.0f * vh * vl;
   return make_float2(ah, al);
@@ -653,11 +673,20 @@ __global__ void __launch_bounds__(THREADS, 1)
 __global__ void __launch_bounds__(256) snp_digits_kernel(int n, const float2* __restrict__ A, long long lda, int S,
                                                          int Ncap, int Kpad, __nv_bfloat16* __restrict__ Ad,
                                                          int* __restrict__ aexp) {
+  // 4 consecutive rows per thread: two 16-byte loads, one 8-byte store per digit
   const int i = blockIdx.x;
-  const float2* a = A + (long long)i * lda;
+  const float4* a4 = (const float4*)(A + (long long)i * lda);  // lda even: 32-byte aligned groups of 4 pairs
+  const int n4 = (n + 3) >> 2;
   __shared__ float red[32];
   float m = 0.0f;
-  for (int l = threadIdx.x; l < n; l += blockDim.x) m = fmaxf(m, a[l].x);
+  for (int g = threadIdx.x; g < n4; g += blockDim.x) {
+    const float4 u = a4[2 * g], w = a4[2 * g + 1];  // pairs 4g .. 4g+3; rows >= n read C padding (ignored)
+    const int l = 4 * g;
+    if (l < n) m = fmaxf(m, u.x);
+    if (l + 1 < n) m = fmaxf(m, u.z);
+    if (l + 2 < n) m = fmaxf(m, w.x);
+    if (l + 3 < n) m = fmaxf(m, w.z);
+  }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
@@ -670,23 +699,41 @@ __global__ void __launch_bounds__(256) snp_digits_kernel(int n, const float2* __
   }
   __syncthreads();
   m = red[0];
-    int e = 0;  // 2^e >= 2 m, so that R2 / sigma <= (1 + 2^-23) / 2 and every digit is <= 32
+  int e = 0;  // 2^e >= 2 m, so that R2 / sigma <= (1 + 2^-23) / 2 and every digit is <= 32
   if (m > 0.0f) {
     int ex;
     frexpf(m, &ex);  // m = f 2^ex, f in [0.5, 1)
     e = ex + 1;
   }
   if (threadIdx.x == 0) aexp[i] = e;
-  for (int l = threadIdx.x; l < n; l += blockDim.x) {
-    const float2 v = a[l];
-    float vh = ldexpf(v.x, 6 - e), vl = ldexpf(v.y, 6 - e);
-    for (int s = 0; s < S; s++) {
-      const float d = rintf(vh);
-      Ad[((long long)s * Ncap + i) * Kpad + l] = __float2bfloat16(d);  // |d| <= 32: exact
-      float hs, he;
-      two_sum_f(__fsub_rn(vh, d), vl, hs, he);
-      vh = hs * 64.0f;
-      vl = he * 64.0f;
+  const int se = 6 - e;  // scale 2^se, a normal float for |se| <= 126
+  const float sc = (se >= -126 && se <= 127) ? __int_as_float((127 + se) << 23) : 0.0f;
+  const bool scale_ok = se >= -126 && se <= 127;
+  for (int g = threadIdx.x; g < n4; g += blockDim.x) {
+    const int l = 4 * g;
+    const float4 u = a4[2 * g], w = a4[2 * g + 1];
+    float vh[4] = {u.x, u.z, w.x, w.z}, vl[4] = {u.y, u.w, w.y, w.w};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      if (l + k >= n) vh[k] = vl[k] = 0.0f;
+      vh[k] = scale_ok ? vh[k] * sc : ldexpf(vh[k], se);
+      vl[k] = scale_ok ? vl[k] * sc : ldexpf(vl[k], se);
+    }
+    for (int sd = 0; sd < S; sd++) {
+      __nv_bfloat16 dg[4];
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const float d = rintf(vh[k]);
+        dg[k] = __float2bfloat16(d);  // |d| <= 32: exact
+        float hs, he;
+        two_sum_f(__fsub_rn(vh[k], d), vl[k], hs, he);
+        vh[k] = hs * 64.0f;
+        vl[k] = he * 64.0f;
+      }
+      uint2 pk;
+      pk.x = (uint32_t)__bfloat16_as_ushort(dg[0]) | ((uint32_t)__bfloat16_as_ushort(dg[1]) << 16);
+      pk.y = (uint32_t)__bfloat16_as_ushort(dg[2]) | ((uint32_t)__bfloat16_as_ushort(dg[3]) << 16);
+      *(uint2*)(Ad + ((long long)sd * Ncap + i) * Kpad + l) = pk;  // rows n..Kpad-1 receive zeros
     }
   }
 }
