@@ -11,9 +11,10 @@
 //  * merge: z = Q^T u / sqrt2, rho = 2|b| > 0; sort the children's eigenvalues
 //    (rank by binary search); deflate tiny |rho z_i| and close pairs (Givens,
 //    sequential scan in one thread); secular equation 1 + rho sum z^2/(d - l)
-//    for each surviving root by bisection in its own interval with the
-//    origin at the nearer pole (one thread per root); z recomputed from the
-//    roots by the Loewner formula so that the eigenvectors are orthogonal to
+//    for each surviving root by a pole-aware Newton iteration in its own
+//    bisection bracket with the origin at the nearer pole (one warp per root); z
+//    recomputed from the roots by the Loewner formula (one warp per root) so
+//    that the eigenvectors are orthogonal to
 //    working precision; eigenvectors u_k = z_i/(d_i - l_k) normalised (one
 //    warp per root); new Q = Q_old[:, kept] * U by DGEMM; final rank sort.
 #include <algorithm>
@@ -280,31 +281,65 @@ __global__ void dc_rotate_kernel(int n, int off, int nn, const int* __restrict__
   }
 }
 
-// f(tau) = 1 + rho sum z_j^2 / (delta_j - tau), delta_j = d_j - d_origin
-__device__ double secular(int K, const double* __restrict__ dk, const double* __restrict__ zk, double org,
-                          double rho, double tau) {
-  double s = 0.0;
-  for (int j = 0; j < K; j++) {
-    const double den = (dk[j] - org) - tau;
-    s += zk[j] * zk[j] / den;
+// Secular function at offset tau from the origin pole o, the K-term sums
+// split over the 32 lanes of a warp (every lane returns the full sums):
+//   f    = 1 + rho sum_j z_j^2 / (delta_j - tau)      (delta_j = d_j - d_o)
+//   amag = 1 + rho sum_j |z_j^2 / (delta_j - tau)|    (rounding scale of f)
+//   psi  = 1 + rho sum_{j != o} z_j^2 / (delta_j - tau),  dpsi = psi'
+__device__ __forceinline__ void secular_warp(int K, const double* __restrict__ dk, const double* __restrict__ zk,
+                                             int o, double rho, double tau, int lane, double& f, double& amag,
+                                             double& psi, double& dpsi) {
+  const double org = dk[o];
+  double s = 0.0, sa = 0.0, so = 0.0, sp = 0.0;
+  for (int j = lane; j < K; j += 32) {
+    const double r = 1.0 / ((dk[j] - org) - tau);
+    const double zr = zk[j] * r;
+    const double term = zk[j] * zr;
+    sa += fabs(term);
+    if (j == o) {
+      so += term;
+    } else {
+      s += term;
+      sp += zr * zr;
+    }
   }
-  return 1.0 + rho * s;
+  s = warp_sum(s);
+  sa = warp_sum(sa);
+  so = warp_sum(so);
+  sp = warp_sum(sp);
+  psi = 1.0 + rho * s;
+  dpsi = rho * sp;
+  f = psi + rho * so;
+  amag = 1.0 + rho * sa;
 }
 
-// One thread per root k: bisection in (d_k, d_k+1) (last: (d_K, d_K + rho |z|^2))
-// with the origin at the nearer pole.  Stores origin index and offset tau.
-__global__ void dc_secular_kernel(int K, const double* __restrict__ dk, const double* __restrict__ zk, double rho,
-                                  int* __restrict__ org_idx, double* __restrict__ tau_out) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= K) return;
+// One warp per root k in (d_k, d_k+1) (last: (d_K, d_K + rho |z|^2)), the
+// origin o at the nearer pole (the sign of f at the midpoint picks it).
+// Iteration on tau in a bisection bracket [lo, hi] that shrinks with the sign
+// of f at every iterate: each step keeps the origin's term -rho z_o^2 / tau
+// exact and linearises the rest (psi), i.e. solves
+//   psi(t) + psi'(t) (tau - t) - rho z_o^2 / tau = 0,
+// a quadratic whose root on the origin's side is taken in its stable form
+// (a pole-aware Newton step; LAPACK's dlaed4 uses refinements of the same
+// idea).  Steps outside the bracket fall back to bisection.  Stops when |f|
+// is below its rounding scale or the bracket is exhausted.  2-3 iterations
+// per root on kinship spectra instead of ~55 of bisection.
+__global__ void __launch_bounds__(256) dc_secular_kernel(int K, const double* __restrict__ dk,
+                                                         const double* __restrict__ zk, double rho,
+                                                         int* __restrict__ org_idx, double* __restrict__ tau_out) {
+  const int k = blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (k >= K) return;  // warp-uniform
   double zn = 0.0;
-  for (int j = 0; j < K; j++) zn += zk[j] * zk[j];
+  for (int j = lane; j < K; j += 32) zn += zk[j] * zk[j];
+  zn = warp_sum(zn);
   int o;
   double lo, hi;
+  double f, amag, psi, dpsi;
   if (k < K - 1) {
     const double gap = dk[k + 1] - dk[k];
-    const double fm = secular(K, dk, zk, dk[k], rho, 0.5 * gap);
-    if (fm >= 0.0) {
+    secular_warp(K, dk, zk, k, rho, 0.5 * gap, lane, f, amag, psi, dpsi);
+    if (f >= 0.0) {
       o = k;
       lo = 0.0;
       hi = 0.5 * gap;
@@ -318,37 +353,60 @@ __global__ void dc_secular_kernel(int K, const double* __restrict__ dk, const do
     lo = 0.0;
     hi = rho * zn;
     // f(hi) > 0 is guaranteed in exact arithmetic; widen if rounding disagrees
-    for (int w = 0; w < 8 && secular(K, dk, zk, dk[k], rho, hi) < 0.0; w++) hi *= 2.0;
+    for (int w = 0; w < 8; w++) {
+      secular_warp(K, dk, zk, k, rho, hi, lane, f, amag, psi, dpsi);
+      if (f >= 0.0) break;
+      hi *= 2.0;
+    }
   }
-  for (int it = 0; it < 200; it++) {
-    const double mid = 0.5 * (lo + hi);
-    if (mid <= lo || mid >= hi) break;
-    if (hi - lo <= 2.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi))) break;
-    const double f = secular(K, dk, zk, dk[o], rho, mid);
-    if (f < 0.0) lo = mid; else hi = mid;
-  }
+  const double c = rho * zk[o] * zk[o];
   double t = 0.5 * (lo + hi);
+  for (int it = 0; it < 200; it++) {
+    if (!(t > lo && t < hi)) t = 0.5 * (lo + hi);
+    if (t <= lo || t >= hi) break;  // bracket exhausted at working precision
+    secular_warp(K, dk, zk, o, rho, t, lane, f, amag, psi, dpsi);
+    if (fabs(f) <= 16.0 * DBL_EPSILON * amag) break;
+    if (f < 0.0) lo = t; else hi = t;
+    if (hi - lo <= 2.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi))) break;
+    const double a = dpsi, b = psi - dpsi * t;
+    const double sq = sqrt(b * b + 4.0 * a * c);
+    double tn;
+    if (o == k)  // root on the positive side of the origin
+      tn = b > 0.0 ? 2.0 * c / (b + sq) : (-b + sq) / (2.0 * a);
+    else
+      tn = b < 0.0 ? -2.0 * c / (-b + sq) : (-b - sq) / (2.0 * a);
+    t = (tn > lo && tn < hi && tn != t) ? tn : 0.5 * (lo + hi);
+  }
+  if (!(t > lo && t < hi)) t = 0.5 * (lo + hi);
   if (t == 0.0) t = (o == k) ? hi : lo;  // never exactly on the pole
-  org_idx[k] = o;
-  tau_out[k] = t;
+  if (lane == 0) {
+    org_idx[k] = o;
+    tau_out[k] = t;
+  }
 }
 
-// Loewner recomputation of z from the roots (one thread per i):
+// Loewner recomputation of z from the roots (one warp per i, the product
+// split over the lanes):
 //   z_i^2 = (l_i - d_i)/rho * prod_{j != i} (l_j - d_i)/(d_j - d_i)
-__global__ void dc_lowner_kernel(int K, const double* __restrict__ dk, const double* __restrict__ zk,
-                                 const int* __restrict__ org_idx, const double* __restrict__ tau, double rho,
-                                 double* __restrict__ zh) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(256) dc_lowner_kernel(int K, const double* __restrict__ dk,
+                                                        const double* __restrict__ zk,
+                                                        const int* __restrict__ org_idx, const double* __restrict__ tau,
+                                                        double rho, double* __restrict__ zh) {
+  const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
   if (i >= K) return;
   const double di = dk[i];
-  double prod = ((dk[org_idx[i]] - di) + tau[i]) / rho;
-  for (int j = 0; j < K; j++) {
+  double prod = 1.0;
+  for (int j = lane; j < K; j += 32) {
     if (j == i) continue;
     const double num = (dk[org_idx[j]] - di) + tau[j];
     const double den = dk[j] - di;
     prod *= num / den;
   }
-  zh[i] = copysign(sqrt(fmax(prod, 0.0)), zk[i]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) prod *= __shfl_xor_sync(0xffffffffu, prod, o);
+  prod *= ((dk[org_idx[i]] - di) + tau[i]) / rho;
+  if (lane == 0) zh[i] = copysign(sqrt(fmax(prod, 0.0)), zk[i]);
 }
 
 // U[:, k] = (z_i / (d_i - l_k))_i normalised; one warp per root k.
@@ -547,8 +605,8 @@ cudaError_t dc_tridiag_eig(cudaStream_t s, int n, double* d, double* e, double* 
       nl++;
     }
     if (K > 0) {
-      dc_secular_kernel<<<ceil_div(K, 64), 64, 0, s>>>(K, dk, zk, rho, orgi, tau);
-      dc_lowner_kernel<<<ceil_div(K, 64), 64, 0, s>>>(K, dk, zk, orgi, tau, rho, zh);
+      dc_secular_kernel<<<ceil_div(K, 8), 256, 0, s>>>(K, dk, zk, rho, orgi, tau);
+      dc_lowner_kernel<<<ceil_div(K, 8), 256, 0, s>>>(K, dk, zk, orgi, tau, rho, zh);
       dc_vectors_kernel<<<ceil_div(K, 8), 256, 0, s>>>(K, dk, zh, orgi, tau, U);
       dc_gather_kernel<<<grid_for((long long)nn * K), 256, 0, s>>>(n, off, nn, K, colk, V, G);
       nl += 4;

@@ -294,8 +294,12 @@ cudaError_t dsyev_device(cudaStream_t s, int n, const double* Phi, long long ldp
   mark(1);
   mark(2);  // (no explicit Q: the reflectors are applied to the eigenvectors below)
   // 3. eigenpairs of T by divide and conquer (fgls_dc.cu) into Z; A keeps the reflectors
+  // one workspace for the divide and conquer, then for the back-transform
+  // (Y: n x NBT, G, T: NBT x NBT, W, W2: NBT x n)
+  constexpr int NBT = 256;
+  const size_t bt_bytes = sizeof(double) * ((size_t)3 * NBT * n + (size_t)2 * NBT * NBT);
   void* dcw = nullptr;
-  FGLS_CUDA_TRY(cudaMalloc(&dcw, dc_workspace_bytes(n)));
+  FGLS_CUDA_TRY(cudaMalloc(&dcw, std::max(dc_workspace_bytes(n), bt_bytes)));
   int* dfail = rank;  // n ints of scratch; first used as the failure flag
   FGLS_CUDA_TRY(cudaMemsetAsync(dfail, 0, sizeof(int), s));
   cudaError_t rc = dc_tridiag_eig(s, n, d, e, W, Z, dcw, dfail, &nl);
@@ -304,7 +308,7 @@ cudaError_t dsyev_device(cudaStream_t s, int n, const double* Phi, long long ldp
   //    in compact-WY form (I - Y T Y^T): three DGEMMs per block, 2 n^3 flops
   //    in all -- what a DGEMM with an explicit Q costs, without forming Q.
   {
-    constexpr int NB = 256;  // wide blocks: the Y^T Z product has NB/64 x n/64 output tiles
+    constexpr int NB = NBT;  // wide blocks: the Y^T Z product has NB/64 x n/64 output tiles
     double* Yb = (double*)dcw;         // n x NB
     double* G = Yb + (size_t)n * NB;   // NB x NB
     double* Tm = G + (size_t)NB * NB;  // NB x NB
