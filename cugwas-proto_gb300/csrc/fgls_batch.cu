@@ -146,7 +146,7 @@ __global__ void probe_genotypes_kernel(int c, int n, int x, unsigned char* out, 
     h *= 2246822519u;
     h ^= h >> 13;
     const unsigned char g = (unsigned char)(h % 3u);
-    out[e] = g;
+    if (out) out[e] = g;
     if (out64) out64[e] = (double)g;
   }
 }
@@ -407,37 +407,59 @@ int time_step(fglsgpu_batch* b, int x_b, double* rate) {
 struct Scratch {
   double *L = nullptr, *Linv = nullptr, *LinvT = nullptr, *WY = nullptr, *U = nullptr;
   double *X64 = nullptr, *GYL = nullptr, *GR64 = nullptr, *Vp = nullptr;
-  double *Phi = nullptr, *XL = nullptr, *Y = nullptr;
+  DevStatus* st = nullptr;
+  cudaStream_t s = nullptr;
+  cudaError_t alloc(int nmax, int wmax) {
+    const size_t nn = (size_t)nmax * nmax;
+    cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    for (double** v : {&L, &Linv, &LinvT})
+      if (e == cudaSuccess) e = dalloc(v, nn);
+    if (e == cudaSuccess) e = dalloc(&WY, (size_t)nmax * (1 + wmax));
+    if (e == cudaSuccess) e = dalloc(&U, (size_t)nmax * (1 + wmax));
+    if (e == cudaSuccess) e = dalloc(&X64, (size_t)nmax * PROBE);
+    if (e == cudaSuccess) e = dalloc(&GYL, (size_t)PROBE * (1 + wmax));
+    if (e == cudaSuccess) e = dalloc(&GR64, (size_t)PROBE);
+    if (e == cudaSuccess) e = dalloc(&Vp, (size_t)PROBE * FGLS_MAX_P * FGLS_MAX_P);
+    if (e == cudaSuccess) e = dalloc(&st, 1);
+    if (e == cudaSuccess) e = cudaMemset(st, 0, sizeof(DevStatus));
+    return e;
+  }
   void release() {
-    void* ptrs[] = {L, Linv, LinvT, WY, U, X64, GYL, GR64, Vp, Phi, XL, Y};
+    void* ptrs[] = {L, Linv, LinvT, WY, U, X64, GYL, GR64, Vp, st};
     for (void* v : ptrs)
       if (v) cudaFree(v);
+    if (s) cudaStreamDestroy(s);
   }
 };
 
-int setup_problem(fglsgpu_batch* b, Scratch& w, Problem& q, const fglsgpu_cohort& in) {
+// Cohort inputs shared by its traits' setup streams.
+struct CohortInputs {
+  double *Phi = nullptr, *XL = nullptr, *Y = nullptr;
+};
+
+// Enqueues the whole one-off setup of problem q on w.s (no host waits): M,
+// potrf, whitening, null model, split operand, FP64-path probe betas.  Data
+// failures land in w.st and are read after the cohort.
+cudaError_t setup_problem(fglsgpu_batch* b, Scratch& w, const CohortInputs& ci, Problem& q,
+                          const fglsgpu_cohort& in) {
   const Cohort& c = b->co[q.c];
   const int n = c.n, wXL = c.wXL, p = c.p;
-  cudaStream_t s = b->s;
+  cudaStream_t s = w.s;
   const double h = in.h[q.j], sg = in.sigma[q.j];
-  B_TRY(b, build_shifted(s, n, w.Phi, n, h * sg, (1.0 - h) * sg, w.L, n), "build M");
-  B_TRY(b, dpotrf_lower(s, n, w.L, n, b->dst), "potrf");
-  B_TRY(b, cudaMemcpyAsync(w.WY, w.Y + (size_t)q.j * n, sizeof(double) * n, cudaMemcpyDeviceToDevice, s), "copy y");
-  B_TRY(b, cudaMemcpyAsync(w.WY + n, w.XL, sizeof(double) * n * wXL, cudaMemcpyDeviceToDevice, s), "copy XL");
-  int rc = check_status(b, "potrf(M)");
-  if (rc) return bfail(b, FGLSGPU_ENOTSPD, "dpotrf(M) failed - cohort %d, trait %d", q.c, q.j);
-  B_TRY(b, dtrsm_llnn(s, n, 1 + wXL, w.L, n, w.WY, n), "whiten y, XL");
-  B_TRY(b, null_model_chol(s, n, wXL, w.WY, q.top, b->dst, 0), "null model");
-  rc = check_status(b, "null model");
-  if (rc) return rc;
-  B_TRY(b, split_chol_operand(s, n, wXL, w.L, w.WY, S_BUILT, q.Mpad, c.Kpad, q.A, q.scale6, w.Linv, w.LinvT, w.U),
-        "split operand");
+  probe_genotypes_kernel<<<256, 256, 0, s>>>(q.c, n, PROBE, q.j == 0 ? b->co[q.c].probe : nullptr, w.X64);
+  FGLS_CUDA_TRY(build_shifted(s, n, ci.Phi, n, h * sg, (1.0 - h) * sg, w.L, n));
+  FGLS_CUDA_TRY(dpotrf_lower(s, n, w.L, n, w.st));
+  FGLS_CUDA_TRY(cudaMemcpyAsync(w.WY, ci.Y + (size_t)q.j * n, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  FGLS_CUDA_TRY(cudaMemcpyAsync(w.WY + n, ci.XL, sizeof(double) * n * wXL, cudaMemcpyDeviceToDevice, s));
+  FGLS_CUDA_TRY(dtrsm_llnn(s, n, 1 + wXL, w.L, n, w.WY, n));
+  FGLS_CUDA_TRY(null_model_chol(s, n, wXL, w.WY, q.top, w.st, 0));
+  FGLS_CUDA_TRY(split_chol_operand(s, n, wXL, w.L, w.WY, S_BUILT, q.Mpad, c.Kpad, q.A, q.scale6, w.Linv, w.LinvT,
+                                   w.U));
   // FP64 path on the probe block (the reference's chol per-block loop)
-  B_TRY(b, dtrsm_llnn(s, n, PROBE, w.L, n, w.X64, n), "probe TRSM");
-  B_TRY(b, gram_skinny(s, n, PROBE, wXL, 1, w.X64, n, w.WY, w.GYL, w.GR64), "probe Gram");
-  B_TRY(b, snp_solve(s, p, PROBE, 1, wXL, q.top, w.GYL, 1, PROBE, w.GR64, PROBE, q.ref, 0, w.Vp, 0, b->dst, 0),
-        "probe solve");
-  return check_status(b, "probe solve");
+  FGLS_CUDA_TRY(dtrsm_llnn(s, n, PROBE, w.L, n, w.X64, n));
+  FGLS_CUDA_TRY(gram_skinny(s, n, PROBE, wXL, 1, w.X64, n, w.WY, w.GYL, w.GR64));
+  FGLS_CUDA_TRY(snp_solve(s, p, PROBE, 1, wXL, q.top, w.GYL, 1, PROBE, w.GR64, PROBE, q.ref, 0, w.Vp, 0, w.st, 0));
+  return cudaGetLastError();
 }
 
 }  // namespace
@@ -523,50 +545,72 @@ int fglsgpu_batch_create(const fglsgpu_cohort* cohorts, int count, const fglsgpu
     B_CHECK(dalloc(&q.GR, b->ncap), "Gram");
     B_CHECK(dalloc(&q.ref, (size_t)PROBE * k.p), "probe reference");
   }
-  // one-off FP64 setup of every problem
+  // one-off FP64 setup of every problem: the traits of a cohort run
+  // concurrently on NS streams, each with its own scratch and status word
   {
-    Scratch w;
+    constexpr int NS = 4;
+    Scratch w[NS];
+    CohortInputs ci;
+    auto release = [&]() {
+      for (auto& x : w) x.release();
+      for (double* v : {ci.Phi, ci.XL, ci.Y})
+        if (v) cudaFree(v);
+    };
     auto fail_scratch = [&](cudaError_t e, const char* what) {
-      w.release();
+      release();
       return bail(bfail(nullptr, e == cudaErrorMemoryAllocation ? FGLSGPU_ENOMEM : FGLSGPU_ECUDA, "%s: %s", what,
                         cudaGetErrorString(e)));
     };
-    const size_t nn = (size_t)nmax * nmax;
-    cudaError_t e = cudaSuccess;
-    for (double** v : {&w.L, &w.Linv, &w.LinvT, &w.Phi})
-      if (e == cudaSuccess) e = dalloc(v, nn);
-    if (e == cudaSuccess) e = dalloc(&w.WY, (size_t)nmax * (1 + wmax));
-    if (e == cudaSuccess) e = dalloc(&w.U, (size_t)nmax * (1 + wmax));
-    if (e == cudaSuccess) e = dalloc(&w.X64, (size_t)nmax * PROBE);
-    if (e == cudaSuccess) e = dalloc(&w.GYL, (size_t)PROBE * (1 + wmax));
-    if (e == cudaSuccess) e = dalloc(&w.GR64, (size_t)PROBE);
-    if (e == cudaSuccess) e = dalloc(&w.Vp, (size_t)PROBE * FGLS_MAX_P * FGLS_MAX_P);
-    if (e == cudaSuccess) e = dalloc(&w.XL, (size_t)nmax * wmax);
-    if (e != cudaSuccess) return fail_scratch(e, "setup scratch");
+    int tmax = 1;
     size_t ymax = 0;
-    for (int c = 0; c < count; c++) ymax = std::max(ymax, (size_t)cohorts[c].n * cohorts[c].t);
-    if ((e = dalloc(&w.Y, ymax)) != cudaSuccess) return fail_scratch(e, "setup scratch");
-    size_t k = 0;
     for (int c = 0; c < count; c++) {
+      tmax = std::max(tmax, cohorts[c].t);
+      ymax = std::max(ymax, (size_t)cohorts[c].n * cohorts[c].t);
+    }
+    const int ns = std::min(NS, tmax);
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < ns && e == cudaSuccess; k++) e = w[k].alloc(nmax, wmax);
+    if (e == cudaSuccess) e = dalloc(&ci.Phi, (size_t)nmax * nmax);
+    if (e == cudaSuccess) e = dalloc(&ci.XL, (size_t)nmax * wmax);
+    if (e == cudaSuccess) e = dalloc(&ci.Y, ymax);
+    if (e != cudaSuccess) return fail_scratch(e, "setup scratch");
+    cudaEvent_t up = nullptr;
+    if ((e = cudaEventCreateWithFlags(&up, cudaEventDisableTiming)) != cudaSuccess)
+      return fail_scratch(e, "setup events");
+    size_t k = 0;
+    for (int c = 0; c < count && e == cudaSuccess; c++) {
       const fglsgpu_cohort& in = cohorts[c];
       const int n = in.n;
-      e = cudaMemcpyAsync(w.Phi, in.Phi, sizeof(double) * n * n, cudaMemcpyHostToDevice, b->s);
+      e = cudaMemcpyAsync(ci.Phi, in.Phi, sizeof(double) * n * n, cudaMemcpyHostToDevice, b->s);
       if (e == cudaSuccess)
-        e = cudaMemcpyAsync(w.XL, in.XL, sizeof(double) * n * in.wXL, cudaMemcpyHostToDevice, b->s);
-      if (e == cudaSuccess) e = cudaMemcpyAsync(w.Y, in.Y, sizeof(double) * n * in.t, cudaMemcpyHostToDevice, b->s);
-      if (e != cudaSuccess) return fail_scratch(e, "upload cohort");
-      for (; k < b->pr.size() && b->pr[k].c == c; k++) {
-        probe_genotypes_kernel<<<256, 256, 0, b->s>>>(c, n, PROBE, b->co[c].probe, w.X64);
-        rc = setup_problem(b, w, b->pr[k], in);
-        if (rc) {
-          tl_err = b->err;
-          w.release();
-          return bail(rc);
+        e = cudaMemcpyAsync(ci.XL, in.XL, sizeof(double) * n * in.wXL, cudaMemcpyHostToDevice, b->s);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(ci.Y, in.Y, sizeof(double) * n * in.t, cudaMemcpyHostToDevice, b->s);
+      if (e == cudaSuccess) e = cudaEventRecord(up, b->s);
+      const size_t k0 = k;
+      for (; e == cudaSuccess && k < b->pr.size() && b->pr[k].c == c; k++) {
+        Scratch& x = w[(k - k0) % ns];
+        e = cudaStreamWaitEvent(x.s, up, 0);
+        if (e == cudaSuccess) e = setup_problem(b, x, ci, b->pr[k], in);
+      }
+      // the next cohort's upload overwrites the inputs: wait for all traits,
+      // then read the status words
+      for (int q = 0; q < ns && e == cudaSuccess; q++) e = cudaStreamSynchronize(w[q].s);
+      for (int q = 0; q < ns && e == cudaSuccess; q++) {
+        DevStatus hs{};
+        e = cudaMemcpy(&hs, w[q].st, sizeof(DevStatus), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess && hs.code != FGLSGPU_OK) {
+          cudaEventDestroy(up);
+          release();
+          return bail(bfail(nullptr, hs.code == FGLSGPU_ENOTSPD ? FGLSGPU_ENOTSPD : hs.code,
+                            "cohort %d: a trait's M or null model is not positive definite (info %d, item %lld)",
+                            c, hs.info, hs.idx));
         }
       }
     }
-    if ((e = cudaStreamSynchronize(b->s)) != cudaSuccess) return fail_scratch(e, "setup");
-    w.release();
+    cudaEventDestroy(up);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->s);
+    if (e != cudaSuccess) return fail_scratch(e, "setup");
+    release();
   }
   // device tables
   {
