@@ -608,7 +608,7 @@ def main():
     ap.add_argument("--xb", type=int, default=16384)
     ap.add_argument("--slices", type=int, default=6)
     ap.add_argument("--pool", type=int, default=4)
-    ap.add_argument("--e2e-blocks", type=int, default=4)
+    ap.add_argument("--e2e-blocks", type=int, default=8)
     ap.add_argument("--fp64-snps", type=int, default=2048)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-snps", type=int, default=128)

@@ -459,7 +459,8 @@ __global__ void __launch_bounds__(THREADS, 1)
 // with sigma_i, tau_j powers of two such that a, b <= 1/2.  A digit product
 // is at most 2^10, so a K-sum over K <= 16384 rows is an integer of at most
 // 2^24: exact in the FP32 TMEM accumulator.  Pairs with s + t <= L are kept
-// (L = 11: dropped terms below 2^-60 of sigma_i tau_j per row).  The epilogue
+// (L = 10, 9 digits a side: the dropped pairs and the digit remainders stay
+// below 2^-52 of sigma_i tau_j per row).  The epilogue
 // scales each exact pair sum by 64^-(s+t) (exact) and accumulates it in a
 // float pair by TwoSum (relative error ~2^-47), then multiplies by
 // sigma_i tau_j in FP64.
@@ -937,7 +938,7 @@ struct OzakiPlan {
   int sms = 0;                  // SM count of the device
   // tensor-core quadratic Gram (eigen, 33 <= t <= 112): digit operands
   bool tq = false;
-  int SQ = 10;                    // digits per side; pairs with s + t <= SQ + 1
+  int SQ = 9;                     // digits per side; pairs with s + t <= SQ + 1
   __nv_bfloat16* Adig = nullptr;  // SQ x Ncap x Kpad SNP digits
   __nv_bfloat16* Ddig = nullptr;  // SQ x QT_TP x Kpad trait digits
   int *aexp = nullptr, *dexp = nullptr;
