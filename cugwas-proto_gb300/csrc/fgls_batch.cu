@@ -31,7 +31,9 @@
 #include <string.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -494,6 +496,13 @@ int fglsgpu_batch_create(const fglsgpu_cohort* cohorts, int count, const fglsgpu
     return rc;
   };
   int rc = 0;
+  // FGLS_BATCH_TIMING=1 prints the wall time of the setup phases to stderr
+  const bool timing = getenv("FGLS_BATCH_TIMING") && atoi(getenv("FGLS_BATCH_TIMING")) != 0;
+  auto now = [] { return std::chrono::steady_clock::now(); };
+  auto secs = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point z) {
+    return std::chrono::duration<double>(z - a).count();
+  };
+  const auto t_start = now();
 #define B_CHECK(expr, what)                                                                                  \
   do {                                                                                                       \
     cudaError_t _c = (expr);                                                                                 \
@@ -649,6 +658,7 @@ int fglsgpu_batch_create(const fglsgpu_cohort* cohorts, int count, const fglsgpu
     }
   }
   // autotuning
+  const auto t_setup = now();
   int S = cfg->slices;
   if (S == 0) {
     S = S_BUILT;
@@ -668,6 +678,7 @@ int fglsgpu_batch_create(const fglsgpu_cohort* cohorts, int count, const fglsgpu
     }
   }
   b->S = S;
+  const auto t_probe = now();
   int xb = cfg->x_b;
   if (xb == 0) {
     double best = -1.0;
@@ -689,6 +700,12 @@ int fglsgpu_batch_create(const fglsgpu_cohort* cohorts, int count, const fglsgpu
   if (rc) {
     tl_err = b->err;
     return bail(rc);
+  }
+  if (timing) {
+    cudaDeviceSynchronize();
+    const auto t_end = now();
+    fprintf(stderr, "[fgls batch] factorisations + operands %.2f s, slice probe %.2f s, block timing %.2f s\n",
+            secs(t_start, t_setup), secs(t_setup, t_probe), secs(t_probe, t_end));
   }
 #undef B_CHECK
   *out = b;

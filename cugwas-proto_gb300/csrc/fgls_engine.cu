@@ -748,6 +748,83 @@ int fglsgpu_reml(fglsgpu_engine* e, double* loglik, double* dloglik_dh) {
   return FGLSGPU_OK;
 }
 
+int fglsgpu_reml_fit(fglsgpu_engine* e, double h_lo, double h_hi, int grid, double* h, double* sigma,
+                     double* loglik, double* dloglik_dh) {
+  if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
+  if (!e->problem_set) return fail(e, FGLSGPU_ESTATE, "set_problem must precede reml_fit");
+  const fglsgpu_config& c = e->cfg;
+  if (c.variant != FGLSGPU_VARIANT_EIGEN) return fail(e, FGLSGPU_EINVAL, "reml_fit needs the eigen variant");
+  if (grid == 0) grid = 64;
+  if (!(h_lo >= 0.0 && h_lo < h_hi && h_hi <= 1.0))
+    return fail(e, FGLSGPU_EINVAL, "need 0 <= h_lo < h_hi <= 1 (h_lo=%g h_hi=%g)", h_lo, h_hi);
+  if (grid < 2 || grid > FGLS_REML_MAX_GRID) return fail(e, FGLSGPU_EINVAL, "grid=%d outside [2, %d]", grid, FGLS_REML_MAX_GRID);
+  if (c.n <= c.wXL) return fail(e, FGLSGPU_EINVAL, "n=%d must exceed wXL=%d", c.n, c.wXL);
+  ENG_TRY(e, cudaSetDevice(c.device), "cudaSetDevice");
+  const int t = c.t;
+  int rc = reset_status(e);
+  if (rc) return rc;
+  double* dout = nullptr;
+  ENG_TRY(e, dalloc(&dout, 4 * (size_t)t), "reml_fit output");
+  std::vector<double> r(4 * (size_t)t);
+  cudaError_t ce = reml_fit(e->comp, c.n, t, c.wXL, e->dW, e->dZtXL, e->dZtY, h_lo, h_hi, grid, dout, e->dst);
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(r.data(), dout, sizeof(double) * 4 * t, cudaMemcpyDeviceToHost, e->comp);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->comp);
+  cudaFree(dout);
+  if (ce != cudaSuccess) return cuda_fail(e, ce, "reml_fit");
+  ENG_TRY(e, cudaMemcpy(e->hst, e->dst, sizeof(DevStatus), cudaMemcpyDeviceToHost), "status copy");
+  const DevStatus st = *e->hst;
+  if (st.code != FGLSGPU_OK) {
+    reset_status(e);
+    return fail(e, st.code, "reml_fit: trait %lld: the covariate Gram is not positive definite or "
+                "1 + h (w - 1) <= 0 inside [%g, %g]", st.idx, h_lo, h_hi);
+  }
+  for (int j = 0; j < t; j++) {
+    if (h) h[j] = r[j];
+    if (sigma) sigma[j] = r[t + j];
+    if (loglik) loglik[j] = r[2 * t + j];
+    if (dloglik_dh) dloglik_dh[j] = r[3 * t + j];
+  }
+  return FGLSGPU_OK;
+}
+
+int fglsgpu_set_hsigma(fglsgpu_engine* e, const double* h, const double* sigma) {
+  if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
+  if (!e->problem_set) return fail(e, FGLSGPU_ESTATE, "set_problem must precede set_hsigma");
+  if (!h || !sigma) return fail(e, FGLSGPU_EINVAL, "null input pointer");
+  const fglsgpu_config& c = e->cfg;
+  for (int j = 0; j < c.t; j++)
+    if (!(h[j] >= 0.0 && h[j] <= 1.0) || !(sigma[j] > 0.0))
+      return fail(e, FGLSGPU_EINVAL, "trait %d: need 0 <= h <= 1 and sigma > 0 (h=%g sigma=%g)", j, h[j], sigma[j]);
+  ENG_TRY(e, cudaSetDevice(c.device), "cudaSetDevice");
+  cudaStream_t s = e->comp;
+  ENG_TRY(e, cudaStreamSynchronize(s), "set_hsigma");
+  e->hh.assign(h, h + c.t);
+  e->hs.assign(sigma, sigma + c.t);
+  e->adj_ready = false;
+  ENG_TRY(e, cudaMemcpyAsync(e->dh, h, sizeof(double) * c.t, cudaMemcpyHostToDevice, s), "upload h");
+  ENG_TRY(e, cudaMemcpyAsync(e->dsig, sigma, sizeof(double) * c.t, cudaMemcpyHostToDevice, s), "upload sigma");
+  if (c.variant != FGLSGPU_VARIANT_EIGEN) {
+    e->trait_sel = -1;  // the next select_trait builds and factors M_j with the new values
+    ENG_TRY(e, cudaStreamSynchronize(s), "set_hsigma");
+    return FGLSGPU_OK;
+  }
+  int rc = reset_status(e);
+  if (rc) return rc;
+  e->problem_set = false;
+  ENG_TRY(e, eigen_traits(s, c.n, c.t, c.wXL, e->dW, e->dh, e->dsig, e->dZtXL, e->dZtY, e->ddinv, e->dAYL,
+                          e->dtop, e->dst),
+          "trait weights");
+  rc = check_status(e, "eigen setup");
+  if (rc) return rc;
+  if (split(e)) {
+    if (!e->oz) ENG_TRY(e, ozaki_create(&e->oz, c.n, c.t, c.wXL, c.wXR, c.x_b, c.slices, 1), "split plan");
+    ENG_TRY(e, ozaki_set_eigen(e->oz, s, e->dZ, e->dAYL, e->ddinv), "split operands");
+  }
+  ENG_TRY(e, cudaStreamSynchronize(s), "set_hsigma");
+  e->problem_set = true;
+  return FGLSGPU_OK;
+}
+
 int fglsgpu_profile(fglsgpu_engine* e, int enable) {
   if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
   ENG_TRY(e, cudaSetDevice(e->cfg.device), "cudaSetDevice");

@@ -85,6 +85,13 @@ cudaError_t adjoint_reduce(cudaStream_t s, int x, int t, int p, int wXL, const d
 cudaError_t adjoint_ybar(cudaStream_t s, int n, int t, int wXL, const double* dinv, const double* ZtXL,
                          const double* acc, const double* U, double* V2);
 
+// Null-model REML fit per trait over h in [lo, hi] (grid of `grid` points,
+// 2 <= grid <= FGLS_REML_MAX_GRID, then root refinement of the h-gradient).
+// out (4 x t): h, sigma_hat, profiled log-likelihood, its h-gradient there.
+#define FGLS_REML_MAX_GRID 256
+cudaError_t reml_fit(cudaStream_t s, int n, int t, int wXL, const double* W, const double* ZtXL, const double* ZtY,
+                     double lo, double hi, int grid, double* out, DevStatus* st);
+
 // Genotype conversion: FP64 or u8 hard calls -> FP64 (device to device).
 cudaError_t u8_to_f64(cudaStream_t s, const unsigned char* in, double* out, long long count);
 

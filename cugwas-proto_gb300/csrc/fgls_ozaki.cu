@@ -56,9 +56,35 @@ namespace oz {
 constexpr int BM = 128, BN = 256, BK = 64;
 constexpr int STAGES = 3;
 constexpr int A_TILE = BM * BK * 2;               // 16 KB
-constexpr int B_TILE = BN * BK * 2;               // 32 KB
-constexpr int STAGE_BYTES = 2 * A_TILE + B_TILE;  // 64 KB
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+// split GEMM ring for a K-step KB (32: 64-byte rows, 64B swizzle, 6 stages of
+// 32 KB; 64: 128-byte rows, 128B swizzle, 3 stages of 64 KB).  The smaller
+// stages keep more bytes in flight per SM for the same shared memory (the MMA
+// thread waits on stage arrivals, not on L2 bandwidth): 10.72 against
+// 11.20 ms per launch at n = 10000, x_b = 16384.  The grouped launch, whose
+// small cohorts have short K, stays at KB = 64 (32.3 against 32.8 ms per
+// step of the 64-cohort batch).
+#ifndef FGLS_GEMM_BK
+#define FGLS_GEMM_BK 32
+#endif
+#ifndef FGLS_GROUPED_BK
+#define FGLS_GROUPED_BK 64
+#endif
+#ifndef FGLS_GEMM_STAGES32
+#define FGLS_GEMM_STAGES32 6
+#endif
+template <int KB>
+struct GemmRing {
+  static_assert(KB == 64 || KB == 32, "K-step of the split GEMM");
+  static constexpr int STAGES = KB == 64 ? 3 : FGLS_GEMM_STAGES32;
+  static constexpr int A = BM * KB * 2;
+  static constexpr int B = BN * KB * 2;
+  static constexpr int STAGE = 2 * A + B;
+  static constexpr int SMEM = STAGES * STAGE + 1024 + 256;
+};
+constexpr int GBK = FGLS_GEMM_BK;         // single-problem launch
+constexpr int GRBK = FGLS_GROUPED_BK;     // grouped launch
+constexpr int SMEM_BYTES = GemmRing<GBK>::SMEM;
+constexpr int GROUPED_SMEM_BYTES = GemmRing<GRBK>::SMEM;
 constexpr int THREADS = 320;  // producer, MMA, 8 epilogue warps
 constexpr int MAX_SLICES = 6;
 constexpr int GROUP_M = 8;
@@ -145,6 +171,20 @@ __device__ __forceinline__ uint64_t desc_sw128(const void* p) {
   d |= (uint64_t)2 << 61;                // 128B swizzle
   return d;
 }
+
+// K-major operand rows of 64 bytes with 64-byte swizzle (8-row atoms of 512 B)
+__device__ __forceinline__ uint64_t desc_sw64(const void* p) {
+  const uint32_t a = smem_u32(p);
+  uint64_t d = 0;
+  d |= (uint64_t)((a & 0x3FFFFu) >> 4);  // start address
+  d |= (uint64_t)1 << 16;                // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(512 >> 4) << 32;       // stride byte offset: 8 rows x 64 B
+  d |= (uint64_t)1 << 46;                // descriptor version (sm_100 family)
+  d |= (uint64_t)4 << 61;                // 64B swizzle
+  return d;
+}
+template <int KB>
+__device__ __forceinline__ uint64_t desc_gemm(const void* p) { return KB == 64 ? desc_sw128(p) : desc_sw64(p); }
 
 __device__ __forceinline__ void mma_bf16(uint32_t dt, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
   asm volatile(
@@ -246,13 +286,15 @@ __device__ __forceinline__ float2 square_pair(long long V, float fscale) {
 // are kernel parameters (single problem) or live in global memory (grouped
 // launch, written by the host before the launch: acquired through the
 // tensormap proxy before their first use).
+template <int KB>
 __device__ __forceinline__ void gemm_tile(const CUtensorMap* tmA, const CUtensorMap* tmB, const GemmArgs g,
                                           const int m_tile, const int n_tile, const bool global_maps) {
+  using R = GemmRing<KB>;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
-  uint64_t* empty = full + STAGES;
-  uint64_t* tfull = empty + STAGES;
+  uint64_t* full = (uint64_t*)(smem + R::STAGES * R::STAGE);
+  uint64_t* empty = full + R::STAGES;
+  uint64_t* tfull = empty + R::STAGES;
   uint64_t* tempty = tfull + 1;
   uint64_t* drain = tempty + 1;
   uint32_t* tbase_slot = (uint32_t*)(drain + 1);
@@ -261,11 +303,11 @@ __device__ __forceinline__ void gemm_tile(const CUtensorMap* tmA, const CUtensor
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = m_tile * BM, n0 = n_tile * BN;
   const int passes = (g.S + 1) / 2;
-  int nk = g.Kpad / BK;
-  if (m0 + BM <= g.tri_rows) nk = min(nk, (m0 + BM + BK - 1) / BK);  // zero upper part of L^-1
+  int nk = g.Kpad / KB;
+  if (m0 + BM <= g.tri_rows) nk = min(nk, (m0 + BM + KB - 1) / KB);  // zero upper part of L^-1
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < STAGES; s++) {
+    for (int s = 0; s < R::STAGES; s++) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
@@ -290,9 +332,9 @@ __device__ __forceinline__ void gemm_tile(const CUtensorMap* tmA, const CUtensor
     if (lane == 0) {
       int stage = 0;
       uint32_t phase = 0;
-      int issued[STAGES];
-      uint32_t issued_phase[STAGES];
-      for (int s = 0; s < STAGES; s++) issued[s] = 0;
+      int issued[R::STAGES];
+      uint32_t issued_phase[R::STAGES];
+      for (int s = 0; s < R::STAGES; s++) issued[s] = 0;
       if (global_maps) {
         asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;" ::"l"((uint64_t)tmA) : "memory");
         asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;" ::"l"((uint64_t)tmB) : "memory");
@@ -304,19 +346,19 @@ __device__ __forceinline__ void gemm_tile(const CUtensorMap* tmA, const CUtensor
         for (int kb = 0; kb < nk; kb++) {
           if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, g.err, 1)) { ok = false; break; }
           issued[stage] = 0;
-          uint8_t* sb = smem + stage * STAGE_BYTES;
-          mbar_expect_tx(&full[stage], (two ? 2 * A_TILE : A_TILE) + B_TILE);
-          tma_load_2d(sb, tmA, kb * BK, s0 * g.Mpad + m0, &full[stage]);
-          if (two) tma_load_2d(sb + A_TILE, tmA, kb * BK, s1 * g.Mpad + m0, &full[stage]);
-          tma_load_2d(sb + 2 * A_TILE, tmB, kb * BK, g.col0 + n0, &full[stage]);
+          uint8_t* sb = smem + stage * R::STAGE;
+          mbar_expect_tx(&full[stage], (two ? 2 * R::A : R::A) + R::B);
+          tma_load_2d(sb, tmA, kb * KB, s0 * g.Mpad + m0, &full[stage]);
+          if (two) tma_load_2d(sb + R::A, tmA, kb * KB, s1 * g.Mpad + m0, &full[stage]);
+          tma_load_2d(sb + 2 * R::A, tmB, kb * KB, g.col0 + n0, &full[stage]);
           issued[stage] = 1;
           issued_phase[stage] = phase;
-          if (++stage == STAGES) { stage = 0; phase ^= 1; }
+          if (++stage == R::STAGES) { stage = 0; phase ^= 1; }
         }
       }
       if (!ok) {
         // let this CTA's own copies land before the shared memory is released
-        for (int s = 0; s < STAGES; s++)
+        for (int s = 0; s < R::STAGES; s++)
           if (issued[s]) mbar_drain(&full[s], issued_phase[s]);
       }
     }
@@ -333,10 +375,10 @@ __device__ __forceinline__ void gemm_tile(const CUtensorMap* tmA, const CUtensor
         for (int kb = 0; kb < nk; kb++) {
           if (!mbar_wait(&full[stage], phase, abort_flag, g.err, 3)) { ok = false; break; }
           tc_fence_after();
-          uint8_t* sb = smem + stage * STAGE_BYTES;
-          const uint64_t a0 = desc_sw128(sb), a1 = desc_sw128(sb + A_TILE), b = desc_sw128(sb + 2 * A_TILE);
+          uint8_t* sb = smem + stage * R::STAGE;
+          const uint64_t a0 = desc_gemm<KB>(sb), a1 = desc_gemm<KB>(sb + R::A), b = desc_gemm<KB>(sb + 2 * R::A);
 #pragma unroll
-          for (int k = 0; k < BK / 16; k++) {
+          for (int k = 0; k < KB / 16; k++) {
             const uint64_t koff = (uint64_t)((k * 32) >> 4);
             const uint32_t acc = (kb > 0 || k > 0) ? 1u : 0u;
             mma_bf16(tbase, a0 + koff, b + koff, IDESC, acc);
@@ -344,7 +386,7 @@ __device__ __forceinline__ void gemm_tile(const CUtensorMap* tmA, const CUtensor
           }
           any = true;
           mma_commit(&empty[stage]);
-          if (++stage == STAGES) { stage = 0; phase ^= 1; }
+          if (++stage == R::STAGES) { stage = 0; phase ^= 1; }
         }
         if (!ok) break;
         mma_commit(tfull);
@@ -433,7 +475,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   const int gsz = min(g.tiles_m - first_m, GROUP_M);
   const int m_tile = first_m + (tile % per_group) % gsz;
   const int n_tile = (tile % per_group) / gsz;
-  gemm_tile(&tmA, &tmB, g, m_tile, n_tile, false);
+  gemm_tile<GBK>(&tmA, &tmB, g, m_tile, n_tile, false);
 }
 
 // Many independent problems in one launch: CTA b computes tiles[b] of
@@ -446,7 +488,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   GemmArgs g = probs[tl.prob].g;
   g.N = cols[probs[tl.prob].cohort];
   if (tl.n_tile * BN >= g.N) return;
-  gemm_tile(maps + 2 * tl.prob, maps + 2 * tl.prob + 1, g, tl.m_tile, tl.n_tile, true);
+  gemm_tile<GRBK>(maps + 2 * tl.prob, maps + 2 * tl.prob + 1, g, tl.m_tile, tl.n_tile, true);
 }
 
 // ---------------------------------------------------------------------------
@@ -674,7 +716,10 @@ __global__ void __launch_bounds__(THREADS, 1)
 __global__ void __launch_bounds__(256) snp_digits_kernel(int n, const float2* __restrict__ A, long long lda, int S,
                                                          int Ncap, int Kpad, __nv_bfloat16* __restrict__ Ad,
                                                          int* __restrict__ aexp) {
-  // 4 consecutive rows per thread: two 16-byte loads, one 8-byte store per digit
+  // 4 consecutive rows per thread: two 16-byte loads, one 8-byte store per
+  // digit.  The column is read twice (maximum, then digits; the second read
+  // mostly hits L2): staging it in shared memory limited the kernel to two
+  // CTAs per SM and measured slower.
   const int i = blockIdx.x;
   const float4* a4 = (const float4*)(A + (long long)i * lda);  // lda even: 32-byte aligned groups of 4 pairs
   const int n4 = (n + 3) >> 2;
@@ -708,8 +753,8 @@ __global__ void __launch_bounds__(256) snp_digits_kernel(int n, const float2* __
   }
   if (threadIdx.x == 0) aexp[i] = e;
   const int se = 6 - e;  // scale 2^se, a normal float for |se| <= 126
-  const float sc = (se >= -126 && se <= 127) ? __int_as_float((127 + se) << 23) : 0.0f;
   const bool scale_ok = se >= -126 && se <= 127;
+  const float sc = scale_ok ? __int_as_float((127 + se) << 23) : 0.0f;
   for (int g = threadIdx.x; g < n4; g += blockDim.x) {
     const int l = 4 * g;
     const float4 u = a4[2 * g], w = a4[2 * g + 1];
@@ -900,18 +945,27 @@ EncodeTiledFn get_encoder() {
   return fn;
 }
 
-// 2D BF16 tensor map, K innermost, 128B swizzle, box {BK, box_rows}
-cudaError_t make_map(CUtensorMap* m, const void* base, long long K, long long rows, int box_rows) {
+// 2D BF16 tensor map, K innermost, box {box_k, box_rows}; 128B swizzle for
+// 64-element (128-byte) rows, 64B swizzle for 32-element rows.  make_map is
+// the split GEMM's operand layout (K-step GBK); the tensor-core quadratic Gram
+// uses 64-element rows (make_map_k64).
+cudaError_t make_map_box(CUtensorMap* m, const void* base, long long K, long long rows, int box_rows, int box_k) {
   EncodeTiledFn enc = get_encoder();
   if (!enc) return cudaErrorNotSupported;
   cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)K * 2};
-  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint32_t box[2] = {(cuuint32_t)box_k, (cuuint32_t)box_rows};
   cuuint32_t es[2] = {1, 1};
   CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, box_k == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+cudaError_t make_map(CUtensorMap* m, const void* base, long long K, long long rows, int box_rows) {
+  return make_map_box(m, base, K, rows, box_rows, GBK);
+}
+cudaError_t make_map_k64(CUtensorMap* m, const void* base, long long K, long long rows, int box_rows) {
+  return make_map_box(m, base, K, rows, box_rows, 64);
 }
 
 int grid_for(long long total) { return (int)std::min<long long>((total + 255) / 256, 152LL * 32); }
@@ -1012,8 +1066,8 @@ cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_
     if (r == cudaSuccess) chk(cudaMemset(p->Adig, 0, sizeof(__nv_bfloat16) * na));
     if (r == cudaSuccess) chk(cudaMemset(p->Ddig, 0, sizeof(__nv_bfloat16) * nd));
     if (r == cudaSuccess) chk(cudaMemset(p->dexp, 0, sizeof(int) * QT_TP));
-    if (r == cudaSuccess) chk(make_map(&p->mapAd, p->Adig, p->Kpad, (long long)p->SQ * p->Ncap, BM));
-    if (r == cudaSuccess) chk(make_map(&p->mapDd, p->Ddig, p->Kpad, (long long)p->SQ * QT_TP, QT_TP));
+    if (r == cudaSuccess) chk(make_map_k64(&p->mapAd, p->Adig, p->Kpad, (long long)p->SQ * p->Ncap, BM));
+    if (r == cudaSuccess) chk(make_map_k64(&p->mapDd, p->Ddig, p->Kpad, (long long)p->SQ * QT_TP, QT_TP));
     if (r == cudaSuccess)
       chk(cudaFuncSetAttribute(quadtc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, QT_SMEM));
     // passes: one SNP digit s with up to four trait digits t, s + t <= SQ + 1
@@ -1290,8 +1344,8 @@ cudaError_t grouped_gemm_create(GroupedGemm** out, const GroupedGemmDesc* d, int
     g.err = err;
     probs[i].cohort = d[i].cohort;
     probs[i].pad = 0;
-    FGLS_CUDA_TRY(make_map(&maps[2 * i], d[i].A, d[i].Kpad, (long long)d[i].S_alloc * d[i].Mpad, BM));
-    FGLS_CUDA_TRY(make_map(&maps[2 * i + 1], d[i].G, d[i].Kpad, d[i].Ncap, BN));
+    FGLS_CUDA_TRY(make_map_box(&maps[2 * i], d[i].A, d[i].Kpad, (long long)d[i].S_alloc * d[i].Mpad, BM, GRBK));
+    FGLS_CUDA_TRY(make_map_box(&maps[2 * i + 1], d[i].G, d[i].Kpad, d[i].Ncap, BN, GRBK));
     order[i] = i;
     work[i] = (long long)g.tiles_m * g.Kpad;
   }
@@ -1323,7 +1377,8 @@ cudaError_t grouped_gemm_create(GroupedGemm** out, const GroupedGemmDesc* d, int
   if (r == cudaSuccess)
     chk(cudaMemcpy(gg->maps, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice));
   if (r == cudaSuccess)
-    chk(cudaFuncSetAttribute(ozaki_grouped_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    chk(cudaFuncSetAttribute(ozaki_grouped_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             GROUPED_SMEM_BYTES));
   if (r != cudaSuccess) {
     grouped_gemm_destroy(gg);
     return r;
@@ -1334,7 +1389,7 @@ cudaError_t grouped_gemm_create(GroupedGemm** out, const GroupedGemmDesc* d, int
 
 cudaError_t grouped_gemm_run(GroupedGemm* gg, cudaStream_t s, const int* dcols) {
   if (gg->ntiles == 0) return cudaSuccess;
-  ozaki_grouped_gemm_kernel<<<gg->ntiles, THREADS, SMEM_BYTES, s>>>(gg->tiles, gg->probs, gg->maps, dcols);
+  ozaki_grouped_gemm_kernel<<<gg->ntiles, THREADS, GROUPED_SMEM_BYTES, s>>>(gg->tiles, gg->probs, gg->maps, dcols);
   note_launch();
   return cudaGetLastError();
 }

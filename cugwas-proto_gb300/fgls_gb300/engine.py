@@ -42,6 +42,7 @@ EXPORTS = (
     "fglsgpu_batch_create", "fglsgpu_batch_destroy", "fglsgpu_batch_params", "fglsgpu_batch_step",
     "fglsgpu_batch_sync", "fglsgpu_batch_stream", "fglsgpu_batch_last_error", "fglsgpu_batch_profile",
     "fglsgpu_batch_profile_read", "fglsgpu_run_block_device_packed", "fglsgpu_run_snps_compact",
+    "fglsgpu_reml_fit", "fglsgpu_set_hsigma",
 )
 PROF_CLASSES = ("genotypes", "split_gemm", "selfgram", "solve", "fp64_gemm", "trsm", "gram", "spare")
 
@@ -108,6 +109,8 @@ def lib():
     L.fglsgpu_adjoint_block_device.argtypes = [P, P, I, P, LL]
     L.fglsgpu_adjoint_read.argtypes = [P, P, P, P]
     L.fglsgpu_reml.argtypes = [P, P, P]
+    L.fglsgpu_reml_fit.argtypes = [P, C.c_double, C.c_double, I, P, P, P, P]
+    L.fglsgpu_set_hsigma.argtypes = [P, P, P]
     L.fglsgpu_pvalues_device.argtypes = [P, P, P, I, LL, LL, P, LL]
     L.fglsgpu_batch_create.argtypes = [C.POINTER(CohortDesc), I, C.POINTER(BatchConfig), C.POINTER(P)]
     L.fglsgpu_batch_destroy.argtypes = [P]
@@ -241,6 +244,18 @@ class Engine:
         ll, dll = np.empty(self.t), np.empty(self.t)
         self._check(self.L.fglsgpu_reml(self._h, _ptr(ll), _ptr(dll)))
         return ll, dll
+
+    def reml_fit(self, h_lo=0.0, h_hi=1.0 - 1e-5, grid=64):
+        """REML estimates per trait: (h, sigma, profiled loglik, its h-gradient), each (t,)."""
+        h, sg, ll, dll = (np.empty(self.t) for _ in range(4))
+        self._check(self.L.fglsgpu_reml_fit(self._h, float(h_lo), float(h_hi), int(grid), _ptr(h), _ptr(sg),
+                                            _ptr(ll), _ptr(dll)))
+        return h, sg, ll, dll
+
+    def set_hsigma(self, h, sigma):
+        h, sigma = _f64(h), _f64(sigma)
+        self._keep_hs = [h, sigma]
+        self._check(self.L.fglsgpu_set_hsigma(self._h, _ptr(h), _ptr(sigma)))
 
     def sync(self):
         self._check(self.L.fglsgpu_sync(self._h))

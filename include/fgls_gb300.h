@@ -188,6 +188,26 @@ int fglsgpu_adjoint_read(fglsgpu_engine *e, double *dh, double *dsigma, double *
  * and dl/dh_j; valid after fglsgpu_adjoint_reset. */
 int fglsgpu_reml(fglsgpu_engine *e, double *loglik, double *dloglik_dh);
 
+/* ---- variance-component estimation (eigen variant, FP64) ----
+ * No counterpart in the reference, which reads h and sigma from the H.in and
+ * Sig.in files (src/fgls_chol.c:139-145).  Fits, per trait, the null model
+ * y ~ N(XL b, sigma (h Phi + (1-h) I)) by REML with sigma profiled out
+ * (sigma_hat = y^T P y / (n - wXL)) and h maximised over [h_lo, h_hi]
+ * (0 <= h_lo < h_hi <= 1) on a grid of `grid` points (2..256; 0 = 64) whose
+ * gradient sign changes are refined to roots.  Outputs (host, t each, any may
+ * be NULL): h, sigma, the profiled REML log-likelihood (constants dropped;
+ * equal to fglsgpu_reml's value at that h and sigma) and its h-gradient there
+ * (about 0 unless the maximum is on an endpoint).  Needs set_problem; does not
+ * change the engine's h and sigma. */
+int fglsgpu_reml_fit(fglsgpu_engine *e, double h_lo, double h_hi, int grid, double *h, double *sigma,
+                     double *loglik, double *dloglik_dh);
+
+/* Replaces every trait's h and sigma (host arrays of t) without redoing the
+ * eigendecomposition (eigen) or Phi upload (chol: the next select_trait
+ * refactors M_j).  Same checks as set_problem.  Invalidates the adjoint
+ * state (call fglsgpu_adjoint_reset again). */
+int fglsgpu_set_hsigma(fglsgpu_engine *e, const double *h, const double *sigma);
+
 /* Switches a live engine between FGLSGPU_PREC_FP64 and FGLSGPU_PREC_SPLIT
  * without redoing set_problem (eigen keeps its eigendecomposition; chol
  * needs select_trait again). */

@@ -286,3 +286,55 @@ def reml(Z, W, XL, Y, h, sigma):
         ll[j] = -0.5 * (-np.sum(np.log(d)) + np.linalg.slogdet(Vt)[1] + np.sum(d * r0 * r0))
         dll[j] = -0.5 * (-np.sum(c / d) + np.trace(np.linalg.solve(Vt, Vc)) + np.sum(c * r0 * r0))
     return ll, dll
+
+
+def reml_profiled(W, ZtXL, zty, h):
+    """Profiled null-model REML of one trait at h (sigma = sigma_hat(h)).
+
+    The reference reads h and sigma from files (src/fgls_chol.c:139-145) and
+    uses M = sigma (h Phi + (1 - h) I) (src/fgls_chol.c:251-256).  With
+    d = 1/(h w + 1 - h), sigma_hat(h) = r^T D r / (n - wXL) for the GLS
+    residual r, and the value/gradient are ``reml`` evaluated at
+    (h, sigma_hat(h)) (the sigma-gradient vanishes there).
+    Returns (loglik, dloglik/dh, sigma_hat)."""
+    n, wXL = ZtXL.shape
+    d = 1.0 / (h * W + (1.0 - h))
+    c = -(W - 1.0) * d * d
+    G = (ZtXL * d[:, None]).T @ ZtXL
+    b = np.linalg.solve(G, (ZtXL * d[:, None]).T @ zty)
+    r = zty - ZtXL @ b
+    q = float(np.sum(d * r * r))
+    nn = n - wXL
+    sig = q / nn
+    Gc = (ZtXL * c[:, None]).T @ ZtXL
+    ll = -0.5 * (nn * np.log(sig) - np.sum(np.log(d)) + np.linalg.slogdet(G)[1] + nn)
+    dll = -0.5 * (nn * np.sum(c * r * r) / q - np.sum(c / d) + np.trace(np.linalg.solve(G, Gc)))
+    return float(ll), float(dll), sig
+
+
+def reml_fit(W, ZtXL, ZtY, lo=0.0, hi=1.0 - 1e-5, grid=64):
+    """REML estimate of (h, sigma) per trait: the maximiser of the profiled
+    likelihood over [lo, hi] found EMMA-style (Kang et al. 2008): grid, every
+    + -> - sign change of the gradient solved by Brent's method
+    (scipy.optimize.brentq), endpoints whose gradient points outward, best
+    value kept.  Returns (h, sigma, loglik, dloglik) arrays of t."""
+    from scipy.optimize import brentq
+    t = ZtY.shape[1]
+    hs = np.linspace(lo, hi, grid)
+    out = np.zeros((4, t))
+    for j in range(t):
+        y = ZtY[:, j]
+        f = lambda h: reml_profiled(W, ZtXL, y, h)  # noqa: E731
+        ev = [f(h) for h in hs]
+        cands = []
+        if not ev[0][1] > 0:
+            cands.append((hs[0],) + ev[0])
+        if ev[-1][1] >= 0:
+            cands.append((hs[-1],) + ev[-1])
+        for k in range(grid - 1):
+            if ev[k][1] > 0 and not ev[k + 1][1] > 0:
+                x = brentq(lambda h: f(h)[1], hs[k], hs[k + 1], xtol=1e-15, rtol=1e-15, maxiter=200)
+                cands.append((x,) + f(x))
+        best = max(cands, key=lambda c: c[1])
+        out[:, j] = [best[0], best[3], best[1], best[2]]
+    return out[0], out[1], out[2], out[3]

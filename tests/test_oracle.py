@@ -75,3 +75,40 @@ def test_oracle_on_reference_fixture_inputs():
     B, V = O.fgls_chol(pb, 32)
     r = O.compare(B, V, Bref, Vref)
     assert r["beta_normwise"] < 1e-12 and r["se_rel"] < 1e-12, r
+
+
+def _reml_problem(n=240, seed=21):
+    from fgls_gb300 import datagen
+    pb = datagen.make_problem(n, 4, 4, seed=seed, h=[0.0, 0.3, 0.7, 0.95], sigma=[1.0, 2.0, 0.5, 1.5])
+    W, Z = np.linalg.eigh(pb.Phi)
+    return pb, W, Z
+
+
+def test_profiled_reml_is_the_null_model_reml_at_sigma_hat():
+    """The profiled value/gradient equal oracle.reml at (h, sigma_hat(h)) and
+    the gradient matches central differences of the profiled value."""
+    pb, W, Z = _reml_problem()
+    ZtXL, ZtY = Z.T @ pb.XL, Z.T @ pb.Y
+    for j in range(pb.t):
+        for h in (0.05, 0.4, 0.9):
+            ll, dll, sig = O.reml_profiled(W, ZtXL, ZtY[:, j], h)
+            a, da = O.reml(Z, W, pb.XL, pb.Y[:, [j]], [h], [sig])
+            assert abs(a[0] - ll) <= 1e-12 * abs(ll)
+            assert abs(da[0] - dll) <= 1e-10 * abs(ll)
+            e = 1e-6
+            fd = (O.reml_profiled(W, ZtXL, ZtY[:, j], h + e)[0] - O.reml_profiled(W, ZtXL, ZtY[:, j], h - e)[0]) / (2 * e)
+            assert abs(fd - dll) <= 1e-6 * abs(ll)
+
+
+def test_oracle_reml_fit_is_a_maximum():
+    pb, W, Z = _reml_problem()
+    ZtXL, ZtY = Z.T @ pb.XL, Z.T @ pb.Y
+    lo, hi = 0.0, 1.0 - 1e-5
+    h, s, ll, dll = O.reml_fit(W, ZtXL, ZtY, lo, hi, 32)
+    dense = np.linspace(lo, hi, 2001)
+    for j in range(pb.t):
+        prof = [O.reml_profiled(W, ZtXL, ZtY[:, j], x)[0] for x in dense]
+        assert ll[j] >= max(prof) - 1e-9 * abs(ll[j])
+        if lo < h[j] < hi:
+            assert abs(dll[j]) <= 1e-8 * abs(ll[j])
+        assert abs(O.reml_profiled(W, ZtXL, ZtY[:, j], h[j])[2] - s[j]) <= 1e-14 * s[j]
