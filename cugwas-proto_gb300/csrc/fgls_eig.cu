@@ -4,9 +4,12 @@
 //
 // Algorithm (all FP64, no vendor library):
 //  1. Householder reduction to tridiagonal form on the lower triangle
-//     (A := H A H per column; per step: reflector, A v by 32 x 32 lower
-//     tiles with a fixed-order reduction, rank-2 update of the lower
-//     triangle).  Memory-bound: ~1.5 passes over the trailing matrix per column.
+//     (A := H A H per column).  Each column's rank-2 update is deferred by
+//     one step: step k first applies update k-1 to column k (reflector
+//     kernel), then one pass over the trailing matrix applies update k-1 and
+//     forms A v_k by 32 x 32 lower tiles with a fixed-order reduction.
+//     Memory-bound: one read and one write of the trailing lower triangle
+//     per column.
 //  2. Eigenpairs of the tridiagonal by divide and conquer (fgls_dc.cu):
 //     eigenvalues ascending, eigenvectors V of T.
 //  3. Z = H_0 H_1 ... H_{n-3} V applied in blocks of 256 reflectors in
@@ -54,151 +57,238 @@ __global__ void symmetrize_kernel(int n, double* A, long long lda) {
   }
 }
 
-// Householder reflector for column k (one CTA).  v (length m = n-k-1, v[0]=1)
-// to vbuf; v[1:] also stored in A[k+2:, k]; d[k], e[k], tau[k].
-__global__ void __launch_bounds__(256) householder_kernel(int n, int k, double* A, long long lda, double* d,
-                                                          double* e, double* tau, double* vbuf) {
-  __shared__ double red[33];
-  const int m = n - k - 1;
-  const double* x = A + (k + 1) + (long long)k * lda;
-  double s = 0.0;
-  for (int i = 1 + threadIdx.x; i < m; i += blockDim.x) s += x[i] * x[i];
-  const double xnorm2 = block_sum(s, red);
-  const double alpha = x[0];
-  double beta, t, scal;
+// Per column k the work is three launches, all spread over the SMs (a
+// single CTA would be bound by one SM's FP64 rate):
+//   tridiag_col_kernel   w_{k-1} = p + g v from the previous step's p, v and
+//                        partial dots; the pending update of step k-1 applied
+//                        to column k; partial sums of squares of column k
+//   tridiag_step_kernel  the reflector v_k from those sums (every CTA derives
+//                        the same scalars), then one pass over the trailing
+//                        matrix: pending update and A v_k
+//   tridiag_p_kernel     p_k = tau_k A v_k from the tile partials, partial
+//                        dots p_k^T v_k
+constexpr int RT = 256;  // rows per CTA of the row kernels
+
+// Scalars of the Householder reflector of x (x[0] = alpha, |x[1:]|^2 = xnorm2):
+// beta, tau and the scale of x[1:] into v[1:].
+__device__ __forceinline__ void reflector(double alpha, double xnorm2, double& beta, double& tau, double& scal) {
   if (xnorm2 == 0.0) {
-    t = 0.0;
+    tau = 0.0;
     beta = alpha;
     scal = 0.0;
   } else {
     beta = -copysign(sqrt(alpha * alpha + xnorm2), alpha);
-    t = (beta - alpha) / beta;
+    tau = (beta - alpha) / beta;
     scal = 1.0 / (alpha - beta);
   }
-  double* xs = A + (k + 1) + (long long)k * lda;
-  for (int i = 1 + threadIdx.x; i < m; i += blockDim.x) {
-    double v = x[i] * scal;
-    vbuf[i] = v;
-    xs[i] = v;
-  }
-  if (threadIdx.x == 0) {
-    vbuf[0] = 1.0;
-    d[k] = A[k + (long long)k * lda];
-    e[k] = beta;
-    tau[k] = t;
-  }
 }
 
-
-// w = p - (tau/2)(p^T v) v  (one CTA, in place in p)
-__global__ void __launch_bounds__(256) tridiag_w_kernel(int m, const double* v, const double* tau_ptr,
-                                                        double* p) {
+// Column k (rows k+1 .. n-1, i = 0 .. m-1).  With k > 0: g = -(tau_{k-1}/2)
+// sum(dpart) (p^T v of step k-1, fixed order), w_{k-1} = p + g v into wprev
+// (index 0 = row k), x_i = A[k+1+i, k] - (v[1+i] w[0] + w[1+i] v[0]) written
+// back, d[k] = A[k, k] - 2 v[0] w[0], and v_{k-1}[1:] stored below the
+// subdiagonal of column k-1.  Partial sums of x_i^2 (i >= 1) to npart.
+__global__ void __launch_bounds__(RT) tridiag_col_kernel(int n, int k, double* A, long long lda, double* d,
+                                                         const double* __restrict__ tau,
+                                                         const double* __restrict__ pprev,
+                                                         const double* __restrict__ vprev,
+                                                         double* __restrict__ wprev,
+                                                         const double* __restrict__ dpart, int ndp,
+                                                         double* __restrict__ npart) {
   __shared__ double red[33];
-  double s = 0.0;
-  for (int i = threadIdx.x; i < m; i += blockDim.x) s += p[i] * v[i];
-  s = block_sum(s, red);
-  const double g = -0.5 * (*tau_ptr) * s;
-  __syncthreads();
-  for (int i = threadIdx.x; i < m; i += blockDim.x) p[i] += g * v[i];
+  const int m = n - k - 1;
+  const int i = blockIdx.x * RT + threadIdx.x;
+  const bool upd = k > 0;
+  double* x = A + (k + 1) + (long long)k * lda;
+  double sq = 0.0;
+  if (upd) {
+    double dot = 0.0;
+    for (int c = 0; c < ndp; c++) dot += dpart[c];
+    const double g = -0.5 * tau[k - 1] * dot;
+    const double v0 = vprev[0];
+    const double w0 = pprev[0] + g * v0;
+    if (i < m) {
+      const double vi = vprev[1 + i];
+      const double wi = pprev[1 + i] + g * vi;
+      wprev[1 + i] = wi;
+      const double xi = x[i] - (vi * w0 + wi * v0);
+      x[i] = xi;
+      if (i >= 1) sq = xi * xi;
+      A[(k + 1 + i) + (long long)(k - 1) * lda] = vi;  // reflector k-1, row k+1+i
+    }
+    if (i == 0) {
+      wprev[0] = w0;
+      d[k] = A[k + (long long)k * lda] - 2.0 * v0 * w0;
+    }
+  } else {
+    if (i < m && i >= 1) sq = x[i] * x[i];
+    if (i == 0) d[k] = A[k + (long long)k * lda];
+  }
+  sq = block_sum(sq, red);
+  if (threadIdx.x == 0) npart[blockIdx.x] = sq;
 }
 
+// p[i] = tau_k * (strip slots K = 0 .. R/SS, then tile slots K = R+1 .. nt-1
+// of row block R = i / 32, in that order); partial p^T v per CTA to dpart.
+__global__ void __launch_bounds__(RT) tridiag_p_kernel(int m, int nt, const double* __restrict__ part,
+                                                       const double* __restrict__ tau_ptr,
+                                                       const double* __restrict__ v, double* __restrict__ p,
+                                                       double* __restrict__ dpart);
 
-
-__global__ void tridiag_tail_kernel(int n, const double* A, long long lda, double* d, double* e) {
-  if (n >= 2) {
-    d[n - 2] = A[(n - 2) + (long long)(n - 2) * lda];
-    e[n - 2] = A[(n - 1) + (long long)(n - 2) * lda];
+// The last 2 x 2 block.  n >= 3: w of step n-3 from its p, v and partial
+// dots, its reflector stored (A[n-1, n-3]), and its pending update applied.
+__global__ void tridiag_tail_kernel(int n, double* A, long long lda, double* d, double* e, const double* tau,
+                                    const double* p, const double* v, const double* dpart, int ndp) {
+  if (n >= 3) {
+    double dot = 0.0;
+    for (int c = 0; c < ndp; c++) dot += dpart[c];
+    const double g = -0.5 * tau[n - 3] * dot;
+    const double v0 = v[0], v1 = v[1];
+    const double w0 = p[0] + g * v0, w1 = p[1] + g * v1;
+    A[(n - 1) + (long long)(n - 3) * lda] = v1;
+    d[n - 2] = A[(n - 2) + (long long)(n - 2) * lda] - 2.0 * v0 * w0;
+    e[n - 2] = A[(n - 1) + (long long)(n - 2) * lda] - (v1 * w0 + w1 * v0);
+    d[n - 1] = A[(n - 1) + (long long)(n - 1) * lda] - 2.0 * v1 * w1;
+  } else if (n == 2) {
+    d[0] = A[0];
+    e[0] = A[1];
+    d[1] = A[1 + lda];
+  } else {
+    d[0] = A[0];
   }
-  d[n - 1] = A[(n - 1) + (long long)(n - 1) * lda];
   e[n - 1] = 0.0;
 }
 
-
-
 int grid_for(long long total) { return (int)std::min<long long>((total + 255) / 256, 152LL * 32); }
 
-// Symmetric matrix-vector product on the lower triangle only, in 32 x 32
-// tiles: CTA (I, J), I >= J, adds A_IJ v_J to row block I and, below the
-// diagonal, A_IJ^T v_I to row block J, each as its own partial vector
-// part[(R * nt + K) * 32 + r] (R = the receiving row block, K = the other
-// one; every slot is written exactly once), so that the reduction is a fixed
-// order sum: deterministic, no atomics.  Reads m^2/2 elements instead of m^2.
+// One pass over the trailing lower triangle (m x m, 32 x 32 tiles) per
+// column: apply the pending rank-2 update A -= vo wo^T + wo vo^T (vo, wo:
+// the previous step's vectors shifted to this trailing matrix; nullptr at
+// step 0) and form A v with the updated values.  v is the reflector of
+// column x (x[0] = alpha, rows below: the updated column), derived by every
+// CTA from the same fixed-order sum of npart; CTAs Jc = 0 store it (vout),
+// CTA (0, 0) stores tau and e.  CTA (Jc, I) takes the lower tiles (I, J), J
+// in [Jc*SS, min(Jc*SS + SS, I + 1)).  Row block I's partial of A v from the
+// strip goes to slot (I, Jc), and the below-diagonal tiles' A_IJ^T v_I to
+// slot (J, I) (> J), each written exactly once: part[(R * nt + K) * 32 + r].
+// The reduction sums them in a fixed order (deterministic, no atomics).
 constexpr int ST = 32;
-__global__ void __launch_bounds__(256) symv_tiles_kernel(int m, const double* __restrict__ A, long long lda,
-                                                         const double* __restrict__ v, double* __restrict__ part) {
-  const int I = blockIdx.y, J = blockIdx.x;
-  if (J > I) return;
-  const int nt = gridDim.x;
-  __shared__ double a[ST][ST + 1];  // a[c][r] = A[I*32 + r, J*32 + c]
-  __shared__ double vr[ST], vc[ST];
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
-  for (int c = ty; c < ST; c += 8) {
-    const int gr = I * ST + tx, gc = J * ST + c;
-    a[c][tx] = (gr < m && gc < m) ? A[gr + (long long)gc * lda] : 0.0;
-  }
-  if (ty == 0) {
-    vc[tx] = (J * ST + tx < m) ? v[J * ST + tx] : 0.0;
-    vr[tx] = (I * ST + tx < m) ? v[I * ST + tx] : 0.0;
-  }
-  __syncthreads();
-  __shared__ double red[8][ST];
-  if (I == J) {
-    // diagonal tile: the symmetric block from its lower part
-    double s = 0.0;
-    for (int c = ty; c < ST; c += 8) s += (tx >= c ? a[c][tx] : a[tx][c]) * vc[c];
-    red[ty][tx] = s;
-    __syncthreads();
-    if (ty == 0) {
-      double t = 0.0;
-#pragma unroll
-      for (int q = 0; q < 8; q++) t += red[q][tx];
-      part[((long long)I * nt + J) * ST + tx] = t;
+constexpr int SS = 4;
+__global__ void __launch_bounds__(256) tridiag_step_kernel(int m, double* __restrict__ A, long long lda,
+                                                           const double* __restrict__ vo,
+                                                           const double* __restrict__ wo,
+                                                           const double* __restrict__ x,
+                                                           const double* __restrict__ npart, int nnp,
+                                                           double* __restrict__ vout, double* __restrict__ tau_out,
+                                                           double* __restrict__ e_out, double* __restrict__ part) {
+  const int I = blockIdx.y, Jc = blockIdx.x, J0 = Jc * SS;
+  if (J0 > I) return;
+  __shared__ double scal_s;
+  if (threadIdx.x == 0) {
+    double xn2 = 0.0;
+    for (int c = 0; c < nnp; c++) xn2 += npart[c];
+    double beta, tau, scal;
+    reflector(x[0], xn2, beta, tau, scal);
+    scal_s = scal;
+    if (blockIdx.x == 0 && blockIdx.y == 0) {
+      *tau_out = tau;
+      *e_out = beta;
     }
-    return;
   }
-  double s = 0.0;  // row r = tx of A_IJ v_J
-  for (int c = ty; c < ST; c += 8) s += a[c][tx] * vc[c];
-  red[ty][tx] = s;
+  __syncthreads();
+  const double scal = scal_s;
+  // v_i: 1 at i = 0, x_i * scal below, 0 past the matrix
+  auto vval = [&](int i) { return i < m ? (i == 0 ? 1.0 : x[i] * scal) : 0.0; };
+  const int J1 = min(J0 + SS, I + 1);
+  const int nt = gridDim.y;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+  __shared__ double a[ST][ST + 1];  // a[c][r] = A[I*32 + r, J*32 + c]
+  __shared__ double vr[ST], vor[ST], wor[ST], vc[ST], voc[ST], woc[ST];
+  __shared__ double red[8][ST];
+  const bool upd = vo != nullptr;
+  const int gr = I * ST + tx;
+  if (ty == 0) {
+    const double vi = vval(gr);
+    vr[tx] = vi;
+    if (Jc == 0 && gr < m) vout[gr] = vi;
+    vor[tx] = (upd && gr < m) ? vo[gr] : 0.0;
+    wor[tx] = (upd && gr < m) ? wo[gr] : 0.0;
+  }
+  double rs = 0.0;  // row tx of this strip's A_I. v, over this thread's columns
+  for (int J = J0; J < J1; J++) {
+    __syncthreads();  // the previous tile's shared reads are done
+    if (ty == 1) {
+      const int gc = J * ST + tx;
+      vc[tx] = vval(gc);
+      voc[tx] = (upd && gc < m) ? vo[gc] : 0.0;
+      woc[tx] = (upd && gc < m) ? wo[gc] : 0.0;
+    }
+    __syncthreads();
+    for (int c = ty; c < ST; c += 8) {
+      const int gc = J * ST + c;
+      double av = 0.0;
+      if (gr < m && gc < m && (I != J || tx >= c)) {
+        double* pa = A + gr + (long long)gc * lda;
+        av = *pa;
+        if (upd) {
+          // two FMAs (FP64 issue rate bounds this pass)
+          av = fma(-vor[tx], woc[c], av);
+          av = fma(-wor[tx], voc[c], av);
+          *pa = av;
+        }
+      }
+      a[c][tx] = av;
+    }
+    __syncthreads();
+    if (I == J) {
+      // diagonal tile: the symmetric block from its lower part
+      for (int c = ty; c < ST; c += 8) rs += (tx >= c ? a[c][tx] : a[tx][c]) * vc[c];
+    } else {
+      for (int c = ty; c < ST; c += 8) rs += a[c][tx] * vc[c];
+      // column tx of A_IJ^T v_I: rows ty, ty+8, ... here, the eight partial
+      // sums added by one thread (FP64 issue rate is the bound: no shuffles)
+      double cs = 0.0;
+      for (int r = ty; r < ST; r += 8) cs += a[tx][r] * vr[r];
+      red[ty][tx] = cs;
+      __syncthreads();
+      if (ty == 0) {
+        double t = 0.0;
+#pragma unroll
+        for (int q = 0; q < 8; q++) t += red[q][tx];
+        part[((long long)J * nt + I) * ST + tx] = t;
+      }
+    }
+  }
+  __syncthreads();  // the last tile's column reduction has read red
+  red[ty][tx] = rs;
   __syncthreads();
   if (ty == 0) {
     double t = 0.0;
 #pragma unroll
     for (int q = 0; q < 8; q++) t += red[q][tx];
-    part[((long long)I * nt + J) * ST + tx] = t;
-  }
-  __syncthreads();
-  s = 0.0;  // column c = tx of A_IJ^T v_I
-  for (int r = ty; r < ST; r += 8) s += a[tx][r] * vr[r];
-  red[ty][tx] = s;
-  __syncthreads();
-  if (ty == 0) {
-    double t = 0.0;
-#pragma unroll
-    for (int q = 0; q < 8; q++) t += red[q][tx];
-    part[((long long)J * nt + I) * ST + tx] = t;
+    part[((long long)I * nt + Jc) * ST + tx] = t;
   }
 }
 
-// p[i] = tau * sum_K part[(i/32 * nt + K) * 32 + i%32], K ascending
-__global__ void symv_reduce_kernel(int m, int nt, const double* __restrict__ part, const double* __restrict__ tau_ptr,
-                                   double* __restrict__ p) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= m) return;
-  const double* q = part + ((long long)(i / ST) * nt) * ST + (i % ST);
-  double s = 0.0;
-  for (int K = 0; K < nt; K++) s += q[(long long)K * ST];
-  p[i] = *tau_ptr * s;
-}
-
-// A[i, j] -= v_i w_j + w_i v_j on the lower triangle (i >= j) of the trailing matrix
-__global__ void syr2_lower_kernel(int m, double* A, long long lda, const double* v, const double* w) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= m) return;
-  const double vi = v[i], wi = w[i];
-  for (int j = blockIdx.y; j <= i; j += gridDim.y) {
-    double* a = A + i + (long long)j * lda;
-    *a -= vi * w[j] + wi * v[j];
+__global__ void __launch_bounds__(RT) tridiag_p_kernel(int m, int nt, const double* __restrict__ part,
+                                                       const double* __restrict__ tau_ptr,
+                                                       const double* __restrict__ v, double* __restrict__ p,
+                                                       double* __restrict__ dpart) {
+  __shared__ double red[33];
+  const int i = blockIdx.x * RT + threadIdx.x;
+  double pv = 0.0;
+  if (i < m) {
+    const int R = i / ST;
+    const double* q = part + ((long long)R * nt) * ST + (i % ST);
+    double s = 0.0;
+    for (int K = 0; K <= R / SS; K++) s += q[(long long)K * ST];
+    for (int K = R + 1; K < nt; K++) s += q[(long long)K * ST];
+    const double pi = *tau_ptr * s;
+    p[i] = pi;
+    pv = pi * v[i];
   }
+  pv = block_sum(pv, red);
+  if (threadIdx.x == 0) dpart[blockIdx.x] = pv;
 }
 
 // Y (mr x nb, ld mr): reflectors b .. b+nb-1 as explicit columns over rows
@@ -245,9 +335,11 @@ __global__ void __launch_bounds__(256) larft_kernel(int nb, const double* __rest
 }  // namespace
 
 size_t eig_workspace_bytes(int n) {
-  // d, e, tau, vbuf, p (n each) + n ints of scratch + symv partials (nt^2 x 32)
+  // d, e, tau, two v and two w buffers, p (n each), per-CTA dot and norm
+  // partials (n / RT each) + n ints of scratch + symv partials (nt^2 x 32)
   const size_t nt = (size_t)(n + ST - 1) / ST;
-  return sizeof(double) * ((size_t)n * 5 + nt * nt * ST) + sizeof(int) * (size_t)n + 256;
+  const size_t nr = (size_t)(n + RT - 1) / RT;
+  return sizeof(double) * ((size_t)n * 8 + 2 * nr + nt * nt * ST) + sizeof(int) * (size_t)n + 256;
 }
 
 cudaError_t dsyev_device(cudaStream_t s, int n, const double* Phi, long long ldp, double* A, double* Z,
@@ -255,9 +347,12 @@ cudaError_t dsyev_device(cudaStream_t s, int n, const double* Phi, long long ldp
   double* d = (double*)work;
   double* e = d + n;
   double* tau = e + n;
-  double* vbuf = tau + n;
-  double* p = vbuf + n;
-  int* rank = (int*)(p + n);
+  double* vb[2] = {tau + n, tau + 2 * (size_t)n};      // reflectors of even / odd steps
+  double* wb[2] = {tau + 3 * (size_t)n, tau + 4 * (size_t)n};  // their w vectors
+  double* pbuf = tau + 5 * (size_t)n;                  // p of the current step
+  double* dpart = pbuf + n;                            // per-CTA p^T v
+  double* npart = dpart + (n + RT - 1) / RT;           // per-CTA sums of squares of the column
+  int* rank = (int*)(npart + (n + RT - 1) / RT);
   double* part = (double*)(((uintptr_t)(rank + n) + 15) & ~(uintptr_t)15);  // symv partials
   long long nl = 0;
   // FGLS_EIG_TIMING=1 prints the phase times (CUDA events on s) to stderr
@@ -276,19 +371,23 @@ cudaError_t dsyev_device(cudaStream_t s, int n, const double* Phi, long long ldp
   nl++;
   FGLS_CUDA_TRY(cudaGetLastError());
   // 1. tridiagonalization
+  int ndp = 0;  // CTAs of the previous step's p kernel
   for (int k = 0; k + 2 < n; k++) {
     const int m = n - k - 1;
-    householder_kernel<<<1, 256, 0, s>>>(n, k, A, n, d, e, tau, vbuf);
+    const int cur = k & 1, prv = cur ^ 1;
+    const int nr = ceil_div(m, RT);
+    tridiag_col_kernel<<<nr, RT, 0, s>>>(n, k, A, n, d, tau, pbuf, vb[prv], wb[prv], dpart, ndp, npart);
     double* Asub = A + (k + 1) + (long long)(k + 1) * n;
     const int nt = ceil_div(m, ST);
-    symv_tiles_kernel<<<dim3(nt, nt), 256, 0, s>>>(m, Asub, n, vbuf, part);
-    symv_reduce_kernel<<<ceil_div(m, 256), 256, 0, s>>>(m, nt, part, tau + k, p);
-    tridiag_w_kernel<<<1, 256, 0, s>>>(m, vbuf, tau + k, p);
-    dim3 g2(ceil_div(m, 256), std::min(m, 512));
-    syr2_lower_kernel<<<g2, 256, 0, s>>>(m, Asub, n, vbuf, p);
-    nl += 5;
+    const double* vo = k > 0 ? vb[prv] + 1 : nullptr;  // pending update of step k-1, shifted to rows k+1..
+    const double* wo = k > 0 ? wb[prv] + 1 : nullptr;
+    tridiag_step_kernel<<<dim3(ceil_div(nt, SS), nt), 256, 0, s>>>(m, Asub, n, vo, wo, A + (k + 1) + (long long)k * n,
+                                                                    npart, nr, vb[cur], tau + k, e + k, part);
+    tridiag_p_kernel<<<nr, RT, 0, s>>>(m, nt, part, tau + k, vb[cur], pbuf, dpart);
+    ndp = nr;
+    nl += 3;
   }
-  tridiag_tail_kernel<<<1, 1, 0, s>>>(n, A, n, d, e);
+  tridiag_tail_kernel<<<1, 1, 0, s>>>(n, A, n, d, e, tau, pbuf, n >= 3 ? vb[(n - 3) & 1] : nullptr, dpart, ndp);
   nl++;
   FGLS_CUDA_TRY(cudaGetLastError());
   mark(1);

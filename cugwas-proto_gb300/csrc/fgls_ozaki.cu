@@ -507,7 +507,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 // float pair by TwoSum (relative error ~2^-47), then multiplies by
 // sigma_i tau_j in FP64.
 //
-// quadtc_kernel: one CTA per 128 SNP rows, all traits (<= 112) as N.  A pass
+// quadtc_kernel: one CTA per 128 SNP rows and group of 112 traits (N).  A pass
 // holds one SNP digit s (A tile 128 x 64) and up to four trait digits t
 // (B tiles 112 x 64, two per MMA as N = 224); TMEM accumulators at columns
 // [0, 224) and [224, 448).  Same warp roles and bounded waits as
@@ -530,14 +530,28 @@ struct QuadPasses {
 struct QuadArgs {
   int x;          // valid SNP rows
   int t;          // valid traits
+  int tgp;        // rows per trait digit plane: trait groups of QT_TP times QT_TP
   int Ncap;       // rows per SNP digit slice
   int Kpad;
+  int groups;     // trait groups (tgp / QT_TP)
+  int units;      // work units: tiles (128 SNPs x one trait group) x passes
   const int* aexp;  // per SNP: sigma_i = 2^aexp
   const int* dexp;  // per trait: tau_j = 2^dexp
-  double* GR;
-  long long ldg;
+  double* part;     // QT_SLOTS partial planes of Ncap x tgp (column-major, ld Ncap)
   int* err;
 };
+
+// Work units are dealt to the persistent CTAs in contiguous ranges, unit
+// u = tile * passes + pass, tile = m_tile * groups + group.  A tile whose
+// passes span several CTAs gets one partial plane per CTA (slot = CTA -
+// first owner); quadtc_combine_kernel adds them in slot order.
+constexpr int QT_SLOTS = 3;
+__host__ __device__ __forceinline__ int qt_range_begin(int c, int units, int ctas) {
+  return (int)(((long long)c * units) / ctas);
+}
+__host__ __device__ __forceinline__ int qt_owner(int u, int units, int ctas) {
+  return (int)((((long long)u + 1) * ctas - 1) / units);
+}
 
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
@@ -549,6 +563,23 @@ __device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) 
   s = __fadd_rn(a, b);
   const float bp = __fsub_rn(s, a);
   e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+}
+
+// Partial plane of tile `tl` from this CTA (slot = this CTA - the tile's
+// first owner): the thread's SNP row and 56 traits, scaled to FP64.
+__device__ __forceinline__ void quadtc_flush(const QuadArgs& g, int tl, int np, int q, int lane, int jl,
+                                             const float (&H)[56], const float (&L)[56]) {
+  const int i = (tl / g.groups) * BM + q * 32 + lane;
+  const int jh = (tl % g.groups) * QT_TP + jl;
+  const int slot = (int)blockIdx.x - qt_owner(tl * np, g.units, gridDim.x);
+  if (i >= g.x) return;
+  const double si = ldexp(1.0, g.aexp[i]);
+  double* P = g.part + (size_t)slot * g.Ncap * g.tgp;
+#pragma unroll
+  for (int c = 0; c < 56; c++) {
+    const int j = jh + c;
+    if (j < g.t) P[i + (size_t)j * g.Ncap] = ((double)H[c] + (double)L[c]) * si * ldexp(1.0, g.dexp[j]);
+  }
 }
 
 __global__ void __launch_bounds__(THREADS, 1)
@@ -565,8 +596,10 @@ __global__ void __launch_bounds__(THREADS, 1)
   volatile int* abort_flag = (volatile int*)(tbase_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.x * BM;
   const int nk = g.Kpad / BK;
+  const int np = qp.n;
+  const int u0 = qt_range_begin(blockIdx.x, g.units, gridDim.x);
+  const int u1 = qt_range_begin(blockIdx.x + 1, g.units, gridDim.x);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; s++) {
@@ -598,7 +631,9 @@ __global__ void __launch_bounds__(THREADS, 1)
       uint32_t issued_phase[STAGES];
       for (int s = 0; s < STAGES; s++) issued[s] = 0;
       bool ok = true;
-      for (int p = 0; p < qp.n && ok; p++) {
+      for (int u = u0; u < u1 && ok; u++) {
+        const int tile = u / np, p = u - tile * np;
+        const int m0 = (tile / g.groups) * BM, grp = tile % g.groups;
         int nt = 0;
         for (int q = 0; q < 4; q++) nt += qp.t[p][q] > 0 ? 1 : 0;
         for (int kb = 0; kb < nk; kb++) {
@@ -609,7 +644,8 @@ __global__ void __launch_bounds__(THREADS, 1)
           tma_load_2d(sb, &tmA, kb * BK, (qp.s[p] - 1) * g.Ncap + m0, &full[stage]);
           for (int q = 0; q < 4; q++)
             if (qp.t[p][q] > 0)
-              tma_load_2d(sb + A_TILE + q * QT_BT, &tmD, kb * BK, (qp.t[p][q] - 1) * QT_TP, &full[stage]);
+              tma_load_2d(sb + A_TILE + q * QT_BT, &tmD, kb * BK, (qp.t[p][q] - 1) * g.tgp + grp * QT_TP,
+                          &full[stage]);
           issued[stage] = 1;
           issued_phase[stage] = phase;
           if (++stage == STAGES) { stage = 0; phase ^= 1; }
@@ -624,9 +660,11 @@ __global__ void __launch_bounds__(THREADS, 1)
       int stage = 0;
       uint32_t phase = 0;
       bool ok = true, any = false;
-      for (int p = 0; p < qp.n && ok; p++) {
+      for (int u = u0; u < u1 && ok; u++) {
+        const int lu = u - u0;
+        const int p = u % np;
         const bool second = qp.t[p][2] > 0;
-        if (!mbar_wait(tempty, (p & 1) ^ 1, abort_flag, g.err, 12)) { ok = false; break; }
+        if (!mbar_wait(tempty, (lu & 1) ^ 1, abort_flag, g.err, 12)) { ok = false; break; }
         tc_fence_after();
         for (int kb = 0; kb < nk; kb++) {
           if (!mbar_wait(&full[stage], phase, abort_flag, g.err, 13)) { ok = false; break; }
@@ -655,52 +693,50 @@ __global__ void __launch_bounds__(THREADS, 1)
     __syncwarp();
   } else {
     // epilogue: warp w reads TMEM lane quarter w % 4 (SNP rows) and the
-    // trait half (w - 2) / 4 (56 traits)
+    // trait half (w - 2) / 4 (56 traits) of the unit's trait group
     const int q = warp & 3;
-    const int jh = ((warp - 2) >> 2) * 56;
-    const int i = m0 + q * 32 + lane;
+    const int jl = ((warp - 2) >> 2) * 56;  // TMEM column offset within the group
     float H[56], L[56];
-#pragma unroll
-    for (int c = 0; c < 56; c++) H[c] = L[c] = 0.0f;
     bool done = true;
-    for (int p = 0; p < qp.n; p++) {
-      int ok = 1;
-      if (lane == 0) ok = mbar_wait(tfull, p & 1, abort_flag, g.err, 14) ? 1 : 0;
-      ok = __shfl_sync(0xffffffffu, ok, 0);
-      if (!ok) { done = false; break; }
-      tc_fence_after();
+    for (int u = u0; u < u1 && done;) {
+      const int tile = u / np;
+      const int uend = min(u1, (tile + 1) * np);  // this CTA's passes of the tile
+#pragma unroll
+      for (int c = 0; c < 56; c++) H[c] = L[c] = 0.0f;
+      for (; u < uend; u++) {
+        const int lu = u - u0;
+        const int p = u - tile * np;
+        int ok = 1;
+        if (lane == 0) ok = mbar_wait(tfull, lu & 1, abort_flag, g.err, 14) ? 1 : 0;
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (!ok) { done = false; break; }
+        tc_fence_after();
 #pragma unroll 1
-      for (int slot = 0; slot < 4; slot++) {
-        const int tt = qp.t[p][slot];
-        if (tt <= 0) continue;  // uniform across the CTA
-        const float w = __int_as_float((127 - 6 * (qp.s[p] + tt)) << 23);  // 64^-(s+t)
-        const uint32_t col = (uint32_t)((slot >> 1) * 224 + (slot & 1) * QT_TP + jh);
-        const uint32_t ta = tbase + ((uint32_t)(q * 32) << 16) + col;
+        for (int slot = 0; slot < 4; slot++) {
+          const int tt = qp.t[p][slot];
+          if (tt <= 0) continue;  // uniform across the CTA
+          const float w = __int_as_float((127 - 6 * (qp.s[p] + tt)) << 23);  // 64^-(s+t)
+          const uint32_t col = (uint32_t)((slot >> 1) * 224 + (slot & 1) * QT_TP + jl);
+          const uint32_t ta = tbase + ((uint32_t)(q * 32) << 16) + col;
 #pragma unroll
-        for (int c8 = 0; c8 < 7; c8++) {
-          uint32_t v[8];
-          tmem_ld8(ta + c8 * 8, v);
-          tmem_ld_wait();
+          for (int c8 = 0; c8 < 7; c8++) {
+            uint32_t v[8];
+            tmem_ld8(ta + c8 * 8, v);
+            tmem_ld_wait();
 #pragma unroll
-          for (int u = 0; u < 8; u++) {
-            const float x = __fmul_rn(__uint_as_float(v[u]), w);  // exact: integer times a power of two
-            float s2, e;
-            two_sum_f(H[c8 * 8 + u], x, s2, e);
-            H[c8 * 8 + u] = s2;
-            L[c8 * 8 + u] = __fadd_rn(L[c8 * 8 + u], e);
+            for (int e8 = 0; e8 < 8; e8++) {
+              const float x = __fmul_rn(__uint_as_float(v[e8]), w);  // exact: integer times a power of two
+              float s2, e;
+              two_sum_f(H[c8 * 8 + e8], x, s2, e);
+              H[c8 * 8 + e8] = s2;
+              L[c8 * 8 + e8] = __fadd_rn(L[c8 * 8 + e8], e);
+            }
           }
         }
+        tc_fence_before();
+        mbar_arrive(tempty);
       }
-      tc_fence_before();
-      mbar_arrive(tempty);
-    }
-    if (done && i < g.x) {
-      const double si = ldexp(1.0, g.aexp[i]);
-#pragma unroll
-      for (int c = 0; c < 56; c++) {
-        const int j = jh + c;
-        if (j < g.t) g.GR[i + (long long)j * g.ldg] = ((double)H[c] + (double)L[c]) * si * ldexp(1.0, g.dexp[j]);
-      }
+      if (done) quadtc_flush(g, tile, np, q, lane, jl, H, L);
     }
   }
   tc_fence_before();
@@ -709,17 +745,37 @@ __global__ void __launch_bounds__(THREADS, 1)
   if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(512) : "memory");
 }
 
+// GR[i + j ldg] = sum over the CTAs that covered tile (i / 128, j / 112) of
+// their partial planes, in slot order (deterministic).
+__global__ void __launch_bounds__(256) quadtc_combine_kernel(int x, int t, int Ncap, int tgp, int groups, int np,
+                                                             int units, int ctas, const double* __restrict__ part,
+                                                             double* __restrict__ GR, long long ldg) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)x * t) return;
+  const int i = (int)(idx % x), j = (int)(idx / x);
+  const int tile = (i / BM) * groups + j / QT_TP;
+  const int first = qt_owner(tile * np, units, ctas), last = qt_owner(tile * np + np - 1, units, ctas);
+  double v = 0.0;
+  for (int c = first; c <= last; c++) v += part[(size_t)(c - first) * Ncap * tgp + i + (size_t)j * Ncap];
+  GR[i + (long long)j * ldg] = v;
+}
+
 // SNP digits: CTA per SNP column i of the R2 float pairs (rows l < n):
 // sigma_i = 2^aexp[i] >= 2 max_l R2, then S signed base-64 digits of R2 / sigma_i
 // at Ad[(s*Ncap + i)*Kpad + l].  Digits from the exact float-pair value:
 // d = rint(hi), (hi, lo) = TwoSum(hi - d, lo), times 64.
-__global__ void __launch_bounds__(256) snp_digits_kernel(int n, const float2* __restrict__ A, long long lda, int S,
-                                                         int Ncap, int Kpad, __nv_bfloat16* __restrict__ Ad,
-                                                         int* __restrict__ aexp) {
+constexpr int QD_THREADS = 256;
+__global__ void __launch_bounds__(QD_THREADS) snp_digits_kernel(int n, const float2* __restrict__ A, long long lda,
+                                                              int S, int Ncap, int Kpad,
+                                                              __nv_bfloat16* __restrict__ Ad,
+                                                              int* __restrict__ aexp) {
   // 4 consecutive rows per thread: two 16-byte loads, one 8-byte store per
-  // digit.  The column is read twice (maximum, then digits; the second read
-  // mostly hits L2): staging it in shared memory limited the kernel to two
-  // CTAs per SM and measured slower.
+  // digit.  The column is read twice (maximum, then digits) and the second
+  // read mostly misses L2 (~1200 columns in flight): 5.5 GB of DRAM traffic
+  // per 16384 x 10000 block at 6.4 TB/s.  CTAs of 1024 threads (two per SM)
+  // made the second read hit L2 but ran slower (0.91 against 0.86 ms), as did
+  // staging the column in shared memory and taking the maxima in the GEMM
+  // epilogue (+0.9 ms of GEMM).
   const int i = blockIdx.x;
   const float4* a4 = (const float4*)(A + (long long)i * lda);  // lda even: 32-byte aligned groups of 4 pairs
   const int n4 = (n + 3) >> 2;
@@ -786,8 +842,9 @@ __global__ void __launch_bounds__(256) snp_digits_kernel(int n, const float2* __
 
 // Trait digits: CTA per trait j of d (FP64, d[l + j*n]): tau_j = 2^dexp[j] >=
 // 2 max_l d, digits of d / tau_j in FP64 at Dd[(s*QT_TP + j)*Kpad + l].
-__global__ void __launch_bounds__(256) trait_digits_kernel(int n, const double* __restrict__ d, int S, int Kpad,
-                                                           __nv_bfloat16* __restrict__ Dd, int* __restrict__ dexp) {
+__global__ void __launch_bounds__(256) trait_digits_kernel(int n, const double* __restrict__ d, int S, int tgp,
+                                                           int Kpad, __nv_bfloat16* __restrict__ Dd,
+                                                           int* __restrict__ dexp) {
   const int j = blockIdx.x;
   const double* c = d + (long long)j * n;
   __shared__ double red[32];
@@ -811,7 +868,7 @@ __global__ void __launch_bounds__(256) trait_digits_kernel(int n, const double* 
     double v = ldexp(c[l], 6 - e);
     for (int s = 0; s < S; s++) {
       const double dd = rint(v);
-      Dd[((long long)s * QT_TP + j) * Kpad + l] = __double2bfloat16(dd);
+      Dd[((long long)s * tgp + j) * Kpad + l] = __double2bfloat16(dd);
       v = (v - dd) * 64.0;
     }
   }
@@ -993,8 +1050,10 @@ struct OzakiPlan {
   // tensor-core quadratic Gram (eigen, 33 <= t <= 112): digit operands
   bool tq = false;
   int SQ = 9;                     // digits per side; pairs with s + t <= SQ + 1
+  int tgp = 0;                    // trait rows per digit plane (multiple of QT_TP)
+  double* qpart = nullptr;        // QT_SLOTS x Ncap x tgp partial planes of the tensor-core Gram
   __nv_bfloat16* Adig = nullptr;  // SQ x Ncap x Kpad SNP digits
-  __nv_bfloat16* Ddig = nullptr;  // SQ x QT_TP x Kpad trait digits
+  __nv_bfloat16* Ddig = nullptr;  // SQ x tgp x Kpad trait digits
   int *aexp = nullptr, *dexp = nullptr;
   CUtensorMap mapAd, mapDd;
   QuadPasses qp;
@@ -1055,19 +1114,21 @@ cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_
   p->sub = p->Ncap;  // one GEMM launch per block
   {
     const char* qe = getenv("FGLS_QUAD_TC");
-    p->tq = eigen && t >= 33 && t <= QT_TP && !(qe && qe[0] == '0');
+    p->tq = eigen && t >= 33 && !(qe && qe[0] == '0');
   }
   if (p->tq && r == cudaSuccess) {
-    const size_t na = (size_t)p->SQ * p->Ncap * p->Kpad, nd = (size_t)p->SQ * QT_TP * p->Kpad;
+    p->tgp = (t + QT_TP - 1) / QT_TP * QT_TP;
+    const size_t na = (size_t)p->SQ * p->Ncap * p->Kpad, nd = (size_t)p->SQ * p->tgp * p->Kpad;
     chk(cudaMalloc(&p->Adig, sizeof(__nv_bfloat16) * na));
     chk(cudaMalloc(&p->Ddig, sizeof(__nv_bfloat16) * nd));
     chk(cudaMalloc(&p->aexp, sizeof(int) * p->Ncap));
-    chk(cudaMalloc(&p->dexp, sizeof(int) * QT_TP));
+    chk(cudaMalloc(&p->dexp, sizeof(int) * p->tgp));
+    chk(cudaMalloc(&p->qpart, sizeof(double) * QT_SLOTS * (size_t)p->Ncap * p->tgp));
     if (r == cudaSuccess) chk(cudaMemset(p->Adig, 0, sizeof(__nv_bfloat16) * na));
     if (r == cudaSuccess) chk(cudaMemset(p->Ddig, 0, sizeof(__nv_bfloat16) * nd));
-    if (r == cudaSuccess) chk(cudaMemset(p->dexp, 0, sizeof(int) * QT_TP));
+    if (r == cudaSuccess) chk(cudaMemset(p->dexp, 0, sizeof(int) * p->tgp));
     if (r == cudaSuccess) chk(make_map_k64(&p->mapAd, p->Adig, p->Kpad, (long long)p->SQ * p->Ncap, BM));
-    if (r == cudaSuccess) chk(make_map_k64(&p->mapDd, p->Ddig, p->Kpad, (long long)p->SQ * QT_TP, QT_TP));
+    if (r == cudaSuccess) chk(make_map_k64(&p->mapDd, p->Ddig, p->Kpad, (long long)p->SQ * p->tgp, QT_TP));
     if (r == cudaSuccess)
       chk(cudaFuncSetAttribute(quadtc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, QT_SMEM));
     // passes: one SNP digit s with up to four trait digits t, s + t <= SQ + 1
@@ -1091,7 +1152,7 @@ cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_
 void ozaki_destroy(OzakiPlan* p) {
   if (!p) return;
   void* ptrs[] = {p->A,    p->G,     p->scale, p->C,     p->U,    p->D,    p->dmax, p->amax,
-                  p->part, p->Linv,  p->LinvT, p->err,   p->Adig, p->Ddig, p->aexp, p->dexp};
+                  p->part, p->Linv,  p->LinvT, p->err,   p->Adig, p->Ddig, p->aexp, p->dexp, p->qpart};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   delete p;
@@ -1142,19 +1203,29 @@ cudaError_t selfgram(OzakiPlan* p, cudaStream_t s, int col0, int xq, int t, doub
   if (!p->tq || col0 != 0)
     return quad_gram(s, p->n, xq, t, A, p->Mpad, p->amax + col0, p->D, p->n, p->dmax, p->part, GR + col0, ldg,
                      p->sms);
-  snp_digits_kernel<<<xq, 256, 0, s>>>(p->n, A, p->Mpad, p->SQ, p->Ncap, p->Kpad, p->Adig, p->aexp);
+  snp_digits_kernel<<<xq, QD_THREADS, 0, s>>>(p->n, A, p->Mpad, p->SQ, p->Ncap, p->Kpad, p->Adig, p->aexp);
   note_launch();
   QuadArgs g;
   g.x = xq;
   g.t = t;
+  g.tgp = p->tgp;
   g.Ncap = p->Ncap;
   g.Kpad = p->Kpad;
+  g.groups = p->tgp / QT_TP;
+  const int tiles = (xq + BM - 1) / BM * g.groups;
+  g.units = tiles * p->qp.n;
   g.aexp = p->aexp;
   g.dexp = p->dexp;
-  g.GR = GR;
-  g.ldg = ldg;
+  g.part = p->qpart;
   g.err = p->err;
-  quadtc_kernel<<<(xq + BM - 1) / BM, THREADS, QT_SMEM, s>>>(p->mapAd, p->mapDd, p->qp, g);
+  // persistent CTAs, at most one per SM, each with >= half a tile's passes
+  // (so a tile spans at most QT_SLOTS CTAs)
+  const int ctas = std::max(1, std::min(p->sms, g.units / ((p->qp.n + 1) / 2)));
+  quadtc_kernel<<<ctas, THREADS, QT_SMEM, s>>>(p->mapAd, p->mapDd, p->qp, g);
+  note_launch();
+  const long long cells = (long long)xq * t;
+  quadtc_combine_kernel<<<(int)((cells + 255) / 256), 256, 0, s>>>(xq, t, p->Ncap, p->tgp, g.groups, p->qp.n,
+                                                                    g.units, ctas, p->qpart, GR, ldg);
   note_launch();
   return cudaGetLastError();
 }
@@ -1169,7 +1240,7 @@ cudaError_t ozaki_set_eigen(OzakiPlan* p, cudaStream_t s, const double* Z, const
   split_pairs_kernel<<<p->t, 256, 0, s>>>(p->n, p->t, dinv, p->D, p->dmax);
   note_launch();
   if (p->tq) {
-    trait_digits_kernel<<<p->t, 256, 0, s>>>(p->n, dinv, p->SQ, p->Kpad, p->Ddig, p->dexp);
+    trait_digits_kernel<<<p->t, 256, 0, s>>>(p->n, dinv, p->SQ, p->tgp, p->Kpad, p->Ddig, p->dexp);
     note_launch();
   }
   return cudaGetLastError();

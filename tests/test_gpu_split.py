@@ -62,7 +62,8 @@ def test_split_gemm_fp64_accuracy():
 
 
 @pytest.mark.parametrize("n,m,t,xb", [(300, 700, 5, 256), (1000, 1100, 16, 512), (200, 300, 1, 256),
-                                      (260, 400, 40, 256), (300, 257, 100, 512), (150, 300, 130, 256)])
+                                      (260, 400, 40, 256), (300, 257, 100, 512), (150, 300, 130, 256),
+                                      (300, 200, 1000, 256), (500, 300, 113, 256)])
 def test_split_eigen_vs_oracle(n, m, t, xb):
     from fgls_gb300 import Engine, datagen
     pb = datagen.make_problem(n, m, t, seed=n + t, hsig_uniform=True)
@@ -125,10 +126,10 @@ def test_split_u8_matches_fp64_genotype_input():
     assert np.array_equal(B, dB.cpu().numpy().reshape(3, 200, 4))
 
 
-@pytest.mark.parametrize("n,t", [(700, 40), (700, 100), (2000, 100)])
+@pytest.mark.parametrize("n,t", [(700, 40), (700, 100), (2000, 100), (900, 250)])
 def test_tensor_core_quad_gram_vs_fp64_path(n, t, monkeypatch):
     """The quadratic Gram on the tensor cores (6-bit digits of both operands,
-    used for 33 <= t <= 112) and the double-FP32 CUDA-core kernel, each
+    used for t >= 33, in groups of 112 traits) and the double-FP32 CUDA-core kernel, each
     against the all-FP64 device path on the same eigendecomposition: the
     tensor-core path is within 2e-12 on the SE scale (measured ~3e-13), the
     double-FP32 one within 1e-10 (measured ~1e-11)."""
