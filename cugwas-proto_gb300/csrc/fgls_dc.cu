@@ -182,85 +182,135 @@ __global__ void dc_sort_kernel(int n, int off, int n1, int nn, double beta, cons
   perm[rk] = i;
 }
 
-// Sequential deflation scan (one thread), the dlaed2 criteria:
+// Sequential deflation scan, the dlaed2 criteria:
 //   |rho z_j| <= tol            -> eigenpair (d_j, column j) kept as is
 //   |(d_nj - d_pj) c s| <= tol  -> rotate columns pj, nj so that z_pj = 0
 // Outputs kept roots (dk, zk, colk) in ascending order, deflated (dd, cold),
-// and the rotation list (rc1, rc2, rcs, rsn) applied in order.
-__global__ void dc_deflate_kernel(int nn, double rho, double* __restrict__ ds, double* __restrict__ zs,
-                                  const int* __restrict__ perm, double* __restrict__ dk, double* __restrict__ zk,
-                                  int* __restrict__ colk, double* __restrict__ dd, int* __restrict__ cold,
-                                  int* __restrict__ rc1, int* __restrict__ rc2, double* __restrict__ rcs,
-                                  double* __restrict__ rsn, MergeState* st) {
+// and the rotation list (rc1, rc2, rcs, rsn) applied in order.  The scan is
+// one thread's dependent chain; with STAGED its operands (d, z, perm) sit in
+// shared memory (loaded and written back by the whole CTA), otherwise in
+// global memory (merges too large for shared memory).  The kept roots are
+// written over the scanned prefix (index K <= the current pair's first
+// index, whose values are already consumed) and sorted there.
+constexpr size_t DEFLATE_SMEM_MAX = 220 * 1024;  // dynamic shared memory of the staged scan (nn <= 11264)
+template <bool STAGED>
+__global__ void __launch_bounds__(256) dc_deflate_kernel(int nn, double rho, double* __restrict__ ds,
+                                                         double* __restrict__ zs, int* __restrict__ perm,
+                                                         double* __restrict__ dk, double* __restrict__ zk,
+                                                         int* __restrict__ colk, double* __restrict__ dd,
+                                                         int* __restrict__ cold, int* __restrict__ rc1,
+                                                         int* __restrict__ rc2, double* __restrict__ rcs,
+                                                         double* __restrict__ rsn, MergeState* st) {
+  extern __shared__ double dsm[];
+  __shared__ double red[2][32];
+  double* sd = STAGED ? dsm : ds;
+  double* sz = STAGED ? dsm + nn : zs;
+  int* sp = STAGED ? (int*)(dsm + 2 * (size_t)nn) : perm;
   double dmax = 0.0, zmax = 0.0;
-  for (int i = 0; i < nn; i++) {
-    dmax = fmax(dmax, fabs(ds[i]));
-    zmax = fmax(zmax, fabs(zs[i]));
-  }
-  const double tol = 8.0 * DBL_EPSILON * fmax(dmax, rho * zmax);
-  int K = 0, nd = 0, nr = 0;
-  int pj = -1;
-  for (int j = 0; j < nn; j++) {
-    if (rho * fabs(zs[j]) <= tol) {
-      dd[nd] = ds[j];
-      cold[nd++] = perm[j];
-      continue;
+  for (int i = threadIdx.x; i < nn; i += blockDim.x) {
+    const double dv = ds[i], zv = zs[i];
+    if (STAGED) {
+      sd[i] = dv;
+      sz[i] = zv;
+      sp[i] = perm[i];
     }
-    if (pj < 0) {
-      pj = j;
-      continue;
-    }
-    double s = zs[pj], c = zs[j];
-    const double tau = hypot(c, s);
-    const double t = ds[j] - ds[pj];
-    c /= tau;
-    s = -s / tau;
-    if (fabs(t * c * s) <= tol) {
-      // rotate: z_j <- tau, z_pj <- 0; columns (pj, j)
-      zs[j] = tau;
-      zs[pj] = 0.0;
-      rc1[nr] = perm[pj];
-      rc2[nr] = perm[j];
-      rcs[nr] = c;
-      rsn[nr] = s;
-      nr++;
-      const double tt = ds[pj] * c * c + ds[j] * s * s;
-      ds[j] = ds[pj] * s * s + ds[j] * c * c;
-      ds[pj] = tt;
-      dd[nd] = ds[pj];
-      cold[nd++] = perm[pj];
-      pj = j;
-    } else {
-      dk[K] = ds[pj];
-      zk[K] = zs[pj];
-      colk[K++] = perm[pj];
-      pj = j;
-    }
+    dmax = fmax(dmax, fabs(dv));
+    zmax = fmax(zmax, fabs(zv));
   }
-  if (pj >= 0) {
-    dk[K] = ds[pj];
-    zk[K] = zs[pj];
-    colk[K++] = perm[pj];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+    zmax = fmax(zmax, __shfl_xor_sync(0xffffffffu, zmax, o));
   }
-  // the rotations change the diagonal of kept entries already in place; the
-  // kept list must stay ascending for the secular intervals
-  for (int a = 1; a < K; a++) {
-    double dv = dk[a], zv = zk[a];
-    int cv = colk[a], b = a - 1;
-    while (b >= 0 && dk[b] > dv) {
-      dk[b + 1] = dk[b];
-      zk[b + 1] = zk[b];
-      colk[b + 1] = colk[b];
-      b--;
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = dmax;
+    red[1][threadIdx.x >> 5] = zmax;
+  }
+  __syncthreads();
+  __shared__ int Ks;
+  if (threadIdx.x == 0) {
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+      dmax = fmax(dmax, red[0][w]);
+      zmax = fmax(zmax, red[1][w]);
     }
-    dk[b + 1] = dv;
-    zk[b + 1] = zv;
-    colk[b + 1] = cv;
+    const double tol = 8.0 * DBL_EPSILON * fmax(dmax, rho * zmax);
+    int K = 0, nd = 0, nr = 0;
+    int pj = -1;
+    for (int j = 0; j < nn; j++) {
+      if (rho * fabs(sz[j]) <= tol) {
+        dd[nd] = sd[j];
+        cold[nd++] = sp[j];
+        continue;
+      }
+      if (pj < 0) {
+        pj = j;
+        continue;
+      }
+      double sn = sz[pj], c = sz[j];
+      const double tau = hypot(c, sn);
+      const double t = sd[j] - sd[pj];
+      c /= tau;
+      sn = -sn / tau;
+      if (fabs(t * c * sn) <= tol) {
+        // rotate: z_j <- tau, z_pj <- 0; columns (pj, j)
+        sz[j] = tau;
+        sz[pj] = 0.0;
+        rc1[nr] = sp[pj];
+        rc2[nr] = sp[j];
+        rcs[nr] = c;
+        rsn[nr] = sn;
+        nr++;
+        const double tt = sd[pj] * c * c + sd[j] * sn * sn;
+        sd[j] = sd[pj] * sn * sn + sd[j] * c * c;
+        sd[pj] = tt;
+        dd[nd] = sd[pj];
+        cold[nd++] = sp[pj];
+        pj = j;
+      } else {
+        const double kd = sd[pj], kz = sz[pj];
+        const int kc = sp[pj];
+        sd[K] = kd;  // K <= pj: entries below pj are consumed
+        sz[K] = kz;
+        sp[K++] = kc;
+        pj = j;
+      }
+    }
+    if (pj >= 0) {
+      const double kd = sd[pj], kz = sz[pj];
+      const int kc = sp[pj];
+      sd[K] = kd;
+      sz[K] = kz;
+      sp[K++] = kc;
+    }
+    // the rotations change the diagonal of kept entries already in place; the
+    // kept list must stay ascending for the secular intervals
+    for (int a = 1; a < K; a++) {
+      const double dv = sd[a], zv = sz[a];
+      const int cv = sp[a];
+      int b = a - 1;
+      while (b >= 0 && sd[b] > dv) {
+        sd[b + 1] = sd[b];
+        sz[b + 1] = sz[b];
+        sp[b + 1] = sp[b];
+        b--;
+      }
+      sd[b + 1] = dv;
+      sz[b + 1] = zv;
+      sp[b + 1] = cv;
+    }
+    st->K = K;
+    st->ndefl = nd;
+    st->nrot = nr;
+    st->rho = rho;
+    Ks = K;
   }
-  st->K = K;
-  st->ndefl = nd;
-  st->nrot = nr;
-  st->rho = rho;
+  __syncthreads();
+  const int K = Ks;
+  for (int i = threadIdx.x; i < K; i += blockDim.x) {
+    dk[i] = sd[i];
+    zk[i] = sz[i];
+    colk[i] = sp[i];
+  }
 }
 
 // Apply the deflation rotations to the node's columns (one thread per row).
@@ -530,6 +580,8 @@ size_t dc_workspace_bytes(int n) {
 // eigenvectors of T (n x n, ld n).
 cudaError_t dc_tridiag_eig(cudaStream_t s, int n, double* d, double* e, double* W, double* V, void* work,
                            int* fail_dev, long long* launches) {
+  FGLS_CUDA_TRY(cudaFuncSetAttribute(dc_deflate_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)DEFLATE_SMEM_MAX));
   double* ds = (double*)work;
   double* zs = ds + n;
   double* dk = zs + n;
@@ -595,7 +647,13 @@ cudaError_t dc_tridiag_eig(cudaStream_t s, int n, double* d, double* e, double* 
     const int nn = nd.size, off = nd.off;
     const double rho = 2.0 * fabs(beta);
     dc_sort_kernel<<<ceil_div(nn, 256), 256, 0, s>>>(n, off, nd.n1, nn, beta, W, V, ds, zs, perm);
-    dc_deflate_kernel<<<1, 1, 0, s>>>(nn, rho, ds, zs, perm, dk, zk, colk, dd, cold, rc1, rc2, rcs, rsn, st);
+    const size_t dsmem = (size_t)nn * (2 * sizeof(double) + sizeof(int));
+    if (dsmem <= DEFLATE_SMEM_MAX)
+      dc_deflate_kernel<true><<<1, 256, dsmem, s>>>(nn, rho, ds, zs, perm, dk, zk, colk, dd, cold, rc1, rc2, rcs,
+                                                    rsn, st);
+    else
+      dc_deflate_kernel<false><<<1, 256, 0, s>>>(nn, rho, ds, zs, perm, dk, zk, colk, dd, cold, rc1, rc2, rcs,
+                                                 rsn, st);
     nl += 2;
     FGLS_CUDA_TRY(cudaMemcpyAsync(&hs, st, sizeof(MergeState), cudaMemcpyDeviceToHost, s));
     FGLS_CUDA_TRY(cudaStreamSynchronize(s));
