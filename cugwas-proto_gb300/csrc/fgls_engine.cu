@@ -535,11 +535,13 @@ int run_snps_impl(fglsgpu_engine* e, const double* XR, long long m, double* B, d
   if (rc) return rc;
   const int p = e->p, nt = out_traits(e);
   const long long colb = (long long)c.n * c.wXR;  // doubles per SNP
-  const long long nblk = (m + c.x_b - 1) / c.x_b;
-  for (long long b = 0; b < nblk; b++) {
+  // Blocks of x_b SNPs, the first two of x_b/4 and x_b/2: the first upload
+  // is the only one no compute hides, so it is kept short.
+  long long ib = 0;
+  for (long long b = 0; ib < m; b++) {
     const int k = (int)(b & 1);
-    const long long ib = b * c.x_b;
-    const int x = (int)std::min<long long>(c.x_b, m - ib);
+    const int want = b == 0 ? std::max(256, c.x_b / 4) : b == 1 ? std::max(256, c.x_b / 2) : c.x_b;
+    const int x = (int)std::min<long long>(std::min(want, c.x_b), m - ib);
     // slot k's input is free once block b-2's compute finished
     ENG_TRY(e, cudaStreamWaitEvent(e->h2d, e->evC[k], 0), "wait");
     ENG_TRY(e, cudaMemcpyAsync(e->dX[k], XR + ib * colb, sizeof(double) * colb * x, cudaMemcpyHostToDevice, e->h2d),
@@ -570,6 +572,7 @@ int run_snps_impl(fglsgpu_engine* e, const double* XR, long long m, double* B, d
               "P download");
     }
     ENG_TRY(e, cudaEventRecord(e->evD[k], e->d2h), "event");
+    ib += x;
   }
   ENG_TRY(e, cudaStreamSynchronize(e->d2h), "run_snps");
   ENG_TRY(e, cudaStreamSynchronize(e->h2d), "run_snps");
