@@ -101,10 +101,15 @@ __global__ void __launch_bounds__(RT) tridiag_col_kernel(int n, int k, double* A
   const bool upd = k > 0;
   double* x = A + (k + 1) + (long long)k * lda;
   double sq = 0.0;
-  if (upd) {
+  __shared__ double dot_s;
+  if (upd && threadIdx.x == 0) {
     double dot = 0.0;
     for (int c = 0; c < ndp; c++) dot += dpart[c];
-    const double g = -0.5 * tau[k - 1] * dot;
+    dot_s = dot;
+  }
+  __syncthreads();
+  if (upd) {
+    const double g = -0.5 * tau[k - 1] * dot_s;
     const double v0 = vprev[0];
     const double w0 = pprev[0] + g * v0;
     if (i < m) {
@@ -127,13 +132,6 @@ __global__ void __launch_bounds__(RT) tridiag_col_kernel(int n, int k, double* A
   sq = block_sum(sq, red);
   if (threadIdx.x == 0) npart[blockIdx.x] = sq;
 }
-
-// p[i] = tau_k * (strip slots K = 0 .. R/SS, then tile slots K = R+1 .. nt-1
-// of row block R = i / 32, in that order); partial p^T v per CTA to dpart.
-__global__ void __launch_bounds__(RT) tridiag_p_kernel(int m, int nt, const double* __restrict__ part,
-                                                       const double* __restrict__ tau_ptr,
-                                                       const double* __restrict__ v, double* __restrict__ p,
-                                                       double* __restrict__ dpart);
 
 // The last 2 x 2 block.  n >= 3: w of step n-3 from its p, v and partial
 // dots, its reflector stored (A[n-1, n-3]), and its pending update applied.
@@ -270,25 +268,38 @@ __global__ void __launch_bounds__(256) tridiag_step_kernel(int m, double* __rest
   }
 }
 
-__global__ void __launch_bounds__(RT) tridiag_p_kernel(int m, int nt, const double* __restrict__ part,
-                                                       const double* __restrict__ tau_ptr,
-                                                       const double* __restrict__ v, double* __restrict__ p,
-                                                       double* __restrict__ dpart) {
-  __shared__ double red[33];
-  const int i = blockIdx.x * RT + threadIdx.x;
-  double pv = 0.0;
-  if (i < m) {
-    const int R = i / ST;
-    const double* q = part + ((long long)R * nt) * ST + (i % ST);
-    double s = 0.0;
-    for (int K = 0; K <= R / SS; K++) s += q[(long long)K * ST];
-    for (int K = R + 1; K < nt; K++) s += q[(long long)K * ST];
-    const double pi = *tau_ptr * s;
-    p[i] = pi;
-    pv = pi * v[i];
+// p[i] = tau_k * sum of row block R = i / 32's slots (strip slots K = 0 ..
+// R/SS, then tile slots K = R+1 .. nt-1).  One CTA per row block: thread
+// (r, c) sums slots c, c+8, ... of row r, the eight partial sums are added in
+// c order (fixed order); the CTA's p^T v goes to dpart[R].
+__global__ void __launch_bounds__(256) tridiag_p_kernel(int m, int nt, const double* __restrict__ part,
+                                                        const double* __restrict__ tau_ptr,
+                                                        const double* __restrict__ v, double* __restrict__ p,
+                                                        double* __restrict__ dpart) {
+  __shared__ double red[8][ST];
+  const int R = blockIdx.x;
+  const int r = threadIdx.x & 31, c = threadIdx.x >> 5;
+  const int i = R * ST + r;
+  const int ns = R / SS + 1;          // strip slots 0 .. R/SS
+  const int nslots = ns + (nt - R - 1);  // then tile slots R+1 .. nt-1
+  const double* q = part + ((long long)R * nt) * ST + r;
+  double sum = 0.0;
+  for (int e = c; e < nslots; e += 8) {
+    const int K = e < ns ? e : R + 1 + (e - ns);
+    sum += q[(long long)K * ST];
   }
-  pv = block_sum(pv, red);
-  if (threadIdx.x == 0) dpart[blockIdx.x] = pv;
+  red[c][r] = sum;
+  __syncthreads();
+  if (c == 0) {
+    double t = 0.0;
+#pragma unroll
+    for (int u = 0; u < 8; u++) t += red[u][r];
+    const double pi = i < m ? *tau_ptr * t : 0.0;
+    if (i < m) p[i] = pi;
+    double pv = i < m ? pi * v[i] : 0.0;
+    pv = warp_sum(pv);
+    if (r == 0) dpart[R] = pv;
+  }
 }
 
 // Y (mr x nb, ld mr): reflectors b .. b+nb-1 as explicit columns over rows
@@ -339,7 +350,7 @@ size_t eig_workspace_bytes(int n) {
   // partials (n / RT each) + n ints of scratch + symv partials (nt^2 x 32)
   const size_t nt = (size_t)(n + ST - 1) / ST;
   const size_t nr = (size_t)(n + RT - 1) / RT;
-  return sizeof(double) * ((size_t)n * 8 + 2 * nr + nt * nt * ST) + sizeof(int) * (size_t)n + 256;
+  return sizeof(double) * ((size_t)n * 8 + nt + nr + nt * nt * ST) + sizeof(int) * (size_t)n + 256;
 }
 
 cudaError_t dsyev_device(cudaStream_t s, int n, const double* Phi, long long ldp, double* A, double* Z,
@@ -350,8 +361,8 @@ cudaError_t dsyev_device(cudaStream_t s, int n, const double* Phi, long long ldp
   double* vb[2] = {tau + n, tau + 2 * (size_t)n};      // reflectors of even / odd steps
   double* wb[2] = {tau + 3 * (size_t)n, tau + 4 * (size_t)n};  // their w vectors
   double* pbuf = tau + 5 * (size_t)n;                  // p of the current step
-  double* dpart = pbuf + n;                            // per-CTA p^T v
-  double* npart = dpart + (n + RT - 1) / RT;           // per-CTA sums of squares of the column
+  double* dpart = pbuf + n;                            // p^T v per 32-row block
+  double* npart = dpart + (n + ST - 1) / ST;           // per-CTA sums of squares of the column
   int* rank = (int*)(npart + (n + RT - 1) / RT);
   double* part = (double*)(((uintptr_t)(rank + n) + 15) & ~(uintptr_t)15);  // symv partials
   long long nl = 0;
@@ -383,8 +394,8 @@ cudaError_t dsyev_device(cudaStream_t s, int n, const double* Phi, long long ldp
     const double* wo = k > 0 ? wb[prv] + 1 : nullptr;
     tridiag_step_kernel<<<dim3(ceil_div(nt, SS), nt), 256, 0, s>>>(m, Asub, n, vo, wo, A + (k + 1) + (long long)k * n,
                                                                     npart, nr, vb[cur], tau + k, e + k, part);
-    tridiag_p_kernel<<<nr, RT, 0, s>>>(m, nt, part, tau + k, vb[cur], pbuf, dpart);
-    ndp = nr;
+    tridiag_p_kernel<<<nt, 256, 0, s>>>(m, nt, part, tau + k, vb[cur], pbuf, dpart);
+    ndp = nt;
     nl += 3;
   }
   tridiag_tail_kernel<<<1, 1, 0, s>>>(n, A, n, d, e, tau, pbuf, n >= 3 ? vb[(n - 3) & 1] : nullptr, dpart, ndp);
