@@ -246,12 +246,14 @@ __global__ void __launch_bounds__(256) dc_deflate_kernel(int nn, double rho, dou
         pj = j;
         continue;
       }
-      double sn = sz[pj], c = sz[j];
-      const double tau = hypot(c, sn);
+      const double zp = sz[pj], zj = sz[j];
       const double t = sd[j] - sd[pj];
-      c /= tau;
-      sn = -sn / tau;
-      if (fabs(t * c * sn) <= tol) {
+      // |t c s| <= tol with c = zj / tau, s = -zp / tau, tau^2 = zj^2 + zp^2,
+      // tested without the square root and divisions (the scan is one
+      // thread's FP64 dependency chain); c, s only for a rotation
+      if (fabs(t * zj * zp) <= tol * (zj * zj + zp * zp)) {
+        const double tau = hypot(zj, zp);
+        const double c = zj / tau, sn = -zp / tau;
         // rotate: z_j <- tau, z_pj <- 0; columns (pj, j)
         sz[j] = tau;
         sz[pj] = 0.0;

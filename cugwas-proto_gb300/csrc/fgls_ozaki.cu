@@ -919,16 +919,30 @@ __global__ void __launch_bounds__(256) slice_rows_kernel(int K, int rows, const 
 __device__ __forceinline__ __nv_bfloat16 geno_bf16(unsigned char v) { return __float2bfloat16((float)v); }
 __device__ __forceinline__ __nv_bfloat16 geno_bf16(double v) { return __float2bfloat16((float)v); }
 
+// One CTA per genotype column (no 64-bit index division per element).  FP64
+// columns that start on a 16-byte boundary move as 16-byte pairs into 4-byte
+// BF16 pairs; rows K .. Kpad-1 of G stay zero from its allocation.
 template <typename T>
-__global__ void genotypes_bf16_kernel(int K, int cols, const T* __restrict__ src, long long lds,
-                                      __nv_bfloat16* __restrict__ G, int Kpad) {
-  const long long total = (long long)cols * K;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
-       e += (long long)gridDim.x * blockDim.x) {
-    const int k = (int)(e % K);
-    const long long c = e / K;
-    G[c * Kpad + k] = geno_bf16(src[c * lds + k]);
+__global__ void __launch_bounds__(256) genotypes_bf16_kernel(int K, int cols, const T* __restrict__ src,
+                                                             long long lds, __nv_bfloat16* __restrict__ G,
+                                                             int Kpad) {
+  const long long c = blockIdx.x;
+  const T* col = src + c * lds;
+  __nv_bfloat16* g = G + c * Kpad;
+  if constexpr (sizeof(T) == 8) {
+    if (((uintptr_t)col & 15) == 0) {
+      const double2* col2 = (const double2*)col;
+      __nv_bfloat162* g2 = (__nv_bfloat162*)g;
+      const int K2 = K >> 1;
+      for (int k = threadIdx.x; k < K2; k += blockDim.x) {
+        const double2 v = col2[k];
+        g2[k] = __halves2bfloat162(geno_bf16(v.x), geno_bf16(v.y));
+      }
+      if ((K & 1) && threadIdx.x == 0) g[K - 1] = geno_bf16(col[K - 1]);
+      return;
+    }
   }
+  for (int k = threadIdx.x; k < K; k += blockDim.x) g[k] = geno_bf16(col[k]);
 }
 
 __global__ void eye_kernel(int n, double* A) {
@@ -1193,7 +1207,8 @@ cudaError_t run_gemm(OzakiPlan* p, cudaStream_t s, int col0, int x, int tri_rows
 
 template <typename T>
 cudaError_t load_genotypes(OzakiPlan* p, cudaStream_t s, const T* X, int x) {
-  genotypes_bf16_kernel<T><<<grid_for((long long)x * p->n), 256, 0, s>>>(p->n, x, X, p->n, p->G, p->Kpad);
+  if (x <= 0) return cudaSuccess;
+  genotypes_bf16_kernel<T><<<x, 256, 0, s>>>(p->n, x, X, p->n, p->G, p->Kpad);
   note_launch();
   return cudaGetLastError();
 }
@@ -1356,12 +1371,24 @@ __global__ void grouped_genotypes_kernel(const GenoCohort* __restrict__ gc, cons
   const int x = sc[c].x, n = gc[c].n, Kpad = gc[c].Kpad;
   const T* __restrict__ src = (const T*)sc[c].X;
   __nv_bfloat16* __restrict__ G = gc[c].G;
-  const long long total = (long long)x * n;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
-       e += (long long)gridDim.x * blockDim.x) {
-    const int k = (int)(e % n);
-    const long long col = e / n;
-    G[col * Kpad + k] = geno_bf16(src[col * n + k]);
+  // columns strided over the CTAs of this cohort, rows over the threads; u8
+  // columns that start on a 4-byte boundary move 4 calls per load
+  for (int col = blockIdx.x; col < x; col += gridDim.x) {
+    const T* s = src + (long long)col * n;
+    __nv_bfloat16* g = G + (long long)col * Kpad;
+    if constexpr (sizeof(T) == 1) {
+      if (((uintptr_t)s & 3) == 0) {
+        const int n4 = n >> 2;
+        for (int q = threadIdx.x; q < n4; q += blockDim.x) {
+          const uchar4 v = ((const uchar4*)s)[q];
+          ((__nv_bfloat162*)g)[2 * q] = __halves2bfloat162(geno_bf16(v.x), geno_bf16(v.y));
+          ((__nv_bfloat162*)g)[2 * q + 1] = __halves2bfloat162(geno_bf16(v.z), geno_bf16(v.w));
+        }
+        for (int k = 4 * n4 + threadIdx.x; k < n; k += blockDim.x) g[k] = geno_bf16(s[k]);
+        continue;
+      }
+    }
+    for (int k = threadIdx.x; k < n; k += blockDim.x) g[k] = geno_bf16(s[k]);
   }
 }
 }  // namespace
@@ -1375,7 +1402,7 @@ cudaError_t split_rescale_rows(cudaStream_t s, int rows, const double* built_sca
 }
 
 cudaError_t grouped_genotypes(cudaStream_t s, const GenoCohort* dgc, const StepCohort* dsc, int cohorts, bool u8) {
-  dim3 grid(96, cohorts);
+  dim3 grid(256, cohorts);
   if (u8)
     grouped_genotypes_kernel<unsigned char><<<grid, 256, 0, s>>>(dgc, dsc);
   else
