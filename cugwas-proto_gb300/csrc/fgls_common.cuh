@@ -37,6 +37,12 @@ inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 cudaError_t dgemm(cudaStream_t s, bool transA, bool transB, int M, int N, int K, double alpha,
                   const double* A, long long lda, const double* B, long long ldb, double beta,
                   double* C, long long ldc);
+// The same product with K split over CTAs when M x N has too few 64 x 64
+// tiles to fill the GPU (partials in work, work_elems doubles, then summed in
+// a fixed order); falls back to dgemm when splitting does not apply.
+cudaError_t dgemm_splitk(cudaStream_t s, bool transA, bool transB, int M, int N, int K, double alpha,
+                         const double* A, long long lda, const double* B, long long ldb, double beta, double* C,
+                         long long ldc, double* work, long long work_elems);
 // Lower-triangle-only variant (C n x n lower, tiles strictly above the
 // diagonal are skipped; entries above the diagonal inside diagonal tiles
 // are written too and must be ignored by the caller).

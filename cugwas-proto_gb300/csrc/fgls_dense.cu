@@ -32,6 +32,15 @@ __global__ void __launch_bounds__(GT) dgemm_kernel(int M, int N, int K, double a
                                                    long long ldc) {
   const int bi = blockIdx.x, bj = blockIdx.y;
   if (LOWER && bj > bi) return;  // tile strictly above the diagonal (square C, GM == GN)
+  if (gridDim.z > 1) {
+    // split K: slice z of the K range into its own M x N partial (ldc = M)
+    const int kc = (K + (int)gridDim.z - 1) / (int)gridDim.z;
+    const int k0 = (int)blockIdx.z * kc;
+    K = max(0, min(K - k0, kc));
+    A += TA ? (long long)k0 : (long long)k0 * lda;
+    B += TB ? (long long)k0 * ldb : (long long)k0;
+    C += (long long)blockIdx.z * ldc * N;
+  }
   const int i0 = bi * GM, j0 = bj * GN;
   __shared__ double As[2][GK][GM + 1];
   __shared__ double Bs[2][GK][GN + 1];
@@ -263,6 +272,43 @@ cudaError_t dgemm(cudaStream_t s, bool tA, bool tB, int M, int N, int K, double 
                   const double* A, long long lda, const double* B, long long ldb, double beta,
                   double* C, long long ldc) {
   return launch_dgemm<false>(s, tA, tB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+
+namespace {
+// C = alpha * sum_z P_z + beta * C, z ascending (P_z: M x N, ld M)
+__global__ void splitk_reduce_kernel(int M, int N, int splits, const double* __restrict__ P, double alpha,
+                                     double beta, double* __restrict__ C, long long ldc) {
+  const long long total = (long long)M * N;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    double v = 0.0;
+    for (int z = 0; z < splits; z++) v += P[e + (long long)z * total];
+    const int i = (int)(e % M), j = (int)(e / M);
+    double* c = C + i + (long long)j * ldc;
+    *c = beta != 0.0 ? fma(beta, *c, alpha * v) : alpha * v;
+  }
+}
+}  // namespace
+
+cudaError_t dgemm_splitk(cudaStream_t s, bool tA, bool tB, int M, int N, int K, double alpha, const double* A,
+                         long long lda, const double* B, long long ldb, double beta, double* C, long long ldc,
+                         double* work, long long work_elems) {
+  if (M <= 0 || N <= 0) return cudaSuccess;
+  const int tiles = ceil_div(M, GM) * ceil_div(N, GN);
+  int splits = std::min(ceil_div(2 * 152, tiles), K / 512);
+  if ((long long)M * N > 0) splits = (int)std::min<long long>(splits, work_elems / ((long long)M * N));
+  if (tiles >= 152 || splits < 2 || !work)
+    return launch_dgemm<false>(s, tA, tB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+  dim3 grid(ceil_div(M, GM), ceil_div(N, GN), splits);
+  if (!tA && !tB) dgemm_kernel<false, false, false><<<grid, GT, 0, s>>>(M, N, K, 1.0, A, lda, B, ldb, 0.0, work, M);
+  else if (!tA && tB) dgemm_kernel<false, true, false><<<grid, GT, 0, s>>>(M, N, K, 1.0, A, lda, B, ldb, 0.0, work, M);
+  else if (tA && !tB) dgemm_kernel<true, false, false><<<grid, GT, 0, s>>>(M, N, K, 1.0, A, lda, B, ldb, 0.0, work, M);
+  else dgemm_kernel<true, true, false><<<grid, GT, 0, s>>>(M, N, K, 1.0, A, lda, B, ldb, 0.0, work, M);
+  const long long total = (long long)M * N;
+  splitk_reduce_kernel<<<(int)std::min<long long>((total + 255) / 256, 152LL * 16), 256, 0, s>>>(M, N, splits, work,
+                                                                                                alpha, beta, C, ldc);
+  note_launch(2);
+  return cudaGetLastError();
 }
 
 cudaError_t dgemm_lower(cudaStream_t s, bool tA, bool tB, int N, int K, double alpha,

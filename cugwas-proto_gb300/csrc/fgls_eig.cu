@@ -430,7 +430,8 @@ cudaError_t dsyev_device(cudaStream_t s, int n, const double* Phi, long long ldp
       const int mr = n - b - 1;
       double* Zs = Z + (b + 1);  // rows b+1 .. n-1, all n columns (ld n)
       build_y_kernel<<<grid_for((long long)mr * nb), 256, 0, s>>>(n, b, nb, A, n, Yb);
-      rc = dgemm(s, true, false, nb, nb, mr, 1.0, Yb, mr, Yb, mr, 0.0, G, nb);
+      // G = Y^T Y has only (nb/64)^2 output tiles: K split over the SMs, W2 as scratch
+      rc = dgemm_splitk(s, true, false, nb, nb, mr, 1.0, Yb, mr, Yb, mr, 0.0, G, nb, W2, (long long)NB * n);
       if (rc == cudaSuccess) {
         larft_kernel<<<1, 256, 0, s>>>(nb, tau + b, G, Tm);
         rc = dgemm(s, true, false, nb, n, mr, 1.0, Yb, mr, Zs, n, 0.0, Wb, nb);
