@@ -746,10 +746,14 @@ def main():
     eng.run_snps_ptr(Xh.data_ptr(), xb, Bh.data_ptr(), Vh.data_ptr())  # warm
     if dist:
         dist.barrier()
-    a = time.perf_counter()
-    eng.run_snps_ptr(Xh.data_ptr(), E * xb, Bh.data_ptr(), Vh.data_ptr())
-    e2e_s = time.perf_counter() - a
-    e2e_s = max_over_ranks(e2e_s, dist, dev)
+    # three whole calls; the median is reported (the host link is shared on
+    # these machines and single calls vary by up to ~25 %)
+    e2e_runs = []
+    for _ in range(3):
+        a = time.perf_counter()
+        eng.run_snps_ptr(Xh.data_ptr(), E * xb, Bh.data_ptr(), Vh.data_ptr())
+        e2e_runs.append(max_over_ranks(time.perf_counter() - a, dist, dev))
+    e2e_s = statistics.median(e2e_runs)
     e2e_value = aggregate_throughput(world, E, xb, t, e2e_s)
 
     # variance components of every trait re-estimated on the device (REML,
@@ -803,7 +807,8 @@ def main():
                              f"{gemm_ms / max(gemm_n, 1):.3f} ms each"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": xb * n * 8,
                 "d2h_bytes_per_step": t * xb * (p + p * p) * 8,
-                "api": "fglsgpu_run_snps (host pinned FP64 XR -> host B/V)", "blocks": E},
+                "api": "fglsgpu_run_snps (host pinned FP64 XR -> host B/V)", "blocks": E,
+                "calls": [aggregate_throughput(world, E, xb, t, x) for x in e2e_runs], "stat": "median of 3 calls"},
         "gpu_launches": launches,
         "clocks": clocks,
         "cpu_baseline": cpu,
