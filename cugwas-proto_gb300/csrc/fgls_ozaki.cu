@@ -35,6 +35,7 @@
 //   chol:  A = [L^-1 ; U^T], U = L^-T [y~ | XL~].
 #include <cuda.h>
 #include <cuda_bf16.h>
+#include <cuda_fp8.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -191,6 +192,14 @@ __device__ __forceinline__ void mma_bf16(uint32_t dt, uint64_t ad, uint64_t bd, 
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dt),
+      "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void mma_f8(uint32_t dt, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}" ::"r"(dt),
       "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
       : "memory");
 }
@@ -496,30 +505,35 @@ __global__ void __launch_bounds__(THREADS, 1)
 //
 //   GR[i + j*ldg] = sum_l R2[l,i] d_j(l),  R2 >= 0, d > 0.
 //
-// Both operands are cut into signed base-64 digits (6 bits, |digit| <= 32):
-// a = R2 / sigma_i = sum_s alpha_s 64^-s, b = d / tau_j = sum_t delta_t 64^-t
-// with sigma_i, tau_j powers of two such that a, b <= 1/2.  A digit product
-// is at most 2^10, so a K-sum over K <= 16384 rows is an integer of at most
-// 2^24: exact in the FP32 TMEM accumulator.  Pairs with s + t <= L are kept
-// (L = 10, 9 digits a side: the dropped pairs and the digit remainders stay
-// below 2^-52 of sigma_i tau_j per row).  The epilogue
-// scales each exact pair sum by 64^-(s+t) (exact) and accumulates it in a
+// Both operands are cut into signed base-32 digits (5 bits, |digit| <= 16,
+// exact in FP8 E4M3): a = R2 / sigma_i = sum_s alpha_s 32^-s,
+// b = d / tau_j = sum_t delta_t 32^-t with sigma_i, tau_j powers of two such
+// that a, b <= 1/2.  A digit product is at most 2^8, so a K-sum over
+// K <= 65536 rows is an integer of at most 2^24: exact in the FP32 TMEM
+// accumulator of the kind::f8f6f4 MMA (twice the BF16 rate).  Pairs with
+// s + t <= L are kept (L = 12, 11 digits a side: the dropped pairs and the
+// digit remainders stay below 2^-55 of sigma_i tau_j per row).  The epilogue
+// scales each exact pair sum by 32^-(s+t) (exact) and accumulates it in a
 // float pair by TwoSum (relative error ~2^-47), then multiplies by
 // sigma_i tau_j in FP64.
 //
-// quadtc_kernel: one CTA per 128 SNP rows and group of 112 traits (N).  A pass
-// holds one SNP digit s (A tile 128 x 64) and up to four trait digits t
-// (B tiles 112 x 64, two per MMA as N = 224); TMEM accumulators at columns
-// [0, 224) and [224, 448).  Same warp roles and bounded waits as
-// ozaki_gemm_kernel.  Threads keep the running (hi, lo) sums of 56 traits.
+// quadtc_kernel: persistent CTAs over (128 SNP rows x group of 112 traits,
+// pass) units.  A pass holds one SNP digit s (A tile 128 x 128 bytes) and up
+// to four trait digits t (B tiles 112 x 128 bytes, two per MMA as N = 224);
+// TMEM accumulators at columns [0, 224) and [224, 448).  Same warp roles and
+// bounded waits as ozaki_gemm_kernel.  Threads keep the running (hi, lo) sums
+// of 56 traits.
 // ---------------------------------------------------------------------------
 constexpr int QT_TP = 112;                          // trait rows of the digit operand
-constexpr int QT_BT = QT_TP * BK * 2;               // 14 KB trait tile
+constexpr int QT_KB = 128;                          // K-block: 128 one-byte digits (one 128B-swizzled row)
+constexpr int QT_BT = QT_TP * QT_KB;                // 14 KB trait tile
 constexpr int QT_STAGE = A_TILE + 4 * QT_BT;        // 72 KB
 constexpr int QT_SMEM = STAGES * QT_STAGE + 1024 + 256;
 constexpr int QT_MAXPASS = 40;
-constexpr uint32_t QT_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(224 >> 3) << 17) |
-                              ((uint32_t)(BM >> 4) << 24);
+// kind::f8f6f4 instruction descriptor: F32 accumulator, A and B E4M3 (format
+// 0), K-major, N = 224, M = 128
+constexpr uint32_t QT_IDESC = (1u << 4) | ((uint32_t)(224 >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+static_assert(A_TILE == BM * QT_KB, "the SNP digit tile is a BF16 split tile's bytes");
 
 struct QuadPasses {
   int n;
@@ -532,7 +546,7 @@ struct QuadArgs {
   int t;          // valid traits
   int tgp;        // rows per trait digit plane: trait groups of QT_TP times QT_TP
   int Ncap;       // rows per SNP digit slice
-  int Kpad;
+  int Kq;         // digit row length (bytes, multiple of QT_KB)
   int groups;     // trait groups (tgp / QT_TP)
   int units;      // work units: tiles (128 SNPs x one trait group) x passes
   const int* aexp;  // per SNP: sigma_i = 2^aexp
@@ -596,7 +610,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   volatile int* abort_flag = (volatile int*)(tbase_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nk = g.Kpad / BK;
+  const int nk = g.Kq / QT_KB;
   const int np = qp.n;
   const int u0 = qt_range_begin(blockIdx.x, g.units, gridDim.x);
   const int u1 = qt_range_begin(blockIdx.x + 1, g.units, gridDim.x);
@@ -641,10 +655,10 @@ __global__ void __launch_bounds__(THREADS, 1)
           issued[stage] = 0;
           uint8_t* sb = smem + stage * QT_STAGE;
           mbar_expect_tx(&full[stage], A_TILE + nt * QT_BT);
-          tma_load_2d(sb, &tmA, kb * BK, (qp.s[p] - 1) * g.Ncap + m0, &full[stage]);
+          tma_load_2d(sb, &tmA, kb * QT_KB, (qp.s[p] - 1) * g.Ncap + m0, &full[stage]);
           for (int q = 0; q < 4; q++)
             if (qp.t[p][q] > 0)
-              tma_load_2d(sb + A_TILE + q * QT_BT, &tmD, kb * BK, (qp.t[p][q] - 1) * g.tgp + grp * QT_TP,
+              tma_load_2d(sb + A_TILE + q * QT_BT, &tmD, kb * QT_KB, (qp.t[p][q] - 1) * g.tgp + grp * QT_TP,
                           &full[stage]);
           issued[stage] = 1;
           issued_phase[stage] = phase;
@@ -672,11 +686,11 @@ __global__ void __launch_bounds__(THREADS, 1)
           uint8_t* sb = smem + stage * QT_STAGE;
           const uint64_t a = desc_sw128(sb), b01 = desc_sw128(sb + A_TILE), b23 = desc_sw128(sb + A_TILE + 2 * QT_BT);
 #pragma unroll
-          for (int k = 0; k < BK / 16; k++) {
+          for (int k = 0; k < QT_KB / 32; k++) {  // K = 32 one-byte digits (32 bytes) per MMA
             const uint64_t koff = (uint64_t)((k * 32) >> 4);
             const uint32_t acc = (kb > 0 || k > 0) ? 1u : 0u;
-            mma_bf16(tbase, a + koff, b01 + koff, QT_IDESC, acc);
-            if (second) mma_bf16(tbase + 224, a + koff, b23 + koff, QT_IDESC, acc);
+            mma_f8(tbase, a + koff, b01 + koff, QT_IDESC, acc);
+            if (second) mma_f8(tbase + 224, a + koff, b23 + koff, QT_IDESC, acc);
           }
           any = true;
           mma_commit(&empty[stage]);
@@ -715,7 +729,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         for (int slot = 0; slot < 4; slot++) {
           const int tt = qp.t[p][slot];
           if (tt <= 0) continue;  // uniform across the CTA
-          const float w = __int_as_float((127 - 6 * (qp.s[p] + tt)) << 23);  // 64^-(s+t)
+          const float w = __int_as_float((127 - 5 * (qp.s[p] + tt)) << 23);  // 32^-(s+t)
           const uint32_t col = (uint32_t)((slot >> 1) * 224 + (slot & 1) * QT_TP + jl);
           const uint32_t ta = tbase + ((uint32_t)(q * 32) << 16) + col;
 #pragma unroll
@@ -761,21 +775,21 @@ __global__ void __launch_bounds__(256) quadtc_combine_kernel(int x, int t, int N
 }
 
 // SNP digits: CTA per SNP column i of the R2 float pairs (rows l < n):
-// sigma_i = 2^aexp[i] >= 2 max_l R2, then S signed base-64 digits of R2 / sigma_i
-// at Ad[(s*Ncap + i)*Kpad + l].  Digits from the exact float-pair value:
-// d = rint(hi), (hi, lo) = TwoSum(hi - d, lo), times 64.
+// sigma_i = 2^aexp[i] >= 2 max_l R2, then S signed base-32 digits of R2 / sigma_i
+// as E4M3 bytes at Ad[(s*Ncap + i)*Kq + l].  Digits from the exact float-pair
+// value: d = rint(hi), (hi, lo) = TwoSum(hi - d, lo), times 32.
+__device__ __forceinline__ uint32_t e4m3_digit(float d) {  // |d| <= 16, an integer: exact
+  return (uint32_t)__nv_cvt_float_to_fp8(d, __NV_SATFINITE, __NV_E4M3);
+}
 constexpr int QD_THREADS = 256;
 __global__ void __launch_bounds__(QD_THREADS) snp_digits_kernel(int n, const float2* __restrict__ A, long long lda,
-                                                              int S, int Ncap, int Kpad,
-                                                              __nv_bfloat16* __restrict__ Ad,
+                                                              int S, int Ncap, int Kq, uint8_t* __restrict__ Ad,
                                                               int* __restrict__ aexp) {
-  // 4 consecutive rows per thread: two 16-byte loads, one 8-byte store per
+  // 4 consecutive rows per thread: two 16-byte loads, one 4-byte store per
   // digit.  The column is read twice (maximum, then digits) and the second
-  // read mostly misses L2 (~1200 columns in flight): 5.5 GB of DRAM traffic
-  // per 16384 x 10000 block at 6.4 TB/s.  CTAs of 1024 threads (two per SM)
-  // made the second read hit L2 but ran slower (0.91 against 0.86 ms), as did
-  // staging the column in shared memory and taking the maxima in the GEMM
-  // epilogue (+0.9 ms of GEMM).
+  // read mostly misses L2 (~1200 columns in flight).  CTAs of 1024 threads
+  // (two per SM) made the second read hit L2 but ran slower, as did staging
+  // the column in shared memory and taking the maxima in the GEMM epilogue.
   const int i = blockIdx.x;
   const float4* a4 = (const float4*)(A + (long long)i * lda);  // lda even: 32-byte aligned groups of 4 pairs
   const int n4 = (n + 3) >> 2;
@@ -801,14 +815,14 @@ __global__ void __launch_bounds__(QD_THREADS) snp_digits_kernel(int n, const flo
   }
   __syncthreads();
   m = red[0];
-  int e = 0;  // 2^e >= 2 m, so that R2 / sigma <= (1 + 2^-23) / 2 and every digit is <= 32
+  int e = 0;  // 2^e >= 2 m, so that R2 / sigma <= (1 + 2^-23) / 2 and every digit is <= 16
   if (m > 0.0f) {
     int ex;
     frexpf(m, &ex);  // m = f 2^ex, f in [0.5, 1)
     e = ex + 1;
   }
   if (threadIdx.x == 0) aexp[i] = e;
-  const int se = 6 - e;  // scale 2^se, a normal float for |se| <= 126
+  const int se = 5 - e;  // scale 2^se, a normal float for |se| <= 126
   const bool scale_ok = se >= -126 && se <= 127;
   const float sc = scale_ok ? __int_as_float((127 + se) << 23) : 0.0f;
   for (int g = threadIdx.x; g < n4; g += blockDim.x) {
@@ -822,20 +836,17 @@ __global__ void __launch_bounds__(QD_THREADS) snp_digits_kernel(int n, const flo
       vl[k] = scale_ok ? vl[k] * sc : ldexpf(vl[k], se);
     }
     for (int sd = 0; sd < S; sd++) {
-      __nv_bfloat16 dg[4];
+      uint32_t pk = 0;
 #pragma unroll
       for (int k = 0; k < 4; k++) {
         const float d = rintf(vh[k]);
-        dg[k] = __float2bfloat16(d);  // |d| <= 32: exact
+        pk |= e4m3_digit(d) << (8 * k);
         float hs, he;
         two_sum_f(__fsub_rn(vh[k], d), vl[k], hs, he);
-        vh[k] = hs * 64.0f;
-        vl[k] = he * 64.0f;
+        vh[k] = hs * 32.0f;
+        vl[k] = he * 32.0f;
       }
-      uint2 pk;
-      pk.x = (uint32_t)__bfloat16_as_ushort(dg[0]) | ((uint32_t)__bfloat16_as_ushort(dg[1]) << 16);
-      pk.y = (uint32_t)__bfloat16_as_ushort(dg[2]) | ((uint32_t)__bfloat16_as_ushort(dg[3]) << 16);
-      *(uint2*)(Ad + ((long long)sd * Ncap + i) * Kpad + l) = pk;  // rows n..Kpad-1 receive zeros
+      *(uint32_t*)(Ad + ((long long)sd * Ncap + i) * Kq + l) = pk;  // rows n..Kq-1 receive zeros
     }
   }
 }
@@ -843,7 +854,7 @@ __global__ void __launch_bounds__(QD_THREADS) snp_digits_kernel(int n, const flo
 // Trait digits: CTA per trait j of d (FP64, d[l + j*n]): tau_j = 2^dexp[j] >=
 // 2 max_l d, digits of d / tau_j in FP64 at Dd[(s*QT_TP + j)*Kpad + l].
 __global__ void __launch_bounds__(256) trait_digits_kernel(int n, const double* __restrict__ d, int S, int tgp,
-                                                           int Kpad, __nv_bfloat16* __restrict__ Dd,
+                                                           int Kq, uint8_t* __restrict__ Dd,
                                                            int* __restrict__ dexp) {
   const int j = blockIdx.x;
   const double* c = d + (long long)j * n;
@@ -865,11 +876,11 @@ __global__ void __launch_bounds__(256) trait_digits_kernel(int n, const double* 
   const int e = m > 0.0 ? ilogb(m) + 2 : 0;  // 2^e >= 2 m
   if (threadIdx.x == 0) dexp[j] = e;
   for (int l = threadIdx.x; l < n; l += blockDim.x) {
-    double v = ldexp(c[l], 6 - e);
+    double v = ldexp(c[l], 5 - e);
     for (int s = 0; s < S; s++) {
-      const double dd = rint(v);
-      Dd[((long long)s * tgp + j) * Kpad + l] = __double2bfloat16(dd);
-      v = (v - dd) * 64.0;
+      const double dd = rint(v);  // |dd| <= 16
+      Dd[((long long)s * tgp + j) * Kq + l] = (uint8_t)e4m3_digit((float)dd);
+      v = (v - dd) * 32.0;
     }
   }
 }
@@ -1018,8 +1029,7 @@ EncodeTiledFn get_encoder() {
 
 // 2D BF16 tensor map, K innermost, box {box_k, box_rows}; 128B swizzle for
 // 64-element (128-byte) rows, 64B swizzle for 32-element rows.  make_map is
-// the split GEMM's operand layout (K-step GBK); the tensor-core quadratic Gram
-// uses 64-element rows (make_map_k64).
+// the split GEMM's operand layout (K-step GBK).
 cudaError_t make_map_box(CUtensorMap* m, const void* base, long long K, long long rows, int box_rows, int box_k) {
   EncodeTiledFn enc = get_encoder();
   if (!enc) return cudaErrorNotSupported;
@@ -1035,8 +1045,19 @@ cudaError_t make_map_box(CUtensorMap* m, const void* base, long long K, long lon
 cudaError_t make_map(CUtensorMap* m, const void* base, long long K, long long rows, int box_rows) {
   return make_map_box(m, base, K, rows, box_rows, GBK);
 }
-cudaError_t make_map_k64(CUtensorMap* m, const void* base, long long K, long long rows, int box_rows) {
-  return make_map_box(m, base, K, rows, box_rows, 64);
+// 2D byte tensor map (FP8 digits), K innermost in rows of K bytes, box
+// {QT_KB, box_rows}, 128B swizzle.
+cudaError_t make_map_u8(CUtensorMap* m, const void* base, long long K, long long rows, int box_rows) {
+  EncodeTiledFn enc = get_encoder();
+  if (!enc) return cudaErrorNotSupported;
+  cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)K};
+  cuuint32_t box[2] = {(cuuint32_t)QT_KB, (cuuint32_t)box_rows};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<void*>(base), dims, strides, box, es,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
 int grid_for(long long total) { return (int)std::min<long long>((total + 255) / 256, 152LL * 32); }
@@ -1063,11 +1084,12 @@ struct OzakiPlan {
   int sms = 0;                  // SM count of the device
   // tensor-core quadratic Gram (eigen, 33 <= t <= 112): digit operands
   bool tq = false;
-  int SQ = 9;                     // digits per side; pairs with s + t <= SQ + 1
+  int SQ = 11;                    // digits per side; pairs with s + t <= SQ + 1
+  int Kq = 0;                     // digit row length (bytes): n rounded up to QT_KB
   int tgp = 0;                    // trait rows per digit plane (multiple of QT_TP)
   double* qpart = nullptr;        // QT_SLOTS x Ncap x tgp partial planes of the tensor-core Gram
-  __nv_bfloat16* Adig = nullptr;  // SQ x Ncap x Kpad SNP digits
-  __nv_bfloat16* Ddig = nullptr;  // SQ x tgp x Kpad trait digits
+  uint8_t* Adig = nullptr;        // SQ x Ncap x Kq SNP digits (E4M3)
+  uint8_t* Ddig = nullptr;        // SQ x tgp x Kq trait digits (E4M3)
   int *aexp = nullptr, *dexp = nullptr;
   CUtensorMap mapAd, mapDd;
   QuadPasses qp;
@@ -1132,17 +1154,18 @@ cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_
   }
   if (p->tq && r == cudaSuccess) {
     p->tgp = (t + QT_TP - 1) / QT_TP * QT_TP;
-    const size_t na = (size_t)p->SQ * p->Ncap * p->Kpad, nd = (size_t)p->SQ * p->tgp * p->Kpad;
-    chk(cudaMalloc(&p->Adig, sizeof(__nv_bfloat16) * na));
-    chk(cudaMalloc(&p->Ddig, sizeof(__nv_bfloat16) * nd));
+    p->Kq = (n + QT_KB - 1) / QT_KB * QT_KB;
+    const size_t na = (size_t)p->SQ * p->Ncap * p->Kq, nd = (size_t)p->SQ * p->tgp * p->Kq;
+    chk(cudaMalloc(&p->Adig, na));
+    chk(cudaMalloc(&p->Ddig, nd));
     chk(cudaMalloc(&p->aexp, sizeof(int) * p->Ncap));
     chk(cudaMalloc(&p->dexp, sizeof(int) * p->tgp));
     chk(cudaMalloc(&p->qpart, sizeof(double) * QT_SLOTS * (size_t)p->Ncap * p->tgp));
-    if (r == cudaSuccess) chk(cudaMemset(p->Adig, 0, sizeof(__nv_bfloat16) * na));
-    if (r == cudaSuccess) chk(cudaMemset(p->Ddig, 0, sizeof(__nv_bfloat16) * nd));
+    if (r == cudaSuccess) chk(cudaMemset(p->Adig, 0, na));
+    if (r == cudaSuccess) chk(cudaMemset(p->Ddig, 0, nd));
     if (r == cudaSuccess) chk(cudaMemset(p->dexp, 0, sizeof(int) * p->tgp));
-    if (r == cudaSuccess) chk(make_map_k64(&p->mapAd, p->Adig, p->Kpad, (long long)p->SQ * p->Ncap, BM));
-    if (r == cudaSuccess) chk(make_map_k64(&p->mapDd, p->Ddig, p->Kpad, (long long)p->SQ * p->tgp, QT_TP));
+    if (r == cudaSuccess) chk(make_map_u8(&p->mapAd, p->Adig, p->Kq, (long long)p->SQ * p->Ncap, BM));
+    if (r == cudaSuccess) chk(make_map_u8(&p->mapDd, p->Ddig, p->Kq, (long long)p->SQ * p->tgp, QT_TP));
     if (r == cudaSuccess)
       chk(cudaFuncSetAttribute(quadtc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, QT_SMEM));
     // passes: one SNP digit s with up to four trait digits t, s + t <= SQ + 1
@@ -1218,14 +1241,14 @@ cudaError_t selfgram(OzakiPlan* p, cudaStream_t s, int col0, int xq, int t, doub
   if (!p->tq || col0 != 0)
     return quad_gram(s, p->n, xq, t, A, p->Mpad, p->amax + col0, p->D, p->n, p->dmax, p->part, GR + col0, ldg,
                      p->sms);
-  snp_digits_kernel<<<xq, QD_THREADS, 0, s>>>(p->n, A, p->Mpad, p->SQ, p->Ncap, p->Kpad, p->Adig, p->aexp);
+  snp_digits_kernel<<<xq, QD_THREADS, 0, s>>>(p->n, A, p->Mpad, p->SQ, p->Ncap, p->Kq, p->Adig, p->aexp);
   note_launch();
   QuadArgs g;
   g.x = xq;
   g.t = t;
   g.tgp = p->tgp;
   g.Ncap = p->Ncap;
-  g.Kpad = p->Kpad;
+  g.Kq = p->Kq;
   g.groups = p->tgp / QT_TP;
   const int tiles = (xq + BM - 1) / BM * g.groups;
   g.units = tiles * p->qp.n;
@@ -1255,7 +1278,7 @@ cudaError_t ozaki_set_eigen(OzakiPlan* p, cudaStream_t s, const double* Z, const
   split_pairs_kernel<<<p->t, 256, 0, s>>>(p->n, p->t, dinv, p->D, p->dmax);
   note_launch();
   if (p->tq) {
-    trait_digits_kernel<<<p->t, 256, 0, s>>>(p->n, dinv, p->SQ, p->tgp, p->Kpad, p->Ddig, p->dexp);
+    trait_digits_kernel<<<p->t, 256, 0, s>>>(p->n, dinv, p->SQ, p->tgp, p->Kq, p->Ddig, p->dexp);
     note_launch();
   }
   return cudaGetLastError();
