@@ -3,25 +3,30 @@
 //   C[r, c] = sum_k A[r, k] * G[c, k]        A FP64 (rows of Z^T, U^T or L^-1),
 //                                            G genotypes (0/1/2), K = n
 //
-// A is cut once per problem into S BF16 "digit" slices with a per-row
+// A is cut once per problem into S FP8 (E4M3) "digit" slices with a per-row
 // power-of-two scale 2^e_r:
-//   A[r, k] = 2^(e_r - 7) * sum_s d_s[r, k] * 2^(-8 s),   d_s integer in [-128, 128]
-// (round-to-nearest digits: each slice carries 8 bits, truncation error
-// <= 2^(e_r - 8 S)).  Genotypes are exact in BF16.  Every slice product
-// P_s = d_s G^T is an integer with |P_s| <= 128 * 2 * K < 2^22 for K <= 16383,
-// so FP32 accumulation in TMEM is exact and the result is bit-reproducible.
+//   A[r, k] = 2^(e_r - 4) * sum_s d_s[r, k] * 2^(-5 s),   d_s integer in [-16, 16]
+// (round-to-nearest digits: each slice carries 5 bits, truncation error
+// <= 2^(e_r - 5 S)); every such digit is exact in E4M3.  Genotypes (0/1/2)
+// are exact in E4M3 too.  Every slice product P_s = d_s G^T is an integer
+// with |P_s| <= 16 * 2 * K < 2^20 for K <= 16383, so FP32 accumulation in
+// TMEM is exact and the result is bit-reproducible.  The kind::f8f6f4 MMA
+// runs at twice the BF16 rate: 9 five-bit slices (45 bits) cost 4.5 BF16
+// slice-equivalents where 6 eight-bit BF16 slices (48 bits) cost 6.
 //
 // Kernel ozaki_gemm_kernel (one 128 x 256 output tile per CTA, 10 warps):
-//   warp 0      TMA producer: per K-step of 64, two A-slice tiles (128 x 64)
-//               and one genotype tile (256 x 64), 128B-swizzled, 3 stages.
+//   warp 0      TMA producer: per K-step of 64 bytes (64 digits), two A-slice
+//               tiles (128 x 64) and one genotype tile (256 x 64), 64B-swizzled,
+//               six 32 KB stages (the grouped launch: K-steps of 128, 128B
+//               swizzle, three 64 KB stages).
 //   warp 1      allocates 512 TMEM columns and issues tcgen05.mma
-//               (kind::f16, BF16 x BF16 -> F32, M=128 N=256 K=16): slice 2p
+//               (kind::f8f6f4, E4M3 x E4M3 -> F32, M=128 N=256 K=32): slice 2p
 //               into columns [0,256), slice 2p+1 into [256,512).
 //   warps 2-9   epilogue: tcgen05.ld the two accumulators, combine them
-//               exactly in int32 (q = P_2p * 256 + P_2p+1), Horner-accumulate
-//               the passes in int64 in the output buffer (V = V * 2^16 + q),
-//               and on the last pass write V * 2^(e_r - 15 - 16 (passes-1))
-//               as FP64.  |V| < 2^62 for S <= 6.
+//               exactly in int32 (q = P_2p * 32 + P_2p+1), Horner-accumulate
+//               the passes in int64 in the output buffer (V = V * 2^10 + q),
+//               and on the last pass write V * 2^(e_r - 9 - 10 (passes-1))
+//               as FP64.  |V| < 2^62 for S <= 9.
 // Every mbarrier wait is bounded; on expiry the kernel raises an error flag,
 // drains its own in-flight copies and MMAs (bounded), frees TMEM and exits.
 //
@@ -57,28 +62,29 @@ namespace oz {
 constexpr int BM = 128, BN = 256, BK = 64;
 constexpr int STAGES = 3;
 constexpr int A_TILE = BM * BK * 2;               // 16 KB
-// split GEMM ring for a K-step KB (32: 64-byte rows, 64B swizzle, 6 stages of
-// 32 KB; 64: 128-byte rows, 128B swizzle, 3 stages of 64 KB).  The smaller
+// split GEMM ring for a K-step of KB one-byte digits (64: 64-byte rows, 64B
+// swizzle, 6 stages of 32 KB; 128: 128-byte rows, 128B swizzle, 3 stages of
+// 64 KB).  The smaller
 // stages keep more bytes in flight per SM for the same shared memory (the MMA
 // thread waits on stage arrivals, not on L2 bandwidth): 10.72 against
 // 11.20 ms per launch at n = 10000, x_b = 16384.  The grouped launch, whose
 // small cohorts have short K, stays at KB = 64 (32.3 against 32.8 ms per
 // step of the 64-cohort batch).
 #ifndef FGLS_GEMM_BK
-#define FGLS_GEMM_BK 32
+#define FGLS_GEMM_BK 64
 #endif
 #ifndef FGLS_GROUPED_BK
-#define FGLS_GROUPED_BK 64
+#define FGLS_GROUPED_BK 128
 #endif
-#ifndef FGLS_GEMM_STAGES32
-#define FGLS_GEMM_STAGES32 6
+#ifndef FGLS_GEMM_STAGES64
+#define FGLS_GEMM_STAGES64 6
 #endif
 template <int KB>
 struct GemmRing {
-  static_assert(KB == 64 || KB == 32, "K-step of the split GEMM");
-  static constexpr int STAGES = KB == 64 ? 3 : FGLS_GEMM_STAGES32;
-  static constexpr int A = BM * KB * 2;
-  static constexpr int B = BN * KB * 2;
+  static_assert(KB == 128 || KB == 64, "K-step of the split GEMM (one-byte digits)");
+  static constexpr int STAGES = KB == 128 ? 3 : FGLS_GEMM_STAGES64;
+  static constexpr int A = BM * KB;
+  static constexpr int B = BN * KB;
   static constexpr int STAGE = 2 * A + B;
   static constexpr int SMEM = STAGES * STAGE + 1024 + 256;
 };
@@ -87,13 +93,14 @@ constexpr int GRBK = FGLS_GROUPED_BK;     // grouped launch
 constexpr int SMEM_BYTES = GemmRing<GBK>::SMEM;
 constexpr int GROUPED_SMEM_BYTES = GemmRing<GRBK>::SMEM;
 constexpr int THREADS = 320;  // producer, MMA, 8 epilogue warps
-constexpr int MAX_SLICES = 6;
+constexpr int MAX_SLICES = 9;   // FP8 digit slices; |V| < 2^62 in the epilogue
+constexpr int DEFAULT_SLICES = 9;
+constexpr int KALIGN = 128;     // K padding of the FP8 operands (one 128-byte row)
 constexpr int GROUP_M = 8;
 
-// tcgen05.mma instruction descriptor, kind::f16: D=F32, A=B=BF16, both
-// K-major, N=256, M=128.
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                           ((uint32_t)(BM >> 4) << 24);
+// tcgen05.mma instruction descriptor, kind::f8f6f4: D=F32, A=B=E4M3
+// (format 0), both K-major, N=256, M=128.
+constexpr uint32_t IDESC = (1u << 4) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -185,7 +192,7 @@ __device__ __forceinline__ uint64_t desc_sw64(const void* p) {
   return d;
 }
 template <int KB>
-__device__ __forceinline__ uint64_t desc_gemm(const void* p) { return KB == 64 ? desc_sw128(p) : desc_sw64(p); }
+__device__ __forceinline__ uint64_t desc_gemm(const void* p) { return KB == 128 ? desc_sw128(p) : desc_sw64(p); }
 
 __device__ __forceinline__ void mma_bf16(uint32_t dt, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
   asm volatile(
@@ -231,7 +238,7 @@ struct GemmArgs {
   int S;            // slices (1..MAX_SLICES)
   int tiles_m, tiles_n;
   int tri_rows;     // rows [0, tri_rows) of A are lower triangular in K (0: none)
-  const double* row_scale;  // per row 2^(e_r - 15 - 16 (passes-1))
+  const double* row_scale;  // per row 2^(e_r - 9 - 10 (passes-1))
   double* C;        // output, column-major, ld = ldc (int64 between passes)
   long long ldc;
   int col0;         // first genotype column of this launch (TMA row offset of G)
@@ -387,11 +394,11 @@ __device__ __forceinline__ void gemm_tile(const CUtensorMap* tmA, const CUtensor
           uint8_t* sb = smem + stage * R::STAGE;
           const uint64_t a0 = desc_gemm<KB>(sb), a1 = desc_gemm<KB>(sb + R::A), b = desc_gemm<KB>(sb + 2 * R::A);
 #pragma unroll
-          for (int k = 0; k < KB / 16; k++) {
+          for (int k = 0; k < KB / 32; k++) {  // K = 32 one-byte digits (32 bytes) per MMA
             const uint64_t koff = (uint64_t)((k * 32) >> 4);
             const uint32_t acc = (kb > 0 || k > 0) ? 1u : 0u;
-            mma_bf16(tbase, a0 + koff, b + koff, IDESC, acc);
-            if (two) mma_bf16(tbase + 256, a1 + koff, b + koff, IDESC, acc);
+            mma_f8(tbase, a0 + koff, b + koff, IDESC, acc);
+            if (two) mma_f8(tbase + 256, a1 + koff, b + koff, IDESC, acc);
           }
           any = true;
           mma_commit(&empty[stage]);
@@ -451,10 +458,10 @@ __device__ __forceinline__ void gemm_tile(const CUtensorMap* tmA, const CUtensor
 #pragma unroll
         for (int j = 0; j < 32; j++) {
           if (c0 + j >= cend) break;
-          int qv = exact_f2i(__uint_as_float(v0[j])) * 256;
+          int qv = exact_f2i(__uint_as_float(v0[j])) * 32;
           if (two) qv += exact_f2i(__uint_as_float(v1[j]));
           long long* cp = crow + (long long)(c0 + j) * g.ldc;
-          const long long V = (p == 0) ? (long long)qv : prev[j] * 65536LL + (long long)qv;
+          const long long V = (p == 0) ? (long long)qv : prev[j] * 1024LL + (long long)qv;
           if (!last)
             *cp = V;
           else if (sq)
@@ -891,7 +898,7 @@ __global__ void __launch_bounds__(256) trait_digits_kernel(int n, const double* 
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) slice_rows_kernel(int K, int rows, const double* __restrict__ src,
                                                          long long lds, int row_off, int S, int Mpad, int Kpad,
-                                                         __nv_bfloat16* __restrict__ A, double* __restrict__ row_scale) {
+                                                         uint8_t* __restrict__ A, double* __restrict__ row_scale) {
   const int r = blockIdx.x;
   if (r >= rows) return;
   const double* a = src + (long long)r * lds;
@@ -913,47 +920,55 @@ __global__ void __launch_bounds__(256) slice_rows_kernel(int K, int rows, const 
   const int e = (mx > 0.0) ? ilogb(mx) + 1 : 0;  // max * 2^-e in [0.5, 1)
   const int passes = (S + 1) / 2;
   const int R = row_off + r;
-  if (threadIdx.x == 0) row_scale[R] = ldexp(1.0, e - 15 - 16 * (passes - 1));
+  if (threadIdx.x == 0) row_scale[R] = ldexp(1.0, e - 9 - 10 * (passes - 1));
   for (int k = threadIdx.x; k < K; k += blockDim.x) {
-    double v = ldexp(a[k], 7 - e);  // |v| < 128
+    double v = ldexp(a[k], 4 - e);  // |v| < 16
 #pragma unroll 1
     for (int s = 0; s < S; s++) {
       const double d = rint(v);
-      A[((long long)s * Mpad + R) * Kpad + k] = __double2bfloat16(d);  // |d| <= 128: exact
-      v = (v - d) * 256.0;
+      A[((long long)s * Mpad + R) * Kpad + k] = (uint8_t)e4m3_digit((float)d);  // |d| <= 16: exact
+      v = (v - d) * 32.0;
     }
   }
 }
 
 // genotypes (FP64 or bytes, column c at src[c*lds + k]) -> BF16 [c*Kpad + k]
 // Genotype value -> BF16 (exact for hard calls 0/1/2).
-__device__ __forceinline__ __nv_bfloat16 geno_bf16(unsigned char v) { return __float2bfloat16((float)v); }
-__device__ __forceinline__ __nv_bfloat16 geno_bf16(double v) { return __float2bfloat16((float)v); }
+// genotypes as E4M3 bytes (hard calls 0/1/2 are exact)
+__device__ __forceinline__ uint8_t geno_f8(unsigned char v) {
+  return (uint8_t)__nv_cvt_float_to_fp8((float)v, __NV_SATFINITE, __NV_E4M3);
+}
+__device__ __forceinline__ uint8_t geno_f8(double v) {
+  return (uint8_t)__nv_cvt_float_to_fp8((float)v, __NV_SATFINITE, __NV_E4M3);
+}
+__device__ __forceinline__ uint16_t geno_f8x2(double a, double b) {
+  return (uint16_t)__nv_cvt_float2_to_fp8x2(make_float2((float)a, (float)b), __NV_SATFINITE, __NV_E4M3);
+}
 
 // One CTA per genotype column (no 64-bit index division per element).  FP64
-// columns that start on a 16-byte boundary move as 16-byte pairs into 4-byte
-// BF16 pairs; rows K .. Kpad-1 of G stay zero from its allocation.
+// columns that start on a 16-byte boundary move as 16-byte pairs into 2-byte
+// E4M3 pairs; rows K .. Kpad-1 of G stay zero from its allocation.
 template <typename T>
 __global__ void __launch_bounds__(256) genotypes_bf16_kernel(int K, int cols, const T* __restrict__ src,
-                                                             long long lds, __nv_bfloat16* __restrict__ G,
+                                                             long long lds, uint8_t* __restrict__ G,
                                                              int Kpad) {
   const long long c = blockIdx.x;
   const T* col = src + c * lds;
-  __nv_bfloat16* g = G + c * Kpad;
+  uint8_t* g = G + c * Kpad;
   if constexpr (sizeof(T) == 8) {
     if (((uintptr_t)col & 15) == 0) {
       const double2* col2 = (const double2*)col;
-      __nv_bfloat162* g2 = (__nv_bfloat162*)g;
+      uint16_t* g2 = (uint16_t*)g;
       const int K2 = K >> 1;
       for (int k = threadIdx.x; k < K2; k += blockDim.x) {
         const double2 v = col2[k];
-        g2[k] = __halves2bfloat162(geno_bf16(v.x), geno_bf16(v.y));
+        g2[k] = geno_f8x2(v.x, v.y);
       }
-      if ((K & 1) && threadIdx.x == 0) g[K - 1] = geno_bf16(col[K - 1]);
+      if ((K & 1) && threadIdx.x == 0) g[K - 1] = geno_f8(col[K - 1]);
       return;
     }
   }
-  for (int k = threadIdx.x; k < K; k += blockDim.x) g[k] = geno_bf16(col[k]);
+  for (int k = threadIdx.x; k < K; k += blockDim.x) g[k] = geno_f8(col[k]);
 }
 
 __global__ void eye_kernel(int n, double* A) {
@@ -1027,18 +1042,18 @@ EncodeTiledFn get_encoder() {
   return fn;
 }
 
-// 2D BF16 tensor map, K innermost, box {box_k, box_rows}; 128B swizzle for
-// 64-element (128-byte) rows, 64B swizzle for 32-element rows.  make_map is
-// the split GEMM's operand layout (K-step GBK).
+// 2D byte (E4M3) tensor map, K innermost, box {box_k, box_rows}; 128B
+// swizzle for 128-byte rows, 64B swizzle for 64-byte rows.  make_map is the
+// split GEMM's operand layout (K-step GBK).
 cudaError_t make_map_box(CUtensorMap* m, const void* base, long long K, long long rows, int box_rows, int box_k) {
   EncodeTiledFn enc = get_encoder();
   if (!enc) return cudaErrorNotSupported;
   cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)K * 2};
+  cuuint64_t strides[1] = {(cuuint64_t)K};
   cuuint32_t box[2] = {(cuuint32_t)box_k, (cuuint32_t)box_rows};
   cuuint32_t es[2] = {1, 1};
-  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, box_k == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<void*>(base), dims, strides, box, es,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, box_k == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
@@ -1072,8 +1087,8 @@ struct OzakiPlan {
   int nU = 0;           // U rows appended below the n rows of Z^T / L^-1
   int M = 0, Mpad = 0;  // rows of A
   int Kpad = 0, Ncap = 0;
-  __nv_bfloat16* A = nullptr;   // S x Mpad x Kpad
-  __nv_bfloat16* G = nullptr;   // Ncap x Kpad
+  uint8_t* A = nullptr;         // S x Mpad x Kpad E4M3 digit slices
+  uint8_t* G = nullptr;         // Ncap x Kpad E4M3 genotypes
   double* scale = nullptr;      // Mpad
   double* C = nullptr;          // Mpad x Ncap (ld Mpad)
   double* U = nullptr;          // n x nU
@@ -1111,19 +1126,19 @@ cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_
   p->wXL = wXL;
   p->wXR = wXR;
   p->x_b = x_b;
-  p->S = slices > 0 ? std::min(slices, MAX_SLICES) : 6;
+  p->S = slices > 0 ? std::min(slices, MAX_SLICES) : DEFAULT_SLICES;
   p->eigen = eigen;
   p->nU = eigen ? t * (1 + wXL) : (1 + wXL);
   p->M = n + p->nU;
   p->Mpad = (p->M + BM - 1) / BM * BM;
-  p->Kpad = (n + BK - 1) / BK * BK;
+  p->Kpad = (n + KALIGN - 1) / KALIGN * KALIGN;
   p->Ncap = (x_b + BN - 1) / BN * BN;
   cudaError_t r = cudaSuccess;
   auto chk = [&](cudaError_t e) {
     if (r == cudaSuccess) r = e;
   };
-  chk(cudaMalloc(&p->A, sizeof(__nv_bfloat16) * (size_t)p->S * p->Mpad * p->Kpad));
-  chk(cudaMalloc(&p->G, sizeof(__nv_bfloat16) * (size_t)p->Ncap * p->Kpad));
+  chk(cudaMalloc(&p->A, (size_t)p->S * p->Mpad * p->Kpad));
+  chk(cudaMalloc(&p->G, (size_t)p->Ncap * p->Kpad));
   chk(cudaMalloc(&p->scale, sizeof(double) * p->Mpad));
   chk(cudaMalloc(&p->C, sizeof(double) * (size_t)p->Mpad * p->Ncap));
   chk(cudaMalloc(&p->U, sizeof(double) * (size_t)n * p->nU));
@@ -1139,8 +1154,8 @@ cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_
   chk(cudaMalloc(&p->err, sizeof(int)));
   if (!eigen) chk(cudaMalloc(&p->Linv, sizeof(double) * (size_t)n * n));
   if (!eigen) chk(cudaMalloc(&p->LinvT, sizeof(double) * (size_t)n * n));
-  if (r == cudaSuccess) chk(cudaMemset(p->A, 0, sizeof(__nv_bfloat16) * (size_t)p->S * p->Mpad * p->Kpad));
-  if (r == cudaSuccess) chk(cudaMemset(p->G, 0, sizeof(__nv_bfloat16) * (size_t)p->Ncap * p->Kpad));
+  if (r == cudaSuccess) chk(cudaMemset(p->A, 0, (size_t)p->S * p->Mpad * p->Kpad));
+  if (r == cudaSuccess) chk(cudaMemset(p->G, 0, (size_t)p->Ncap * p->Kpad));
   if (r == cudaSuccess) chk(cudaMemset(p->scale, 0, sizeof(double) * p->Mpad));
   if (r == cudaSuccess) chk(cudaMemset(p->err, 0, sizeof(int)));
   if (r == cudaSuccess) chk(make_map(&p->mapA, p->A, p->Kpad, (long long)p->S * p->Mpad, BM));
@@ -1362,11 +1377,11 @@ int ozaki_read_error(OzakiPlan* p) {
 // grouped genotype conversion and the grouped split GEMM.
 // ---------------------------------------------------------------------------
 int split_rows_padded(int rows) { return (rows + BM - 1) / BM * BM; }
-int split_k_padded(int n) { return (n + BK - 1) / BK * BK; }
+int split_k_padded(int n) { return (n + KALIGN - 1) / KALIGN * KALIGN; }
 int split_cols_padded(int x) { return (x + BN - 1) / BN * BN; }
 
 cudaError_t split_chol_operand(cudaStream_t s, int n, int wXL, const double* L, const double* WY, int S, int Mpad,
-                               int Kpad, __nv_bfloat16* A, double* scale, double* Linv, double* LinvT, double* U) {
+                               int Kpad, uint8_t* A, double* scale, double* Linv, double* LinvT, double* U) {
   const int nU = 1 + wXL;
   FGLS_CUDA_TRY(lower_inverse(s, n, L, Linv));
   FGLS_CUDA_TRY(dgemm(s, true, false, n, nU, n, 1.0, Linv, n, WY, n, 0.0, U, n));
@@ -1385,7 +1400,7 @@ namespace {
 // S_built slices: 2^(e - 15 - 16 (passes - 1)) depends on the pass count only
 __global__ void rescale_rows_kernel(int rows, const double* __restrict__ built, int dpass, double* __restrict__ out) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r < rows) out[r] = ldexp(built[r], 16 * dpass);
+  if (r < rows) out[r] = ldexp(built[r], 10 * dpass);
 }
 
 template <typename T>
@@ -1393,25 +1408,25 @@ __global__ void grouped_genotypes_kernel(const GenoCohort* __restrict__ gc, cons
   const int c = blockIdx.y;
   const int x = sc[c].x, n = gc[c].n, Kpad = gc[c].Kpad;
   const T* __restrict__ src = (const T*)sc[c].X;
-  __nv_bfloat16* __restrict__ G = gc[c].G;
+  uint8_t* __restrict__ G = gc[c].G;
   // columns strided over the CTAs of this cohort, rows over the threads; u8
   // columns that start on a 4-byte boundary move 4 calls per load
   for (int col = blockIdx.x; col < x; col += gridDim.x) {
     const T* s = src + (long long)col * n;
-    __nv_bfloat16* g = G + (long long)col * Kpad;
+    uint8_t* g = G + (long long)col * Kpad;
     if constexpr (sizeof(T) == 1) {
       if (((uintptr_t)s & 3) == 0) {
         const int n4 = n >> 2;
         for (int q = threadIdx.x; q < n4; q += blockDim.x) {
           const uchar4 v = ((const uchar4*)s)[q];
-          ((__nv_bfloat162*)g)[2 * q] = __halves2bfloat162(geno_bf16(v.x), geno_bf16(v.y));
-          ((__nv_bfloat162*)g)[2 * q + 1] = __halves2bfloat162(geno_bf16(v.z), geno_bf16(v.w));
+          ((uint32_t*)g)[q] = (uint32_t)geno_f8(v.x) | ((uint32_t)geno_f8(v.y) << 8) |
+                              ((uint32_t)geno_f8(v.z) << 16) | ((uint32_t)geno_f8(v.w) << 24);
         }
-        for (int k = 4 * n4 + threadIdx.x; k < n; k += blockDim.x) g[k] = geno_bf16(s[k]);
+        for (int k = 4 * n4 + threadIdx.x; k < n; k += blockDim.x) g[k] = geno_f8(s[k]);
         continue;
       }
     }
-    for (int k = threadIdx.x; k < n; k += blockDim.x) g[k] = geno_bf16(s[k]);
+    for (int k = threadIdx.x; k < n; k += blockDim.x) g[k] = geno_f8(s[k]);
   }
 }
 }  // namespace
@@ -1540,7 +1555,7 @@ extern "C" int fglsgpu_selftest_split_gemm(int M, int K, int N, int S, const dou
   p.S = S;
   p.M = M;
   p.Mpad = (M + BM - 1) / BM * BM;
-  p.Kpad = (K + BK - 1) / BK * BK;
+  p.Kpad = (K + KALIGN - 1) / KALIGN * KALIGN;
   p.Ncap = (N + BN - 1) / BN * BN;
   double *dA = nullptr, *dX = nullptr;
   cudaError_t r = cudaSuccess;
@@ -1549,15 +1564,15 @@ extern "C" int fglsgpu_selftest_split_gemm(int M, int K, int N, int S, const dou
   };
   cudaStream_t s = nullptr;
   chk(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-  chk(cudaMalloc(&p.A, sizeof(__nv_bfloat16) * (size_t)S * p.Mpad * p.Kpad));
-  chk(cudaMalloc(&p.G, sizeof(__nv_bfloat16) * (size_t)p.Ncap * p.Kpad));
+  chk(cudaMalloc(&p.A, (size_t)S * p.Mpad * p.Kpad));
+  chk(cudaMalloc(&p.G, (size_t)p.Ncap * p.Kpad));
   chk(cudaMalloc(&p.scale, sizeof(double) * p.Mpad));
   chk(cudaMalloc(&p.C, sizeof(double) * (size_t)p.Mpad * p.Ncap));
   chk(cudaMalloc(&p.err, sizeof(int)));
   chk(cudaMalloc(&dA, sizeof(double) * (size_t)M * K));
   chk(cudaMalloc(&dX, sizeof(double) * (size_t)K * N));
-  if (r == cudaSuccess) chk(cudaMemset(p.A, 0, sizeof(__nv_bfloat16) * (size_t)S * p.Mpad * p.Kpad));
-  if (r == cudaSuccess) chk(cudaMemset(p.G, 0, sizeof(__nv_bfloat16) * (size_t)p.Ncap * p.Kpad));
+  if (r == cudaSuccess) chk(cudaMemset(p.A, 0, (size_t)S * p.Mpad * p.Kpad));
+  if (r == cudaSuccess) chk(cudaMemset(p.G, 0, (size_t)p.Ncap * p.Kpad));
   if (r == cudaSuccess) chk(cudaMemset(p.scale, 0, sizeof(double) * p.Mpad));
   if (r == cudaSuccess) chk(cudaMemset(p.err, 0, sizeof(int)));
   if (r == cudaSuccess) chk(cudaMemcpy(dA, A, sizeof(double) * (size_t)M * K, cudaMemcpyHostToDevice));
@@ -1595,12 +1610,12 @@ extern "C" int fglsgpu_selftest_split_gemm(int M, int K, int N, int S, const dou
 // pool (a raw cudaMalloc would bypass its accounting and can fail once the
 // pool has reserved the memory), and code that must not change the device's
 // memory footprint between steps.  They pass device buffers for the inputs
-// and the output; the kernel's scratch (BF16 slices of A, the BF16 genotype
+// and the output; the kernel's scratch (E4M3 slices of A, the E4M3 genotype
 // operand, per-row scales, an error word) lives in the file-scope array below,
 // which every GPU that loads this library holds until the process exits.
 //
-// Limits (the array's size, 8.4 MB): M <= 256, K <= 2048, N <= 512,
-// slices <= 6.  Every call shares the array and leaves its contents behind;
+// Limits (the array's size, 5.8 MB): M <= 256, K <= 2048, N <= 512,
+// slices <= 9.  Every call shares the array and leaves its contents behind;
 // calls that overlap on the GPU (several streams or threads at once) race on
 // it and must be serialised by the caller.  The first call on a device looks
 // up the array's device address (cudaGetSymbolAddress) with that device
@@ -1609,8 +1624,8 @@ extern "C" int fglsgpu_selftest_split_gemm(int M, int K, int N, int S, const dou
 namespace fgls {
 namespace oz {
 constexpr int NA_MAX_M = 256, NA_MAX_K = 2048, NA_MAX_N = 512, NA_MAX_S = MAX_SLICES;
-constexpr size_t NA_A_BYTES = (size_t)NA_MAX_S * NA_MAX_M * NA_MAX_K * 2;   // BF16 slices
-constexpr size_t NA_G_BYTES = (size_t)NA_MAX_N * NA_MAX_K * 2;              // BF16 genotypes
+constexpr size_t NA_A_BYTES = (size_t)NA_MAX_S * NA_MAX_M * NA_MAX_K;   // E4M3 slices
+constexpr size_t NA_G_BYTES = (size_t)NA_MAX_N * NA_MAX_K;              // E4M3 genotypes
 constexpr size_t NA_SCALE_BYTES = (size_t)NA_MAX_M * 8;                     // row scales
 constexpr size_t NA_BYTES = NA_A_BYTES + NA_G_BYTES + NA_SCALE_BYTES + 256;  // + error word
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
@@ -1645,10 +1660,10 @@ extern "C" int fglsgpu_split_gemm_noalloc(int M, int K, int N, int slices, const
   p.S = slices;
   p.M = M;
   p.Mpad = (M + BM - 1) / BM * BM;
-  p.Kpad = (K + BK - 1) / BK * BK;
+  p.Kpad = (K + KALIGN - 1) / KALIGN * KALIGN;
   p.Ncap = (N + BN - 1) / BN * BN;
-  p.A = (__nv_bfloat16*)base;
-  p.G = (__nv_bfloat16*)(base + NA_A_BYTES);
+  p.A = (uint8_t*)base;
+  p.G = (uint8_t*)(base + NA_A_BYTES);
   p.scale = (double*)(base + NA_A_BYTES + NA_G_BYTES);
   p.err = (int*)(base + NA_A_BYTES + NA_G_BYTES + NA_SCALE_BYTES);
   cudaStream_t s = (cudaStream_t)stream;
@@ -1658,8 +1673,8 @@ extern "C" int fglsgpu_split_gemm_noalloc(int M, int K, int N, int slices, const
   };
   // the array keeps the previous call's contents: zero what must start at zero
   // (slice and genotype padding, scales of padding rows, the error word)
-  chk(cudaMemsetAsync(p.A, 0, sizeof(__nv_bfloat16) * (size_t)slices * p.Mpad * p.Kpad, s));
-  chk(cudaMemsetAsync(p.G, 0, sizeof(__nv_bfloat16) * (size_t)p.Ncap * p.Kpad, s));
+  chk(cudaMemsetAsync(p.A, 0, (size_t)slices * p.Mpad * p.Kpad, s));
+  chk(cudaMemsetAsync(p.G, 0, (size_t)p.Ncap * p.Kpad, s));
   chk(cudaMemsetAsync(p.scale, 0, sizeof(double) * p.Mpad, s));
   chk(cudaMemsetAsync(p.err, 0, sizeof(int), s));
   if (r == cudaSuccess) chk(make_map(&p.mapA, p.A, p.Kpad, (long long)slices * p.Mpad, BM));

@@ -72,8 +72,9 @@ typedef struct fglsgpu_engine fglsgpu_engine;
 #define FGLSGPU_VARIANT_EIGEN 1 /* eigenbasis of Phi, all traits per block (fgls_eigen) */
 
 #define FGLSGPU_PREC_FP64 0     /* all-FP64 arithmetic                       */
-#define FGLSGPU_PREC_SPLIT 1    /* bulk GEMMs as BF16 slices on tcgen05 tensor cores,
-                                   FP32 accumulation, FP64 recombination      */
+#define FGLSGPU_PREC_SPLIT 1    /* bulk GEMMs as 5-bit digit slices (FP8 E4M3) on
+                                   tcgen05 tensor cores, exact FP32 accumulation,
+                                   integer / FP64 recombination               */
 
 typedef struct {
   int n;         /* individuals                                  */
@@ -83,7 +84,8 @@ typedef struct {
   int x_b;       /* maximum SNPs per block                       */
   int variant;   /* FGLSGPU_VARIANT_*                            */
   int precision; /* FGLSGPU_PREC_*                               */
-  int slices;    /* split precision: BF16 slices of the FP64 operand (0 = automatic) */
+  int slices;    /* split precision: 5-bit digit slices of the FP64 operand, 1..9
+                    (0 = 9, about 45 bits)                        */
   int device;    /* CUDA device ordinal                          */
   int reserved;
 } fglsgpu_config;
@@ -244,7 +246,7 @@ int fglsgpu_version(void);
 
 /* Diagnostic: runs the split-precision tensor-core GEMM used by
  * FGLSGPU_PREC_SPLIT on caller data.  C = A * X^T with A M x K (row-major
- * FP64, cut into `slices` BF16 slices, 1..6), X K x N (column-major, integer
+ * FP64, cut into `slices` 5-bit digit slices, 1..9), X K x N (column-major, integer
  * genotypes 0..2) and C M x N column-major, all host pointers; K <= 16383.
  * No counterpart in the reference (its GEMMs are FP64 BLAS calls). */
 int fglsgpu_selftest_split_gemm(int M, int K, int N, int slices, const double *A, const double *X,
@@ -255,9 +257,9 @@ int fglsgpu_selftest_split_gemm(int M, int K, int N, int slices, const double *A
  * own memory pool, or that must keep the device's footprint fixed).  All
  * pointers are DEVICE pointers owned by the caller: A (M x K, row-major
  * FP64), X (K x N, column-major genotypes), C (M x N, column-major FP64 out).
- * The kernel's scratch lives in a fixed 8.4 MB array inside the library
+ * The kernel's scratch lives in a fixed 5.8 MB array inside the library
  * (held by every GPU that loads it): M <= 256, K <= 2048, N <= 512,
- * slices <= 6, else FGLSGPU_EINVAL.  Runs on `stream` (a cudaStream_t, NULL
+ * slices <= 9, else FGLSGPU_EINVAL.  Runs on `stream` (a cudaStream_t, NULL
  * for the default stream) and returns after it finished.  Calls share the
  * array: calls that overlap on the GPU race; serialise them.  The first call
  * on a device sets up the array's address and should come before any stream
@@ -290,7 +292,7 @@ typedef struct {
 
 typedef struct {
   int x_b;          /* SNPs per cohort per step (0: autotune)             */
-  int slices;       /* BF16 slices 3..6 (0: autotune)                     */
+  int slices;       /* 5-bit digit slices 3..9 (0: autotune)              */
   int device;       /* CUDA device ordinal                                */
   int use_graph;    /* 1: replay each step from a captured CUDA graph     */
   int genotypes_u8; /* 1: genotype blocks are bytes, 0: FP64              */

@@ -36,7 +36,7 @@ def _noalloc(A, X, slices):
 def test_noalloc_matches_allocating_entry_point_twice():
     from fgls_gb300.engine import split_gemm_selftest
     rng = np.random.default_rng(42)
-    cases = [(256, 2048, 512, 6), (77, 300, 129, 4)]  # maximum sizes, then a smaller ragged call
+    cases = [(256, 2048, 512, 9), (77, 300, 129, 6)]  # maximum sizes, then a smaller ragged call
     for M, K, N, S in cases:
         A = rng.standard_normal((M, K)) * np.exp(rng.uniform(-3, 3, size=(M, 1)))
         X = rng.integers(0, 3, size=(K, N)).astype(np.float64)
@@ -45,11 +45,11 @@ def test_noalloc_matches_allocating_entry_point_twice():
         assert np.all(np.isfinite(got))
         # same kernels and arithmetic: identical bits (tolerance 0)
         np.testing.assert_array_equal(got, ref)
-        assert np.all(np.abs(got - A @ X) <= 2.0 ** (-8 * S + 4) * (np.abs(A) @ X) + 1e-300)
+        assert np.all(np.abs(got - A @ X) <= 2.0 ** (-5 * S + 4) * (np.abs(A) @ X) + 1e-300)  # 5-bit digits
 
 
 def test_noalloc_rejects_sizes_beyond_its_array():
     from fgls_gb300.engine import EINVAL, lib
     L = lib()
-    for M, K, N, S in [(257, 64, 64, 2), (64, 2049, 64, 2), (64, 64, 513, 2), (64, 64, 64, 7)]:
+    for M, K, N, S in [(257, 64, 64, 2), (64, 2049, 64, 2), (64, 64, 513, 2), (64, 64, 64, 10)]:
         assert L.fglsgpu_split_gemm_noalloc(M, K, N, S, C.c_void_p(1), C.c_void_p(1), C.c_void_p(1), None) == EINVAL
