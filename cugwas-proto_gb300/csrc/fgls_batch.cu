@@ -47,21 +47,21 @@ using namespace fgls;
 
 namespace {
 
-constexpr int S_BUILT = 9;     // E4M3 digit slices cut at setup; fewer may be used
+constexpr int S_BUILT = 6;     // BF16 eight-bit digit slices cut at setup; fewer may be used
 constexpr int PROBE = 256;     // SNPs of the autotuning probe block
 constexpr int XB_MAX = 8192;   // largest autotuned SNP block
 
 struct Cohort {
   int n = 0, wXL = 0, p = 0, t = 0;
   int Kpad = 0, Ncap = 0;
-  uint8_t* G = nullptr;           // E4M3 genotype operand (Ncap x Kpad)
+  __nv_bfloat16* G = nullptr;     // BF16 genotype operand (Ncap x Kpad)
   unsigned char* probe = nullptr; // PROBE x n hashed genotypes
 };
 
 struct Problem {
   int c = 0, j = 0;
   int M = 0, Mpad = 0;
-  uint8_t* A = nullptr;        // S_BUILT x Mpad x Kpad E4M3 slices
+  __nv_bfloat16* A = nullptr;  // S_BUILT x Mpad x Kpad BF16 digit slices
   double* scale6 = nullptr;    // row scales of the S_BUILT-slice cut
   double* scale = nullptr;     // row scales for the slices in use
   double* top = nullptr;       // null model (wXL + wXL^2 + 1)
@@ -531,7 +531,7 @@ int fglsgpu_batch_create(const fglsgpu_cohort* cohorts, int count, const fglsgpu
     nmax = std::max(nmax, k.n);
     wmax = std::max(wmax, k.wXL);
     B_CHECK(dalloc(&k.G, (size_t)k.Ncap * k.Kpad), "genotype operand");
-    B_CHECK(cudaMemset(k.G, 0, (size_t)k.Ncap * k.Kpad), "genotype operand");
+    B_CHECK(cudaMemset(k.G, 0, sizeof(__nv_bfloat16) * (size_t)k.Ncap * k.Kpad), "genotype operand");
     B_CHECK(dalloc(&k.probe, (size_t)PROBE * k.n), "probe block");
     for (int j = 0; j < k.t; j++) {
       Problem q;
@@ -545,7 +545,7 @@ int fglsgpu_batch_create(const fglsgpu_cohort* cohorts, int count, const fglsgpu
   for (auto& q : b->pr) {
     const Cohort& k = b->co[q.c];
     B_CHECK(dalloc(&q.A, (size_t)S_BUILT * q.Mpad * k.Kpad), "split operand");
-    B_CHECK(cudaMemset(q.A, 0, (size_t)S_BUILT * q.Mpad * k.Kpad), "split operand");
+    B_CHECK(cudaMemset(q.A, 0, sizeof(__nv_bfloat16) * (size_t)S_BUILT * q.Mpad * k.Kpad), "split operand");
     B_CHECK(dalloc(&q.scale6, q.Mpad), "row scales");
     B_CHECK(cudaMemset(q.scale6, 0, sizeof(double) * q.Mpad), "row scales");
     B_CHECK(dalloc(&q.scale, q.Mpad), "row scales");

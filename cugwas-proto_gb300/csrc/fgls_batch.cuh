@@ -1,5 +1,6 @@
 // Shared device-side tables of the batched-cohort path (fgls_batch.cu).
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -17,7 +18,7 @@ struct StepCohort {
 
 // Per cohort, fixed: BF16 genotype operand of the split GEMM.
 struct GenoCohort {
-  uint8_t* G;  // E4M3, Ncap x Kpad, column c at G + c*Kpad
+  __nv_bfloat16* G;  // Ncap x Kpad, column c at G + c*Kpad
   int n, Kpad;
 };
 

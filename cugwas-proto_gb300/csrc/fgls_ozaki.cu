@@ -74,24 +74,28 @@ constexpr int A_TILE = BM * BK * 2;               // 16 KB
 #define FGLS_GEMM_BK 64
 #endif
 #ifndef FGLS_GROUPED_BK
-#define FGLS_GROUPED_BK 128
+#define FGLS_GROUPED_BK 64
 #endif
 #ifndef FGLS_GEMM_STAGES64
 #define FGLS_GEMM_STAGES64 6
 #endif
-template <int KB>
+// Operand formats: FP8 E4M3 five-bit digits (single-problem launches) or
+// BF16 eight-bit digits (grouped launches, whose short-K tiles favour three
+// slice-pair passes over five).  KB counts digits per K-step, ESZ their bytes.
+template <int KB, int ESZ>
 struct GemmRing {
-  static_assert(KB == 128 || KB == 64, "K-step of the split GEMM (one-byte digits)");
-  static constexpr int STAGES = KB == 128 ? 3 : FGLS_GEMM_STAGES64;
-  static constexpr int A = BM * KB;
-  static constexpr int B = BN * KB;
+  static constexpr int ROW = KB * ESZ;  // bytes of one K-step row
+  static_assert(ROW == 128 || ROW == 64, "K-step of the split GEMM");
+  static constexpr int STAGES = ROW == 128 ? 3 : FGLS_GEMM_STAGES64;
+  static constexpr int A = BM * ROW;
+  static constexpr int B = BN * ROW;
   static constexpr int STAGE = 2 * A + B;
   static constexpr int SMEM = STAGES * STAGE + 1024 + 256;
 };
 constexpr int GBK = FGLS_GEMM_BK;         // single-problem launch
 constexpr int GRBK = FGLS_GROUPED_BK;     // grouped launch
-constexpr int SMEM_BYTES = GemmRing<GBK>::SMEM;
-constexpr int GROUPED_SMEM_BYTES = GemmRing<GRBK>::SMEM;
+constexpr int SMEM_BYTES = GemmRing<GBK, 1>::SMEM;          // FP8 digits
+constexpr int GROUPED_SMEM_BYTES = GemmRing<GRBK, 2>::SMEM;  // BF16 digits
 constexpr int THREADS = 320;  // producer, MMA, 8 epilogue warps
 constexpr int MAX_SLICES = 9;   // FP8 digit slices; |V| < 2^62 in the epilogue
 constexpr int DEFAULT_SLICES = 9;
@@ -101,6 +105,9 @@ constexpr int GROUP_M = 8;
 // tcgen05.mma instruction descriptor, kind::f8f6f4: D=F32, A=B=E4M3
 // (format 0), both K-major, N=256, M=128.
 constexpr uint32_t IDESC = (1u << 4) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+// kind::f16: D=F32, A=B=BF16 (format 1), K-major, N=256, M=128 (grouped launches)
+constexpr uint32_t IDESC_BF16 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                                ((uint32_t)(BM >> 4) << 24);
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -191,8 +198,8 @@ __device__ __forceinline__ uint64_t desc_sw64(const void* p) {
   d |= (uint64_t)4 << 61;                // 64B swizzle
   return d;
 }
-template <int KB>
-__device__ __forceinline__ uint64_t desc_gemm(const void* p) { return KB == 128 ? desc_sw128(p) : desc_sw64(p); }
+template <int ROW>
+__device__ __forceinline__ uint64_t desc_gemm(const void* p) { return ROW == 128 ? desc_sw128(p) : desc_sw64(p); }
 
 __device__ __forceinline__ void mma_bf16(uint32_t dt, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
   asm volatile(
@@ -302,10 +309,11 @@ __device__ __forceinline__ float2 square_pair(long long V, float fscale) {
 // are kernel parameters (single problem) or live in global memory (grouped
 // launch, written by the host before the launch: acquired through the
 // tensormap proxy before their first use).
-template <int KB>
+template <int KB, int ESZ>
 __device__ __forceinline__ void gemm_tile(const CUtensorMap* tmA, const CUtensorMap* tmB, const GemmArgs g,
                                           const int m_tile, const int n_tile, const bool global_maps) {
-  using R = GemmRing<KB>;
+  using R = GemmRing<KB, ESZ>;
+  constexpr int BASE = ESZ == 1 ? 32 : 256;  // digit base: FP8 five-bit, BF16 eight-bit digits
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* full = (uint64_t*)(smem + R::STAGES * R::STAGE);
@@ -392,13 +400,19 @@ __device__ __forceinline__ void gemm_tile(const CUtensorMap* tmA, const CUtensor
           if (!mbar_wait(&full[stage], phase, abort_flag, g.err, 3)) { ok = false; break; }
           tc_fence_after();
           uint8_t* sb = smem + stage * R::STAGE;
-          const uint64_t a0 = desc_gemm<KB>(sb), a1 = desc_gemm<KB>(sb + R::A), b = desc_gemm<KB>(sb + 2 * R::A);
+          const uint64_t a0 = desc_gemm<R::ROW>(sb), a1 = desc_gemm<R::ROW>(sb + R::A),
+                         b = desc_gemm<R::ROW>(sb + 2 * R::A);
 #pragma unroll
-          for (int k = 0; k < KB / 32; k++) {  // K = 32 one-byte digits (32 bytes) per MMA
+          for (int k = 0; k < R::ROW / 32; k++) {  // 32 bytes of K per MMA (32 FP8 or 16 BF16 digits)
             const uint64_t koff = (uint64_t)((k * 32) >> 4);
             const uint32_t acc = (kb > 0 || k > 0) ? 1u : 0u;
-            mma_f8(tbase, a0 + koff, b + koff, IDESC, acc);
-            if (two) mma_f8(tbase + 256, a1 + koff, b + koff, IDESC, acc);
+            if constexpr (ESZ == 1) {
+              mma_f8(tbase, a0 + koff, b + koff, IDESC, acc);
+              if (two) mma_f8(tbase + 256, a1 + koff, b + koff, IDESC, acc);
+            } else {
+              mma_bf16(tbase, a0 + koff, b + koff, IDESC_BF16, acc);
+              if (two) mma_bf16(tbase + 256, a1 + koff, b + koff, IDESC_BF16, acc);
+            }
           }
           any = true;
           mma_commit(&empty[stage]);
@@ -458,10 +472,10 @@ __device__ __forceinline__ void gemm_tile(const CUtensorMap* tmA, const CUtensor
 #pragma unroll
         for (int j = 0; j < 32; j++) {
           if (c0 + j >= cend) break;
-          int qv = exact_f2i(__uint_as_float(v0[j])) * 32;
+          int qv = exact_f2i(__uint_as_float(v0[j])) * BASE;
           if (two) qv += exact_f2i(__uint_as_float(v1[j]));
           long long* cp = crow + (long long)(c0 + j) * g.ldc;
-          const long long V = (p == 0) ? (long long)qv : prev[j] * 1024LL + (long long)qv;
+          const long long V = (p == 0) ? (long long)qv : prev[j] * (long long)(BASE * BASE) + (long long)qv;
           if (!last)
             *cp = V;
           else if (sq)
@@ -491,7 +505,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   const int gsz = min(g.tiles_m - first_m, GROUP_M);
   const int m_tile = first_m + (tile % per_group) % gsz;
   const int n_tile = (tile % per_group) / gsz;
-  gemm_tile<GBK>(&tmA, &tmB, g, m_tile, n_tile, false);
+  gemm_tile<GBK, 1>(&tmA, &tmB, g, m_tile, n_tile, false);
 }
 
 // Many independent problems in one launch: CTA b computes tiles[b] of
@@ -504,7 +518,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   GemmArgs g = probs[tl.prob].g;
   g.N = cols[probs[tl.prob].cohort];
   if (tl.n_tile * BN >= g.N) return;
-  gemm_tile<GRBK>(maps + 2 * tl.prob, maps + 2 * tl.prob + 1, g, tl.m_tile, tl.n_tile, true);
+  gemm_tile<GRBK, 2>(maps + 2 * tl.prob, maps + 2 * tl.prob + 1, g, tl.m_tile, tl.n_tile, true);
 }
 
 // ---------------------------------------------------------------------------
@@ -896,9 +910,12 @@ __global__ void __launch_bounds__(256) trait_digits_kernel(int n, const double* 
 // Slicing: row r of A (K-contiguous source, element k at src[k + r*lds]) ->
 // S digit slices (BF16) at A[(s*Mpad + r)*Kpad + k], scale per row.
 // ---------------------------------------------------------------------------
+template <bool BF16D>
 __global__ void __launch_bounds__(256) slice_rows_kernel(int K, int rows, const double* __restrict__ src,
                                                          long long lds, int row_off, int S, int Mpad, int Kpad,
-                                                         uint8_t* __restrict__ A, double* __restrict__ row_scale) {
+                                                         void* __restrict__ Aout, double* __restrict__ row_scale) {
+  // FP8: five-bit digits |d| <= 16 (E4M3 bytes); BF16: eight-bit digits |d| <= 128
+  constexpr int LOG_BASE = BF16D ? 8 : 5;
   const int r = blockIdx.x;
   if (r >= rows) return;
   const double* a = src + (long long)r * lds;
@@ -920,21 +937,28 @@ __global__ void __launch_bounds__(256) slice_rows_kernel(int K, int rows, const 
   const int e = (mx > 0.0) ? ilogb(mx) + 1 : 0;  // max * 2^-e in [0.5, 1)
   const int passes = (S + 1) / 2;
   const int R = row_off + r;
-  if (threadIdx.x == 0) row_scale[R] = ldexp(1.0, e - 9 - 10 * (passes - 1));
+  // V (Horner over slice pairs) times 2^(e + 1 - 2 LOG_BASE passes) is the row of C
+  if (threadIdx.x == 0) row_scale[R] = ldexp(1.0, e + 1 - 2 * LOG_BASE * passes);
   for (int k = threadIdx.x; k < K; k += blockDim.x) {
-    double v = ldexp(a[k], 4 - e);  // |v| < 16
+    double v = ldexp(a[k], LOG_BASE - 1 - e);  // |v| < 2^(LOG_BASE - 1)
 #pragma unroll 1
     for (int s = 0; s < S; s++) {
       const double d = rint(v);
-      A[((long long)s * Mpad + R) * Kpad + k] = (uint8_t)e4m3_digit((float)d);  // |d| <= 16: exact
-      v = (v - d) * 32.0;
+      const long long at = ((long long)s * Mpad + R) * Kpad + k;
+      if constexpr (BF16D)
+        ((__nv_bfloat16*)Aout)[at] = __double2bfloat16(d);  // |d| <= 128: exact
+      else
+        ((uint8_t*)Aout)[at] = (uint8_t)e4m3_digit((float)d);  // |d| <= 16: exact
+      v = (v - d) * (double)(1 << LOG_BASE);
     }
   }
 }
 
 // genotypes (FP64 or bytes, column c at src[c*lds + k]) -> BF16 [c*Kpad + k]
 // Genotype value -> BF16 (exact for hard calls 0/1/2).
-// genotypes as E4M3 bytes (hard calls 0/1/2 are exact)
+// genotypes as BF16 (grouped launches) or E4M3 bytes (hard calls 0/1/2 are exact in both)
+__device__ __forceinline__ __nv_bfloat16 geno_bf16(unsigned char v) { return __float2bfloat16((float)v); }
+__device__ __forceinline__ __nv_bfloat16 geno_bf16(double v) { return __float2bfloat16((float)v); }
 __device__ __forceinline__ uint8_t geno_f8(unsigned char v) {
   return (uint8_t)__nv_cvt_float_to_fp8((float)v, __NV_SATFINITE, __NV_E4M3);
 }
@@ -949,7 +973,7 @@ __device__ __forceinline__ uint16_t geno_f8x2(double a, double b) {
 // columns that start on a 16-byte boundary move as 16-byte pairs into 2-byte
 // E4M3 pairs; rows K .. Kpad-1 of G stay zero from its allocation.
 template <typename T>
-__global__ void __launch_bounds__(256) genotypes_bf16_kernel(int K, int cols, const T* __restrict__ src,
+__global__ void __launch_bounds__(256) genotypes_f8_kernel(int K, int cols, const T* __restrict__ src,
                                                              long long lds, uint8_t* __restrict__ G,
                                                              int Kpad) {
   const long long c = blockIdx.x;
@@ -1042,23 +1066,26 @@ EncodeTiledFn get_encoder() {
   return fn;
 }
 
-// 2D byte (E4M3) tensor map, K innermost, box {box_k, box_rows}; 128B
-// swizzle for 128-byte rows, 64B swizzle for 64-byte rows.  make_map is the
-// split GEMM's operand layout (K-step GBK).
-cudaError_t make_map_box(CUtensorMap* m, const void* base, long long K, long long rows, int box_rows, int box_k) {
+// 2D tensor map of esz-byte digits (1: E4M3, 2: BF16), K innermost, box
+// {box_k, box_rows}; 128B swizzle for 128-byte rows, 64B swizzle for 64-byte
+// rows.  make_map is the single-problem split GEMM's E4M3 layout (K-step GBK).
+cudaError_t make_map_box(CUtensorMap* m, const void* base, long long K, long long rows, int box_rows, int box_k,
+                         int esz) {
   EncodeTiledFn enc = get_encoder();
   if (!enc) return cudaErrorNotSupported;
   cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)K};
+  cuuint64_t strides[1] = {(cuuint64_t)K * esz};
   cuuint32_t box[2] = {(cuuint32_t)box_k, (cuuint32_t)box_rows};
   cuuint32_t es[2] = {1, 1};
-  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<void*>(base), dims, strides, box, es,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, box_k == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+  const int row = box_k * esz;
+  CUresult r = enc(m, esz == 2 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_UINT8, 2,
+                   const_cast<void*>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   row == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 cudaError_t make_map(CUtensorMap* m, const void* base, long long K, long long rows, int box_rows) {
-  return make_map_box(m, base, K, rows, box_rows, GBK);
+  return make_map_box(m, base, K, rows, box_rows, GBK, 1);
 }
 // 2D byte tensor map (FP8 digits), K innermost in rows of K bytes, box
 // {QT_KB, box_rows}, 128B swizzle.
@@ -1215,9 +1242,11 @@ namespace {
 cudaError_t slice_operands(OzakiPlan* p, cudaStream_t s, const double* top, long long ldtop, int toprows) {
   // rows [0, toprows) from `top` (row r contiguous at top + r*ldtop), rows
   // [n, n + nU) from the columns of U.
-  slice_rows_kernel<<<toprows, 256, 0, s>>>(p->n, toprows, top, ldtop, 0, p->S, p->Mpad, p->Kpad, p->A, p->scale);
+  slice_rows_kernel<false><<<toprows, 256, 0, s>>>(p->n, toprows, top, ldtop, 0, p->S, p->Mpad, p->Kpad, p->A,
+                                                    p->scale);
   note_launch();
-  slice_rows_kernel<<<p->nU, 256, 0, s>>>(p->n, p->nU, p->U, p->n, p->n, p->S, p->Mpad, p->Kpad, p->A, p->scale);
+  slice_rows_kernel<false><<<p->nU, 256, 0, s>>>(p->n, p->nU, p->U, p->n, p->n, p->S, p->Mpad, p->Kpad, p->A,
+                                                  p->scale);
   note_launch();
   return cudaGetLastError();
 }
@@ -1246,7 +1275,7 @@ cudaError_t run_gemm(OzakiPlan* p, cudaStream_t s, int col0, int x, int tri_rows
 template <typename T>
 cudaError_t load_genotypes(OzakiPlan* p, cudaStream_t s, const T* X, int x) {
   if (x <= 0) return cudaSuccess;
-  genotypes_bf16_kernel<T><<<x, 256, 0, s>>>(p->n, x, X, p->n, p->G, p->Kpad);
+  genotypes_f8_kernel<T><<<x, 256, 0, s>>>(p->n, x, X, p->n, p->G, p->Kpad);
   note_launch();
   return cudaGetLastError();
 }
@@ -1381,16 +1410,16 @@ int split_k_padded(int n) { return (n + KALIGN - 1) / KALIGN * KALIGN; }
 int split_cols_padded(int x) { return (x + BN - 1) / BN * BN; }
 
 cudaError_t split_chol_operand(cudaStream_t s, int n, int wXL, const double* L, const double* WY, int S, int Mpad,
-                               int Kpad, uint8_t* A, double* scale, double* Linv, double* LinvT, double* U) {
+                               int Kpad, __nv_bfloat16* A, double* scale, double* Linv, double* LinvT, double* U) {
   const int nU = 1 + wXL;
   FGLS_CUDA_TRY(lower_inverse(s, n, L, Linv));
   FGLS_CUDA_TRY(dgemm(s, true, false, n, nU, n, 1.0, Linv, n, WY, n, 0.0, U, n));
   dim3 tg((n + 31) / 32, (n + 31) / 32);
   transpose_kernel<<<tg, dim3(32, 8), 0, s>>>(n, Linv, LinvT);
   note_launch();
-  slice_rows_kernel<<<n, 256, 0, s>>>(n, n, LinvT, n, 0, S, Mpad, Kpad, A, scale);
+  slice_rows_kernel<true><<<n, 256, 0, s>>>(n, n, LinvT, n, 0, S, Mpad, Kpad, A, scale);
   note_launch();
-  slice_rows_kernel<<<nU, 256, 0, s>>>(n, nU, U, n, n, S, Mpad, Kpad, A, scale);
+  slice_rows_kernel<true><<<nU, 256, 0, s>>>(n, nU, U, n, n, S, Mpad, Kpad, A, scale);
   note_launch();
   return cudaGetLastError();
 }
@@ -1400,7 +1429,7 @@ namespace {
 // S_built slices: 2^(e - 15 - 16 (passes - 1)) depends on the pass count only
 __global__ void rescale_rows_kernel(int rows, const double* __restrict__ built, int dpass, double* __restrict__ out) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r < rows) out[r] = ldexp(built[r], 10 * dpass);
+  if (r < rows) out[r] = ldexp(built[r], 16 * dpass);  // BF16 digits: 16 bits per slice pair
 }
 
 template <typename T>
@@ -1408,25 +1437,25 @@ __global__ void grouped_genotypes_kernel(const GenoCohort* __restrict__ gc, cons
   const int c = blockIdx.y;
   const int x = sc[c].x, n = gc[c].n, Kpad = gc[c].Kpad;
   const T* __restrict__ src = (const T*)sc[c].X;
-  uint8_t* __restrict__ G = gc[c].G;
+  __nv_bfloat16* __restrict__ G = gc[c].G;
   // columns strided over the CTAs of this cohort, rows over the threads; u8
   // columns that start on a 4-byte boundary move 4 calls per load
   for (int col = blockIdx.x; col < x; col += gridDim.x) {
     const T* s = src + (long long)col * n;
-    uint8_t* g = G + (long long)col * Kpad;
+    __nv_bfloat16* g = G + (long long)col * Kpad;
     if constexpr (sizeof(T) == 1) {
       if (((uintptr_t)s & 3) == 0) {
         const int n4 = n >> 2;
         for (int q = threadIdx.x; q < n4; q += blockDim.x) {
           const uchar4 v = ((const uchar4*)s)[q];
-          ((uint32_t*)g)[q] = (uint32_t)geno_f8(v.x) | ((uint32_t)geno_f8(v.y) << 8) |
-                              ((uint32_t)geno_f8(v.z) << 16) | ((uint32_t)geno_f8(v.w) << 24);
+          ((__nv_bfloat162*)g)[2 * q] = __halves2bfloat162(geno_bf16(v.x), geno_bf16(v.y));
+          ((__nv_bfloat162*)g)[2 * q + 1] = __halves2bfloat162(geno_bf16(v.z), geno_bf16(v.w));
         }
-        for (int k = 4 * n4 + threadIdx.x; k < n; k += blockDim.x) g[k] = geno_f8(s[k]);
+        for (int k = 4 * n4 + threadIdx.x; k < n; k += blockDim.x) g[k] = geno_bf16(s[k]);
         continue;
       }
     }
-    for (int k = threadIdx.x; k < n; k += blockDim.x) g[k] = geno_f8(s[k]);
+    for (int k = threadIdx.x; k < n; k += blockDim.x) g[k] = geno_bf16(s[k]);
   }
 }
 }  // namespace
@@ -1480,8 +1509,8 @@ cudaError_t grouped_gemm_create(GroupedGemm** out, const GroupedGemmDesc* d, int
     g.err = err;
     probs[i].cohort = d[i].cohort;
     probs[i].pad = 0;
-    FGLS_CUDA_TRY(make_map_box(&maps[2 * i], d[i].A, d[i].Kpad, (long long)d[i].S_alloc * d[i].Mpad, BM, GRBK));
-    FGLS_CUDA_TRY(make_map_box(&maps[2 * i + 1], d[i].G, d[i].Kpad, d[i].Ncap, BN, GRBK));
+    FGLS_CUDA_TRY(make_map_box(&maps[2 * i], d[i].A, d[i].Kpad, (long long)d[i].S_alloc * d[i].Mpad, BM, GRBK, 2));
+    FGLS_CUDA_TRY(make_map_box(&maps[2 * i + 1], d[i].G, d[i].Kpad, d[i].Ncap, BN, GRBK, 2));
     order[i] = i;
     work[i] = (long long)g.tiles_m * g.Kpad;
   }
@@ -1582,7 +1611,7 @@ extern "C" int fglsgpu_selftest_split_gemm(int M, int K, int N, int S, const dou
   if (r == cudaSuccess)
     chk(cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
   if (r == cudaSuccess) {
-    slice_rows_kernel<<<M, 256, 0, s>>>(K, M, dA, K, 0, S, p.Mpad, p.Kpad, p.A, p.scale);
+    slice_rows_kernel<false><<<M, 256, 0, s>>>(K, M, dA, K, 0, S, p.Mpad, p.Kpad, p.A, p.scale);
     chk(cudaGetLastError());
   }
   if (r == cudaSuccess) chk(load_genotypes<double>(&p, s, dX, N));
@@ -1680,7 +1709,7 @@ extern "C" int fglsgpu_split_gemm_noalloc(int M, int K, int N, int slices, const
   if (r == cudaSuccess) chk(make_map(&p.mapA, p.A, p.Kpad, (long long)slices * p.Mpad, BM));
   if (r == cudaSuccess) chk(make_map(&p.mapB, p.G, p.Kpad, p.Ncap, BN));
   if (r == cudaSuccess) {
-    slice_rows_kernel<<<M, 256, 0, s>>>(K, M, dA, K, 0, slices, p.Mpad, p.Kpad, p.A, p.scale);
+    slice_rows_kernel<false><<<M, 256, 0, s>>>(K, M, dA, K, 0, slices, p.Mpad, p.Kpad, p.A, p.scale);
     note_launch();
     chk(cudaGetLastError());
   }

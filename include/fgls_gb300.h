@@ -292,7 +292,7 @@ typedef struct {
 
 typedef struct {
   int x_b;          /* SNPs per cohort per step (0: autotune)             */
-  int slices;       /* 5-bit digit slices 3..9 (0: autotune)              */
+  int slices;       /* BF16 eight-bit digit slices 3..6 (0: autotune)     */
   int device;       /* CUDA device ordinal                                */
   int use_graph;    /* 1: replay each step from a captured CUDA graph     */
   int genotypes_u8; /* 1: genotype blocks are bytes, 0: FP64              */
