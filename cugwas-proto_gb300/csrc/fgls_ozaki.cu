@@ -857,17 +857,19 @@ __global__ void __launch_bounds__(QD_THREADS) snp_digits_kernel(int n, const flo
       vl[k] = scale_ok ? vl[k] * sc : ldexpf(vl[k], se);
     }
     for (int sd = 0; sd < S; sd++) {
-      uint32_t pk = 0;
+      float d[4];
 #pragma unroll
       for (int k = 0; k < 4; k++) {
-        const float d = rintf(vh[k]);
-        pk |= e4m3_digit(d) << (8 * k);
+        d[k] = rintf(vh[k]);
         float hs, he;
-        two_sum_f(__fsub_rn(vh[k], d), vl[k], hs, he);
+        two_sum_f(__fsub_rn(vh[k], d[k]), vl[k], hs, he);
         vh[k] = hs * 32.0f;
         vl[k] = he * 32.0f;
       }
-      *(uint32_t*)(Ad + ((long long)sd * Ncap + i) * Kq + l) = pk;  // rows n..Kq-1 receive zeros
+      // two digits per conversion instruction (|d| <= 16: exact in E4M3)
+      const uint32_t lo = __nv_cvt_float2_to_fp8x2(make_float2(d[0], d[1]), __NV_SATFINITE, __NV_E4M3);
+      const uint32_t hi = __nv_cvt_float2_to_fp8x2(make_float2(d[2], d[3]), __NV_SATFINITE, __NV_E4M3);
+      *(uint32_t*)(Ad + ((long long)sd * Ncap + i) * Kq + l) = lo | (hi << 16);  // rows n..Kq-1 receive zeros
     }
   }
 }
