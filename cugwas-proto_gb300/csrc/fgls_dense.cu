@@ -191,9 +191,11 @@ __global__ void __launch_bounds__(DT) potf2_kernel(int kb, double* A, long long 
 // block's rows, c < nrhs over the right-hand sides.  Used for
 //   TRSM:  X := L^-1 X        (si = 1, sc = ldx)
 //   POTRF: P := P L^-T        (rows of the panel are the RHS: si = lda, sc = 1)
+template <int SCB>
 __global__ void __launch_bounds__(DT) diag_solve_kernel(int kb, const double* L, long long ldl,
                                                         double* X, long long si, long long sc,
                                                         int nrhs) {
+  constexpr int G = DT / SCB;      // row groups (a power of two)
   extern __shared__ double sm[];
   const int ldL = NB + 1;
   double* Ls = sm;                 // [NB][NB+1] column-major
@@ -217,14 +219,14 @@ __global__ void __launch_bounds__(DT) diag_solve_kernel(int kb, const double* L,
   }
   __syncthreads();
   const int c = threadIdx.x % SCB;   // my column
-  const int g = threadIdx.x / SCB;   // my row group (4 groups)
+  const int g = threadIdx.x / SCB;   // my row group
   for (int j = 0; j < kb; j++) {
     double xj = 0.0;
     if (c < nc) xj = Xs[c * ldL + j] / Ls[j * ldL + j];
     __syncthreads();
     if (c < nc) {
-      if (g == (j & 3)) Xs[c * ldL + j] = xj;
-      for (int i = j + 1 + ((g - (j + 1)) & 3); i < kb; i += 4) Xs[c * ldL + i] -= Ls[j * ldL + i] * xj;
+      if (g == (j & (G - 1))) Xs[c * ldL + j] = xj;
+      for (int i = j + 1 + ((g - (j + 1)) & (G - 1)); i < kb; i += G) Xs[c * ldL + i] -= Ls[j * ldL + i] * xj;
     }
     __syncthreads();
   }
@@ -243,6 +245,19 @@ __global__ void __launch_bounds__(DT) diag_solve_kernel(int kb, const double* L,
 
 constexpr size_t POTF2_SMEM = sizeof(double) * NB * (NB + 1);
 constexpr size_t DSOLVE_SMEM = sizeof(double) * (NB + SCB) * (NB + 1);
+constexpr int SCB_NARROW = 16;  // RHS per CTA when few right-hand sides (e.g. the 512-wide L^-1 panels)
+constexpr size_t DSOLVE_SMEM_NARROW = sizeof(double) * (NB + SCB_NARROW) * (NB + 1);
+
+// X := L_kk^-1 X for nrhs right-hand sides: 64 per CTA, or 16 when that
+// leaves fewer CTAs than half the SMs (the solve is FP64-issue-bound per SM)
+void launch_diag_solve(cudaStream_t s, int kb, const double* L, long long ldl, double* X, long long si,
+                       long long sc, int nrhs) {
+  if (ceil_div(nrhs, SCB) < 76)
+    diag_solve_kernel<SCB_NARROW><<<ceil_div(nrhs, SCB_NARROW), DT, DSOLVE_SMEM_NARROW, s>>>(kb, L, ldl, X, si,
+                                                                                           sc, nrhs);
+  else
+    diag_solve_kernel<SCB><<<ceil_div(nrhs, SCB), DT, DSOLVE_SMEM, s>>>(kb, L, ldl, X, si, sc, nrhs);
+}
 
 __global__ void build_shifted_kernel(int n, const double* __restrict__ S, long long lds, double alpha,
                                      double beta, double* __restrict__ A, long long lda) {
@@ -261,7 +276,10 @@ bool g_attr_done = false;
 cudaError_t ensure_attrs() {
   if (g_attr_done) return cudaSuccess;
   FGLS_CUDA_TRY(cudaFuncSetAttribute(potf2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)POTF2_SMEM));
-  FGLS_CUDA_TRY(cudaFuncSetAttribute(diag_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DSOLVE_SMEM));
+  FGLS_CUDA_TRY(cudaFuncSetAttribute(diag_solve_kernel<SCB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)DSOLVE_SMEM));
+  FGLS_CUDA_TRY(cudaFuncSetAttribute(diag_solve_kernel<SCB_NARROW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)DSOLVE_SMEM_NARROW));
   g_attr_done = true;
   return cudaSuccess;
 }
@@ -338,7 +356,7 @@ cudaError_t dpotrf_lower(cudaStream_t s, int n, double* A, long long lda, DevSta
     if (rest > 0) {
       double* P = A + (k + kb) + (long long)k * lda;  // rest x kb panel
       // P := P L_kk^-T  (each panel row is a right-hand side)
-      diag_solve_kernel<<<ceil_div(rest, SCB), DT, DSOLVE_SMEM, s>>>(kb, Akk, lda, P, lda, 1, rest);
+      launch_diag_solve(s, kb, Akk, lda, P, lda, 1, rest);
       note_launch();
       FGLS_CUDA_TRY(cudaGetLastError());
       double* T = A + (k + kb) + (long long)(k + kb) * lda;
@@ -356,7 +374,7 @@ cudaError_t dtrsm_llnn(cudaStream_t s, int n, int nrhs, const double* L, long lo
     const int kb = std::min(NB, n - k);
     const double* Lkk = L + k + (long long)k * ldl;
     double* Xk = X + k;
-    diag_solve_kernel<<<ceil_div(nrhs, SCB), DT, DSOLVE_SMEM, s>>>(kb, Lkk, ldl, Xk, 1, ldx, nrhs);
+    launch_diag_solve(s, kb, Lkk, ldl, Xk, 1, ldx, nrhs);
     note_launch();
     FGLS_CUDA_TRY(cudaGetLastError());
     const int rest = n - k - kb;
