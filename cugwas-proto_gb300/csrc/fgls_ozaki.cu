@@ -35,8 +35,10 @@
 //          rows [0, n) of C are R = Z^T X, rows [n, n + t(1+wXL)) are the
 //          Gram terms x~^T y~_j and x~^T XL~_j directly (one-sided: the exact
 //          genotypes are the other operand).  The quadratic terms
-//          sum_l R_l^2 d_j(l) run in double-FP32 (error-free products and
-//          sums) on the CUDA cores: quad_gram (fgls_selfgram.cu).
+//          sum_l R_l^2 d_j(l) run on the tensor cores from base-32 E4M3
+//          digits of R^2 and d_j (quadtc_kernel below, 33 <= t), else in
+//          double-FP32 (error-free products and sums) on the CUDA cores:
+//          quad_gram (fgls_selfgram.cu).
 //   chol:  A = [L^-1 ; U^T], U = L^-T [y~ | XL~].
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -554,7 +556,7 @@ constexpr int QT_MAXPASS = 40;
 // kind::f8f6f4 instruction descriptor: F32 accumulator, A and B E4M3 (format
 // 0), K-major, N = 224, M = 128
 constexpr uint32_t QT_IDESC = (1u << 4) | ((uint32_t)(224 >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
-static_assert(A_TILE == BM * QT_KB, "the SNP digit tile is a BF16 split tile's bytes");
+static_assert(A_TILE == BM * QT_KB, "the SNP digit tile has the bytes of one 128-byte-row GEMM tile");
 
 struct QuadPasses {
   int n;
@@ -910,7 +912,8 @@ __global__ void __launch_bounds__(256) trait_digits_kernel(int n, const double* 
 
 // ---------------------------------------------------------------------------
 // Slicing: row r of A (K-contiguous source, element k at src[k + r*lds]) ->
-// S digit slices (BF16) at A[(s*Mpad + r)*Kpad + k], scale per row.
+// S digit slices (E4M3 bytes, or BF16 when BF16D) at A[(s*Mpad + r)*Kpad + k],
+// scale per row.
 // ---------------------------------------------------------------------------
 template <bool BF16D>
 __global__ void __launch_bounds__(256) slice_rows_kernel(int K, int rows, const double* __restrict__ src,
@@ -956,9 +959,8 @@ __global__ void __launch_bounds__(256) slice_rows_kernel(int K, int rows, const 
   }
 }
 
-// genotypes (FP64 or bytes, column c at src[c*lds + k]) -> BF16 [c*Kpad + k]
-// Genotype value -> BF16 (exact for hard calls 0/1/2).
-// genotypes as BF16 (grouped launches) or E4M3 bytes (hard calls 0/1/2 are exact in both)
+// Genotype value (FP64 or byte) as BF16 (grouped launches) or as an E4M3 byte
+// (single-problem launches); hard calls 0/1/2 are exact in both.
 __device__ __forceinline__ __nv_bfloat16 geno_bf16(unsigned char v) { return __float2bfloat16((float)v); }
 __device__ __forceinline__ __nv_bfloat16 geno_bf16(double v) { return __float2bfloat16((float)v); }
 __device__ __forceinline__ uint8_t geno_f8(unsigned char v) {
