@@ -274,91 +274,231 @@ __device__ __forceinline__ void solve_block(int x, int t, int wXL, const int j, 
   const int i = i0 + threadIdx.x;
   const int tw = wXL + wXL * wXL + 1;
   const double* T = top + (long long)j * tw;
-  double S[P][P];  // lower triangle used
-  double b[P];
-  bool valid = i < x;
-  if (valid) {
-    for (int a = 0; a < wXL; a++) {
-      b[a] = T[a];
-      for (int q = 0; q <= a; q++) S[a][q] = T[wXL + a + q * wXL];
-    }
-    for (int c = 0; c < wXR; c++) {
-      const long long row = (long long)i * wXR + c;
-      b[wXL + c] = GYL[row * rsg + (long long)j * ldg];
-      for (int k = 0; k < wXL; k++) S[wXL + c][k] = GYL[row * rsg + (long long)(t + j * wXL + k) * ldg];
-      for (int d = 0; d <= c; d++) S[wXL + c][wXL + d] = GR[row * wXR + d + (long long)j * ldr];
-    }
-  }
+  const bool valid = i < x;
   double* out = stage + threadIdx.x * (P + P * P);
-  if (valid) {
-    const double rs = T[wXL + wXL * wXL];
-    // potrf (lower, unblocked).  One division per column (ri = 1 / L_cc),
-    // multiplications elsewhere: FP64 division is a multi-instruction
-    // sequence on GB300's narrow FP64 pipe, which bounds this kernel.
-    double L[P][P], ri[P];
-    int info = 0;
+  if (wXL == P - 1) {
+    // One genotype column per SNP (wXR = 1): the leading W x W block of S
+    // (XL^T M^-1 XL) and b (XL^T M^-1 y) are the same for every SNP of trait
+    // j, so thread 0 factors them once for the CTA.  The per-SNP work below
+    // is the last row of the factor, the Schur complement pivot and the
+    // rank-one terms, in the same operation order as the general path, so
+    // both give the same bits.
+    constexpr int W = P - 1;
+    __shared__ double sL[W][W], sri[W], szt[W], sLi[W][W], sAi[W][W], srs;
+    __shared__ int sinfo;
+    if (threadIdx.x == 0) {
+      double A[W][W], L[W][W], ri[W], Li[W][W], z[W];
+      for (int a = 0; a < W; a++)
+        for (int q = 0; q <= a; q++) A[a][q] = T[W + a + q * W];
+      int info = 0;
 #pragma unroll
-    for (int c = 0; c < P; c++) {
-      double a = S[c][c];
+      for (int c = 0; c < W; c++) {
+        double v = A[c][c];
 #pragma unroll
-      for (int q = 0; q < c; q++) a -= L[c][q] * L[c][q];
-      if (!(a > 0.0) && info == 0) info = c + 1;
-      const double lcc = sqrt(a);
-      L[c][c] = lcc;
-      ri[c] = 1.0 / lcc;
+        for (int q = 0; q < c; q++) v -= L[c][q] * L[c][q];
+        if (!(v > 0.0) && info == 0) info = c + 1;
+        const double lcc = sqrt(v);
+        L[c][c] = lcc;
+        ri[c] = 1.0 / lcc;
 #pragma unroll
-      for (int r = c + 1; r < P; r++) {
-        double v = S[r][c];
+        for (int r = c + 1; r < W; r++) {
+          double u = A[r][c];
 #pragma unroll
-        for (int q = 0; q < c; q++) v -= L[r][q] * L[c][q];
-        L[r][c] = v * ri[c];
+          for (int q = 0; q < c; q++) u -= L[r][q] * L[c][q];
+          L[r][c] = u * ri[c];
+        }
       }
+#pragma unroll
+      for (int r = 0; r < W; r++) {
+        double v = T[r];
+#pragma unroll
+        for (int q = 0; q < r; q++) v -= L[r][q] * z[q];
+        z[r] = v * ri[r];
+      }
+#pragma unroll
+      for (int c = 0; c < W; c++) {
+        Li[c][c] = ri[c];
+#pragma unroll
+        for (int r = c + 1; r < W; r++) {
+          double v = 0.0;
+#pragma unroll
+          for (int q = c; q < r; q++) v -= L[r][q] * Li[q][c];
+          Li[r][c] = v * ri[r];
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < W; c++) {
+        sri[c] = ri[c];
+        szt[c] = z[c];
+#pragma unroll
+        for (int r = c; r < W; r++) {
+          sL[r][c] = L[r][c];
+          sLi[r][c] = Li[r][c];
+          double v = 0.0;
+#pragma unroll
+          for (int q = r; q < W; q++) v += Li[q][r] * Li[q][c];
+          sAi[r][c] = v;  // rows q < W of (Li^T Li)[r][c]
+        }
+      }
+      srs = T[W + W * W];
+      sinfo = info;
     }
-    if (info) set_status(st, FGLSGPU_ENOTSPD, tag + info, snp_base + i);
-    // two triangular solves: L z = b, L^T beta = z
-    double z[P];
+    __syncthreads();
+    if (valid) {
+      const long long row = i;
+      double l[W];
+      const double cc = GR[row + (long long)j * ldr];
+      const double yx = GYL[row * rsg + (long long)j * ldg];
 #pragma unroll
-    for (int r = 0; r < P; r++) {
-      double v = b[r];
+      for (int c = 0; c < W; c++) l[c] = GYL[row * rsg + (long long)(t + j * W + c) * ldg];
+      // last row of the factor: l = L_A^-1 s, pivot^2 = c - l^T l
 #pragma unroll
-      for (int q = 0; q < r; q++) v -= L[r][q] * z[q];
-      z[r] = v * ri[r];
-    }
+      for (int c = 0; c < W; c++) {
+        double v = l[c];
 #pragma unroll
-    for (int r = P - 1; r >= 0; r--) {
-      double v = z[r];
+        for (int q = 0; q < c; q++) v -= l[q] * sL[c][q];
+        l[c] = v * sri[c];
+      }
+      double dd = cc;
 #pragma unroll
-      for (int q = r + 1; q < P; q++) v -= L[q][r] * z[q];
-      z[r] = v * ri[r];
-    }
-    // potri: Li = L^-1 (lower), Sinv = Li^T Li (lower part)
-    double Li[P][P];
+      for (int q = 0; q < W; q++) dd -= l[q] * l[q];
+      int info = sinfo;
+      if (!(dd > 0.0) && info == 0) info = P;
+      if (info) set_status(st, FGLSGPU_ENOTSPD, tag + info, snp_base + i);
+      const double rP = 1.0 / sqrt(dd);
+      // forward and back substitution
+      double zP = yx;
 #pragma unroll
-    for (int c = 0; c < P; c++) {
-      Li[c][c] = ri[c];
+      for (int q = 0; q < W; q++) zP -= l[q] * szt[q];
+      zP *= rP;
+      const double bP = zP * rP;
+      double beta[W];
 #pragma unroll
-      for (int r = c + 1; r < P; r++) {
+      for (int r = W - 1; r >= 0; r--) {
+        double v = szt[r];
+#pragma unroll
+        for (int q = r + 1; q < W; q++) v -= sL[q][r] * beta[q];
+        v -= l[r] * bP;
+        beta[r] = v * sri[r];
+      }
+      // last row of L^-1, then S^-1 = Li^T Li
+      double lp[W];
+#pragma unroll
+      for (int c = 0; c < W; c++) {
         double v = 0.0;
 #pragma unroll
-        for (int q = c; q < r; q++) v -= L[r][q] * Li[q][c];
-        Li[r][c] = v * ri[r];
+        for (int q = c; q < W; q++) v -= l[q] * sLi[q][c];
+        lp[c] = v * rP;
+      }
+      const double rs = srs;
+#pragma unroll
+      for (int r = 0; r < W; r++) out[r] = beta[r];
+      out[W] = bP;
+      double* vo = out + P;
+#pragma unroll
+      for (int c = 0; c < P; c++) {
+#pragma unroll
+        for (int r = 0; r < P; r++) {
+          double v = 0.0;
+          if (r >= c) {
+            if (r < W)
+              v = sAi[r][c] + lp[r] * lp[c];
+            else if (c < W)
+              v = rP * lp[c];
+            else
+              v = rP * rP;
+            v *= rs;
+            if (r == c) v = sqrt(v);
+          }
+          vo[r + c * P] = v;  // column-major, strict upper = 0
+        }
       }
     }
+  } else {
+    double S[P][P];  // lower triangle used
+    double b[P];
+    if (valid) {
+      for (int a = 0; a < wXL; a++) {
+        b[a] = T[a];
+        for (int q = 0; q <= a; q++) S[a][q] = T[wXL + a + q * wXL];
+      }
+      for (int c = 0; c < wXR; c++) {
+        const long long row = (long long)i * wXR + c;
+        b[wXL + c] = GYL[row * rsg + (long long)j * ldg];
+        for (int k = 0; k < wXL; k++) S[wXL + c][k] = GYL[row * rsg + (long long)(t + j * wXL + k) * ldg];
+        for (int d = 0; d <= c; d++) S[wXL + c][wXL + d] = GR[row * wXR + d + (long long)j * ldr];
+      }
+    }
+    if (valid) {
+      const double rs = T[wXL + wXL * wXL];
+      // potrf (lower, unblocked).  One division per column (ri = 1 / L_cc),
+      // multiplications elsewhere: FP64 division is a multi-instruction
+      // sequence on GB300's narrow FP64 pipe, which bounds this kernel.
+      double L[P][P], ri[P];
+      int info = 0;
 #pragma unroll
-    for (int r = 0; r < P; r++) out[r] = z[r];
-    double* vo = out + P;
+      for (int c = 0; c < P; c++) {
+        double a = S[c][c];
 #pragma unroll
-    for (int c = 0; c < P; c++) {
+        for (int q = 0; q < c; q++) a -= L[c][q] * L[c][q];
+        if (!(a > 0.0) && info == 0) info = c + 1;
+        const double lcc = sqrt(a);
+        L[c][c] = lcc;
+        ri[c] = 1.0 / lcc;
+#pragma unroll
+        for (int r = c + 1; r < P; r++) {
+          double v = S[r][c];
+#pragma unroll
+          for (int q = 0; q < c; q++) v -= L[r][q] * L[c][q];
+          L[r][c] = v * ri[c];
+        }
+      }
+      if (info) set_status(st, FGLSGPU_ENOTSPD, tag + info, snp_base + i);
+      // two triangular solves: L z = b, L^T beta = z
+      double z[P];
 #pragma unroll
       for (int r = 0; r < P; r++) {
-        double v = 0.0;
-        if (r >= c) {
+        double v = b[r];
 #pragma unroll
-          for (int q = r; q < P; q++) v += Li[q][r] * Li[q][c];
-          v *= rs;
-          if (r == c) v = sqrt(v);
+        for (int q = 0; q < r; q++) v -= L[r][q] * z[q];
+        z[r] = v * ri[r];
+      }
+#pragma unroll
+      for (int r = P - 1; r >= 0; r--) {
+        double v = z[r];
+#pragma unroll
+        for (int q = r + 1; q < P; q++) v -= L[q][r] * z[q];
+        z[r] = v * ri[r];
+      }
+      // potri: Li = L^-1 (lower), Sinv = Li^T Li (lower part)
+      double Li[P][P];
+#pragma unroll
+      for (int c = 0; c < P; c++) {
+        Li[c][c] = ri[c];
+#pragma unroll
+        for (int r = c + 1; r < P; r++) {
+          double v = 0.0;
+#pragma unroll
+          for (int q = c; q < r; q++) v -= L[r][q] * Li[q][c];
+          Li[r][c] = v * ri[r];
         }
-        vo[r + c * P] = v;  // column-major, strict upper = 0
+      }
+#pragma unroll
+      for (int r = 0; r < P; r++) out[r] = z[r];
+      double* vo = out + P;
+#pragma unroll
+      for (int c = 0; c < P; c++) {
+#pragma unroll
+        for (int r = 0; r < P; r++) {
+          double v = 0.0;
+          if (r >= c) {
+#pragma unroll
+            for (int q = r; q < P; q++) v += Li[q][r] * Li[q][c];
+            v *= rs;
+            if (r == c) v = sqrt(v);
+          }
+          vo[r + c * P] = v;  // column-major, strict upper = 0
+        }
       }
     }
   }
