@@ -863,8 +863,16 @@ __global__ void __launch_bounds__(QD_THREADS) snp_digits_kernel(int n, const flo
 #pragma unroll
       for (int k = 0; k < 4; k++) {
         d[k] = rintf(vh[k]);
+        const float r = __fsub_rn(vh[k], d[k]);  // exact
         float hs, he;
-        two_sum_f(__fsub_rn(vh[k], d[k]), vl[k], hs, he);
+        if (sd == 0) {
+          two_sum_f(r, vl[k], hs, he);  // the squared pair from the GEMM need not be normalised
+        } else {
+          // Fast2Sum: (vh, vl) is normalised here, |vl| <= ulp(vh) / 2, and r is
+          // 0 or a multiple of ulp(vh), so |r| >= |vl| and the sum is exact
+          hs = __fadd_rn(r, vl[k]);
+          he = __fsub_rn(vl[k], __fsub_rn(hs, r));
+        }
         vh[k] = hs * 32.0f;
         vl[k] = he * 32.0f;
       }
