@@ -556,6 +556,8 @@ constexpr int QT_MAXPASS = 40;
 // kind::f8f6f4 instruction descriptor: F32 accumulator, A and B E4M3 (format
 // 0), K-major, N = 224, M = 128
 constexpr uint32_t QT_IDESC = (1u << 4) | ((uint32_t)(224 >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+// the same with N = 112: one trait digit of a slot pair whose second slot is empty
+constexpr uint32_t QT_IDESC1 = (1u << 4) | ((uint32_t)(QT_TP >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
 static_assert(A_TILE == BM * QT_KB, "the SNP digit tile has the bytes of one 128-byte-row GEMM tile");
 
 struct QuadPasses {
@@ -701,6 +703,9 @@ __global__ void __launch_bounds__(THREADS, 1)
         const int lu = u - u0;
         const int p = u % np;
         const bool second = qp.t[p][2] > 0;
+        // a slot pair with its second slot empty needs only the first slot's columns
+        const uint32_t id01 = qp.t[p][1] > 0 ? QT_IDESC : QT_IDESC1;
+        const uint32_t id23 = qp.t[p][3] > 0 ? QT_IDESC : QT_IDESC1;
         if (!mbar_wait(tempty, (lu & 1) ^ 1, abort_flag, g.err, 12)) { ok = false; break; }
         tc_fence_after();
         for (int kb = 0; kb < nk; kb++) {
@@ -712,8 +717,8 @@ __global__ void __launch_bounds__(THREADS, 1)
           for (int k = 0; k < QT_KB / 32; k++) {  // K = 32 one-byte digits (32 bytes) per MMA
             const uint64_t koff = (uint64_t)((k * 32) >> 4);
             const uint32_t acc = (kb > 0 || k > 0) ? 1u : 0u;
-            mma_f8(tbase, a + koff, b01 + koff, QT_IDESC, acc);
-            if (second) mma_f8(tbase + 224, a + koff, b23 + koff, QT_IDESC, acc);
+            mma_f8(tbase, a + koff, b01 + koff, id01, acc);
+            if (second) mma_f8(tbase + 224, a + koff, b23 + koff, id23, acc);
           }
           any = true;
           mma_commit(&empty[stage]);
