@@ -505,8 +505,11 @@ __global__ void __launch_bounds__(THREADS, 1)
   const int group = tile / per_group;
   const int first_m = group * GROUP_M;
   const int gsz = min(g.tiles_m - first_m, GROUP_M);
-  const int m_tile = first_m + (tile % per_group) % gsz;
+  int m_tile = first_m + (tile % per_group) % gsz;
   const int n_tile = (tile % per_group) / gsz;
+  // triangular L^-1: row tile i has ~i + 1 K-blocks, so start with the
+  // longest tiles and let the short ones fill the last wave
+  if (g.tri_rows > 0) m_tile = g.tiles_m - 1 - m_tile;
   gemm_tile<GBK, 1>(&tmA, &tmB, g, m_tile, n_tile, false);
 }
 
