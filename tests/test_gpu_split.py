@@ -112,6 +112,24 @@ def test_precision_switch_keeps_eigendecomposition():
     assert d["beta_se_scaled"] <= 1e-10 and d["se_rel"] <= 1e-10, d
 
 
+@pytest.mark.parametrize("variant,t", [("eigen", 40), ("chol", 1)])
+def test_split_run_snps_pipeline_matches_single_blocks(variant, t):
+    """run_snps converts each block's genotypes on a second stream while the
+    previous block's quadratic Gram and solves run; the results must equal,
+    bit for bit, the same blocks run one at a time (conversion in order)."""
+    from fgls_gb300 import Engine, datagen
+    xb, n = 256, 1500
+    pb = datagen.make_problem(n, 6 * xb + 100, t, seed=11, hsig_uniform=True)
+    with Engine(n, 3, 1, t, xb, variant=variant, precision="split", slices=9) as e:
+        e.set_problem(pb.Phi, pb.XL, pb.Y, pb.h, pb.sigma)
+        if variant == "chol":
+            e.select_trait(0)
+        B, V = e.run_snps(pb.XR)
+        for i0 in range(0, pb.XR.shape[1], xb):  # run_snps blocks: max(256, xb/4), max(256, xb/2), xb, ...
+            B2, V2 = e.run_block(pb.XR[:, i0:i0 + xb])
+            assert np.array_equal(B[:, i0:i0 + xb], B2) and np.array_equal(V[:, i0:i0 + xb], V2), i0
+
+
 def test_split_u8_matches_fp64_genotype_input():
     import torch
     from fgls_gb300 import Engine, datagen
