@@ -150,8 +150,8 @@ def test_split_u8_matches_fp64_genotype_input():
 
 @pytest.mark.parametrize("n,t", [(700, 40), (700, 100), (2000, 100), (900, 250)])
 def test_tensor_core_quad_gram_vs_fp64_path(n, t, monkeypatch):
-    """The quadratic Gram on the tensor cores (6-bit digits of both operands,
-    used for t >= 33, in groups of 112 traits) and the double-FP32 CUDA-core kernel, each
+    """The quadratic Gram on the tensor cores (base-32 E4M3 digits of both
+    operands, used for t >= 33, in groups of 112 traits) and the double-FP32 CUDA-core kernel, each
     against the all-FP64 device path on the same eigendecomposition: the
     tensor-core path is within 2e-12 on the SE scale (measured ~3e-13), the
     double-FP32 one within 1e-10 (measured ~1e-11)."""
