@@ -29,7 +29,8 @@ def test_library_exports_every_declared_symbol():
     names = declared_functions()
     missing = [n for n in names if not hasattr(L, n)]
     assert not missing, missing
-    assert set(names) <= set(EXPORTS) | set(names)
+    # the Python mirror binds exactly the functions the header declares
+    assert set(EXPORTS) == set(names), sorted(set(EXPORTS) ^ set(names))
     assert L.fglsgpu_version() >= 10000
 
 
