@@ -47,7 +47,9 @@ def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
         d = json.load(open(p))
-        return d, "measured"
+        if all(k in d for k in FALLBACK_PEAKS):
+            return d, "measured"
+        return {**FALLBACK_PEAKS, **d}, "measured where present, else fallback"
     return dict(FALLBACK_PEAKS), "fallback"
 
 
