@@ -47,7 +47,9 @@ struct fglsgpu_engine {
   unsigned char* dU8 = nullptr;
   DevStatus* dst = nullptr;
   DevStatus* hst = nullptr;
+  int* hst_wait = nullptr;  // pinned copy of the split plan's wait error word
   OzakiPlan* oz = nullptr;  // split-precision state (eigen / chol)
+  unsigned long long wait_ns = 0;  // limit of one tcgen05 pipeline wait (0: the 2 s default)
   std::vector<double> hh, hs;
   int trait_sel = -1;
   bool problem_set = false;
@@ -106,8 +108,21 @@ cudaError_t dalloc(T** p, size_t count) {
 // follow the reference's error texts (src/fgls_chol.c:266-271, :309-314, :418-434).
 int check_status(fglsgpu_engine* e, const char* stage) {
   ENG_TRY(e, cudaMemcpyAsync(e->hst, e->dst, sizeof(DevStatus), cudaMemcpyDeviceToHost, e->comp), "status copy");
+  *e->hst_wait = 0;
+  if (e->oz)
+    ENG_TRY(e, cudaMemcpyAsync(e->hst_wait, ozaki_error_word(e->oz), sizeof(int), cudaMemcpyDeviceToHost, e->comp),
+            "status copy");
   ENG_TRY(e, cudaStreamSynchronize(e->comp), stage);
   const DevStatus s = *e->hst;
+  const int wsite = *e->hst_wait;
+  if (wsite) {
+    // the tcgen05 kernels of the split path gave up on a pipeline wait: their
+    // outputs since the last check are invalid; clear the word so that the
+    // next launches run normally
+    ENG_TRY(e, cudaMemsetAsync(ozaki_error_word(e->oz), 0, sizeof(int), e->comp), "status reset");
+    ENG_TRY(e, cudaStreamSynchronize(e->comp), "status reset");
+    return fail(e, FGLSGPU_ETIMEOUT, "device wait expired in %s (tensor-core kernel wait site %d)", stage, wsite);
+  }
   if (s.code == FGLSGPU_OK) return FGLSGPU_OK;
   if (s.code == FGLSGPU_ENOTSPD) {
     if (!strcmp(stage, "potrf(M)"))
@@ -137,6 +152,7 @@ void free_all(fglsgpu_engine* e) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (e->hst) cudaFreeHost(e->hst);
+  if (e->hst_wait) cudaFreeHost(e->hst_wait);
   for (auto* v : {&e->pev_live, &e->pev_pool})
     for (auto& ev : *v) {
       cudaEventDestroy(ev.a);
@@ -318,6 +334,7 @@ int fglsgpu_create(const fglsgpu_config* cfg, fglsgpu_engine** out) {
   chk(dalloc(&e->dtop, t * e->topw));
   chk(dalloc(&e->dst, 1));
   chk(cudaMallocHost((void**)&e->hst, sizeof(DevStatus)));
+  chk(cudaMallocHost((void**)&e->hst_wait, sizeof(int)));
   for (int k = 0; k < 2; k++) {
     chk(dalloc(&e->dX[k], n * xb * wXR));
     chk(dalloc(&e->dB[k], (long long)nt * xb * p));
@@ -402,6 +419,7 @@ int fglsgpu_set_problem(fglsgpu_engine* e, const double* Phi, const double* XL, 
     if (split(e)) {
       if (!e->oz) {
         ENG_TRY(e, ozaki_create(&e->oz, c.n, c.t, c.wXL, c.wXR, c.x_b, c.slices, /*eigen=*/1), "split plan");
+        ozaki_set_wait_limit(e->oz, e->wait_ns);
       }
       ENG_TRY(e, ozaki_set_eigen(e->oz, s, e->dZ, e->dAYL, e->ddinv), "split operands");
       ENG_TRY(e, cudaStreamSynchronize(s), "split operands");
@@ -439,6 +457,7 @@ int fglsgpu_select_trait(fglsgpu_engine* e, int j) {
   if (rc) return rc;
   if (split(e)) {
     if (!e->oz) ENG_TRY(e, ozaki_create(&e->oz, c.n, 1, c.wXL, c.wXR, c.x_b, c.slices, /*eigen=*/0), "split plan");
+    ozaki_set_wait_limit(e->oz, e->wait_ns);
     ENG_TRY(e, ozaki_set_chol(e->oz, s, e->dL, e->dWY), "split operands");
     ENG_TRY(e, cudaStreamSynchronize(s), "split operands");
   }
@@ -531,6 +550,21 @@ int run_snps_impl(fglsgpu_engine* e, const double* XR, long long m, double* B, d
   if (c.variant == FGLSGPU_VARIANT_CHOL && e->trait_sel < 0)
     return fail(e, FGLSGPU_ESTATE, "fglsgpu_select_trait must precede run_snps (chol)");
   ENG_TRY(e, cudaSetDevice(c.device), "cudaSetDevice");
+  // On an early error return, copies of neighbouring blocks may still be in
+  // flight on the three streams, reading XR or writing B/V/SE/P: wait for
+  // all of them (their status is ignored; the first error is reported) so
+  // that no copy touches the caller's arrays after this call returns.
+  struct DrainOnExit {
+    fglsgpu_engine* e;
+    bool armed = true;
+    ~DrainOnExit() {
+      if (!armed) return;
+      cudaStreamSynchronize(e->h2d);
+      cudaStreamSynchronize(e->comp);
+      cudaStreamSynchronize(e->d2h);
+      cudaGetLastError();
+    }
+  } drain{e};
   int rc = reset_status(e);
   if (rc) return rc;
   const int p = e->p, nt = out_traits(e);
@@ -576,6 +610,7 @@ int run_snps_impl(fglsgpu_engine* e, const double* XR, long long m, double* B, d
   }
   ENG_TRY(e, cudaStreamSynchronize(e->d2h), "run_snps");
   ENG_TRY(e, cudaStreamSynchronize(e->h2d), "run_snps");
+  drain.armed = false;
   return check_status(e, "block");
 }
 
@@ -619,10 +654,19 @@ int fglsgpu_set_precision(fglsgpu_engine* e, int precision) {
   c.precision = precision;
   if (precision == FGLSGPU_PREC_SPLIT && e->problem_set && c.variant == FGLSGPU_VARIANT_EIGEN) {
     if (!e->oz) ENG_TRY(e, ozaki_create(&e->oz, c.n, c.t, c.wXL, c.wXR, c.x_b, c.slices, 1), "split plan");
+    ozaki_set_wait_limit(e->oz, e->wait_ns);
     ENG_TRY(e, ozaki_set_eigen(e->oz, e->comp, e->dZ, e->dAYL, e->ddinv), "split operands");
     ENG_TRY(e, cudaStreamSynchronize(e->comp), "split operands");
   }
   if (c.variant == FGLSGPU_VARIANT_CHOL) e->trait_sel = -1;  // re-select: the operands differ per path
+  return FGLSGPU_OK;
+}
+
+int fglsgpu_set_wait_limit(fglsgpu_engine* e, long long ns) {
+  if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
+  if (ns < 0) return fail(e, FGLSGPU_EINVAL, "wait limit %lld < 0", ns);
+  e->wait_ns = (unsigned long long)ns;
+  if (e->oz) ozaki_set_wait_limit(e->oz, e->wait_ns);
   return FGLSGPU_OK;
 }
 
@@ -821,6 +865,7 @@ int fglsgpu_set_hsigma(fglsgpu_engine* e, const double* h, const double* sigma) 
   if (rc) return rc;
   if (split(e)) {
     if (!e->oz) ENG_TRY(e, ozaki_create(&e->oz, c.n, c.t, c.wXL, c.wXR, c.x_b, c.slices, 1), "split plan");
+    ozaki_set_wait_limit(e->oz, e->wait_ns);
     ENG_TRY(e, ozaki_set_eigen(e->oz, s, e->dZ, e->dAYL, e->ddinv), "split operands");
   }
   ENG_TRY(e, cudaStreamSynchronize(s), "set_hsigma");

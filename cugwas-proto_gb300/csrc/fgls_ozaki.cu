@@ -49,6 +49,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <vector>
 
 #include "fgls_common.cuh"
@@ -139,13 +140,14 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
-constexpr uint64_t WAIT_NS = 2000000000ull;  // one wait gives up after 2 s
+constexpr uint64_t WAIT_NS = 2000000000ull;  // default limit of one wait: 2 s
 
-// Bounded wait: false if the phase does not complete within WAIT_NS (the
+// Bounded wait: false if the phase does not complete within `limit_ns` (the
 // kernel-wide error word `err` then records `site`), or if this CTA or any
-// other CTA of the launch already gave up.
+// other CTA of the launch (or an earlier launch since the host last cleared
+// `err`) already gave up.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
-                                          int* err, int site) {
+                                          int* err, int site, uint64_t limit_ns) {
   const uint64_t t0 = globaltimer_ns();
   for (uint32_t it = 0;; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
@@ -154,7 +156,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volati
         *abort_flag = 1;
         return false;
       }
-      if (globaltimer_ns() - t0 > WAIT_NS) {
+      if (globaltimer_ns() - t0 > limit_ns) {
         *abort_flag = 1;
         atomicCAS(err, 0, site);
         return false;
@@ -163,7 +165,8 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volati
   }
 }
 
-// Bounded drain wait used on the abort path only.
+// Bounded drain wait used on the abort path only (always the default limit,
+// so that no copy or MMA of this CTA outlives its shared memory or TMEM).
 __device__ __forceinline__ void mbar_drain(uint64_t* bar, uint32_t parity) {
   const uint64_t t0 = globaltimer_ns();
   while (!mbar_try_wait(bar, parity) && globaltimer_ns() - t0 < WAIT_NS) {
@@ -253,6 +256,7 @@ struct GemmArgs {
   int col0;         // first genotype column of this launch (TMA row offset of G)
   int sq_rows;      // rows [0, sq_rows): write (C^2) as an error-free float pair (hi, lo)
   int* err;         // first failing wait site (0 = ok)
+  unsigned long long wait_ns;  // limit of one pipeline wait
 };
 
 // Grouped launches: one problem per (cohort, trait), tiles listed by the host.
@@ -370,7 +374,7 @@ __device__ __forceinline__ void gemm_tile(const CUtensorMap* tmA, const CUtensor
         const int s0 = 2 * p, s1 = 2 * p + 1;
         const bool two = s1 < g.S;
         for (int kb = 0; kb < nk; kb++) {
-          if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, g.err, 1)) { ok = false; break; }
+          if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, g.err, 1, g.wait_ns)) { ok = false; break; }
           issued[stage] = 0;
           uint8_t* sb = smem + stage * R::STAGE;
           mbar_expect_tx(&full[stage], (two ? 2 * R::A : R::A) + R::B);
@@ -396,10 +400,10 @@ __device__ __forceinline__ void gemm_tile(const CUtensorMap* tmA, const CUtensor
       bool any = false;
       for (int p = 0; p < passes && ok; p++) {
         const bool two = 2 * p + 1 < g.S;
-        if (!mbar_wait(tempty, (p & 1) ^ 1, abort_flag, g.err, 2)) { ok = false; break; }
+        if (!mbar_wait(tempty, (p & 1) ^ 1, abort_flag, g.err, 2, g.wait_ns)) { ok = false; break; }
         tc_fence_after();
         for (int kb = 0; kb < nk; kb++) {
-          if (!mbar_wait(&full[stage], phase, abort_flag, g.err, 3)) { ok = false; break; }
+          if (!mbar_wait(&full[stage], phase, abort_flag, g.err, 3, g.wait_ns)) { ok = false; break; }
           tc_fence_after();
           uint8_t* sb = smem + stage * R::STAGE;
           const uint64_t a0 = desc_gemm<R::ROW>(sb), a1 = desc_gemm<R::ROW>(sb + R::A),
@@ -453,7 +457,7 @@ __device__ __forceinline__ void gemm_tile(const CUtensorMap* tmA, const CUtensor
         for (int c = cbeg; c < cend; c++)
           asm volatile("prefetch.global.L2 [%0];" ::"l"(crow + (long long)c * g.ldc));
       int ok = 1;
-      if (lane == 0) ok = mbar_wait(tfull, p & 1, abort_flag, g.err, 4) ? 1 : 0;
+      if (lane == 0) ok = mbar_wait(tfull, p & 1, abort_flag, g.err, 4, g.wait_ns) ? 1 : 0;
       ok = __shfl_sync(0xffffffffu, ok, 0);  // warp-uniform: tcgen05.ld is .sync.aligned
       if (!ok) break;
       tc_fence_after();
@@ -581,6 +585,7 @@ struct QuadArgs {
   const int* dexp;  // per trait: tau_j = 2^dexp
   double* part;     // QT_SLOTS partial planes of Ncap x tgp (column-major, ld Ncap)
   int* err;
+  unsigned long long wait_ns;  // limit of one pipeline wait
 };
 
 // Work units are dealt to the persistent CTAs in contiguous ranges, unit
@@ -679,7 +684,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         int nt = 0;
         for (int q = 0; q < 4; q++) nt += qp.t[p][q] > 0 ? 1 : 0;
         for (int kb = 0; kb < nk; kb++) {
-          if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, g.err, 11)) { ok = false; break; }
+          if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, g.err, 11, g.wait_ns)) { ok = false; break; }
           issued[stage] = 0;
           uint8_t* sb = smem + stage * QT_STAGE;
           mbar_expect_tx(&full[stage], A_TILE + nt * QT_BT);
@@ -709,10 +714,10 @@ __global__ void __launch_bounds__(THREADS, 1)
         // a slot pair with its second slot empty needs only the first slot's columns
         const uint32_t id01 = qp.t[p][1] > 0 ? QT_IDESC : QT_IDESC1;
         const uint32_t id23 = qp.t[p][3] > 0 ? QT_IDESC : QT_IDESC1;
-        if (!mbar_wait(tempty, (lu & 1) ^ 1, abort_flag, g.err, 12)) { ok = false; break; }
+        if (!mbar_wait(tempty, (lu & 1) ^ 1, abort_flag, g.err, 12, g.wait_ns)) { ok = false; break; }
         tc_fence_after();
         for (int kb = 0; kb < nk; kb++) {
-          if (!mbar_wait(&full[stage], phase, abort_flag, g.err, 13)) { ok = false; break; }
+          if (!mbar_wait(&full[stage], phase, abort_flag, g.err, 13, g.wait_ns)) { ok = false; break; }
           tc_fence_after();
           uint8_t* sb = smem + stage * QT_STAGE;
           const uint64_t a = desc_sw128(sb), b01 = desc_sw128(sb + A_TILE), b23 = desc_sw128(sb + A_TILE + 2 * QT_BT);
@@ -752,7 +757,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         const int lu = u - u0;
         const int p = u - tile * np;
         int ok = 1;
-        if (lane == 0) ok = mbar_wait(tfull, lu & 1, abort_flag, g.err, 14) ? 1 : 0;
+        if (lane == 0) ok = mbar_wait(tfull, lu & 1, abort_flag, g.err, 14, g.wait_ns) ? 1 : 0;
         ok = __shfl_sync(0xffffffffu, ok, 0);
         if (!ok) { done = false; break; }
         tc_fence_after();
@@ -1161,6 +1166,7 @@ struct OzakiPlan {
   CUtensorMap mapA, mapB;
   bool maps = false;
   int sub = 0;                      // SNPs per pipelined sub-block (multiple of BN)
+  unsigned long long wait_ns = WAIT_NS;  // limit of one wait in the tcgen05 kernels
 };
 
 cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_b, int slices, int eigen) {
@@ -1287,6 +1293,7 @@ cudaError_t run_gemm(OzakiPlan* p, cudaStream_t s, int col0, int x, int tri_rows
   g.C = p->C;
   g.ldc = p->Mpad;
   g.err = p->err;
+  g.wait_ns = p->wait_ns;
   ozaki_gemm_kernel<<<g.tiles_m * g.tiles_n, THREADS, SMEM_BYTES, s>>>(p->mapA, p->mapB, g);
   note_launch();
   return cudaGetLastError();
@@ -1320,6 +1327,7 @@ cudaError_t selfgram(OzakiPlan* p, cudaStream_t s, int col0, int xq, int t, doub
   g.dexp = p->dexp;
   g.part = p->qpart;
   g.err = p->err;
+  g.wait_ns = p->wait_ns;
   // persistent CTAs, at most one per SM, each with >= half a tile's passes
   // (so a tile spans at most QT_SLOTS CTAs)
   const int ctas = std::max(1, std::min(p->sms, g.units / ((p->qp.n + 1) / 2)));
@@ -1415,11 +1423,9 @@ const double* ozaki_gram_rows(const OzakiPlan* p, long long* ld) {
   return p->C + p->n;
 }
 
-int ozaki_read_error(OzakiPlan* p) {
-  int h = 0;
-  cudaMemcpy(&h, p->err, sizeof(int), cudaMemcpyDeviceToHost);
-  return h;
-}
+int* ozaki_error_word(OzakiPlan* p) { return p->err; }
+
+void ozaki_set_wait_limit(OzakiPlan* p, unsigned long long ns) { p->wait_ns = ns ? ns : WAIT_NS; }
 
 // ---------------------------------------------------------------------------
 // Batched cohorts: the split operand of one chol problem into caller buffers,
@@ -1527,6 +1533,7 @@ cudaError_t grouped_gemm_create(GroupedGemm** out, const GroupedGemmDesc* d, int
     g.col0 = 0;
     g.sq_rows = d[i].sq_rows;
     g.err = err;
+    g.wait_ns = WAIT_NS;
     probs[i].cohort = d[i].cohort;
     probs[i].pad = 0;
     FGLS_CUDA_TRY(make_map_box(&maps[2 * i], d[i].A, d[i].Kpad, (long long)d[i].S_alloc * d[i].Mpad, BM, GRBK, 2));
@@ -1668,7 +1675,8 @@ extern "C" int fglsgpu_selftest_split_gemm(int M, int K, int N, int S, const dou
 // calls that overlap on the GPU (several streams or threads at once) race on
 // it and must be serialised by the caller.  The first call on a device looks
 // up the array's device address (cudaGetSymbolAddress) with that device
-// current; make that first call before any stream capture.
+// current; make that first call before any stream capture.  Every call reads
+// the kernel's error word back and synchronizes `stream` before it returns.
 // ---------------------------------------------------------------------------
 namespace fgls {
 namespace oz {
@@ -1680,7 +1688,10 @@ constexpr size_t NA_BYTES = NA_A_BYTES + NA_G_BYTES + NA_SCALE_BYTES + 256;  // 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
 
 constexpr int NA_MAX_DEVICES = 64;
-static void* g_noalloc_addr[NA_MAX_DEVICES];
+// device address of g_noalloc_scratch per device ordinal, set once; atomic
+// because host threads may make their first call on a device concurrently
+// (they then store the same address)
+static std::atomic<void*> g_noalloc_addr[NA_MAX_DEVICES];
 }  // namespace oz
 }  // namespace fgls
 
@@ -1693,7 +1704,8 @@ extern "C" int fglsgpu_split_gemm_noalloc(int M, int K, int N, int slices, const
     return FGLSGPU_EINVAL;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NA_MAX_DEVICES) return FGLSGPU_ENODEV;
-  if (!g_noalloc_addr[dev]) {
+  void* addr = g_noalloc_addr[dev].load(std::memory_order_acquire);
+  if (!addr) {
     // set-up, once per device, with the device current: the host-side name of
     // the array is not a device address
     void* ptr = nullptr;
@@ -1701,9 +1713,10 @@ extern "C" int fglsgpu_split_gemm_noalloc(int M, int K, int N, int slices, const
     if (cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) !=
         cudaSuccess)
       return FGLSGPU_ECUDA;
-    g_noalloc_addr[dev] = ptr;
+    g_noalloc_addr[dev].store(ptr, std::memory_order_release);
+    addr = ptr;
   }
-  unsigned char* base = (unsigned char*)g_noalloc_addr[dev];
+  unsigned char* base = (unsigned char*)addr;
   OzakiPlan p;
   p.n = K;
   p.S = slices;
@@ -1752,6 +1765,7 @@ extern "C" int fglsgpu_split_gemm_noalloc(int M, int K, int N, int slices, const
     g.col0 = 0;
     g.sq_rows = 0;
     g.err = p.err;
+    g.wait_ns = WAIT_NS;
     ozaki_gemm_kernel<<<g.tiles_m * g.tiles_n, THREADS, SMEM_BYTES, s>>>(p.mapA, p.mapB, g);
     note_launch();
     chk(cudaGetLastError());

@@ -35,7 +35,12 @@ double ozaki_flops_per_snp(const OzakiPlan* p);
 // Rows [n, n + nU) of the last block's split GEMM output: the Gram terms
 // x~^T y~_j, x~^T XL~_j; element (SNP i, q) at ptr[q + i * ld].
 const double* ozaki_gram_rows(const OzakiPlan* p, long long* ld);
-int ozaki_read_error(OzakiPlan* p);
+// The plan's device error word: the first pipeline-wait site of a tcgen05
+// kernel that gave up (0 = none).  It stays set, and later launches of the
+// plan abort, until the host reads and clears it.
+int* ozaki_error_word(OzakiPlan* p);
+// Limit of one pipeline wait in the plan's tcgen05 kernels (0: 2 s).
+void ozaki_set_wait_limit(OzakiPlan* p, unsigned long long ns);
 
 // ---- batched cohorts (fgls_batch.cu) -------------------------------------
 struct StepCohort;

@@ -108,6 +108,88 @@ def make_problem(n: int, m: int, t: int, wXL: int = 3, wXR: int = 1, seed: int =
                    XL=XL, XR=XR, Y=Y, meta={"seed": seed})
 
 
+def _reflect_sym(A: np.ndarray, v: np.ndarray) -> None:
+    """A <- H A H in place for symmetric A (Fortran order) and H = I - 2 v v^T,
+    |v| = 1: A - 2 (v w'^T + w' v^T) with w = A v, w' = w - (v^T w) v."""
+    from scipy.linalg.blas import dger
+    w = A @ v
+    w -= (v @ w) * v
+    dger(-2.0, v, w, a=A, overwrite_a=True)
+    dger(-2.0, w, v, a=A, overwrite_a=True)
+
+
+def _reflect_left(Q: np.ndarray, v: np.ndarray) -> None:
+    """Q <- H Q in place (Fortran order), H = I - 2 v v^T."""
+    from scipy.linalg.blas import dger
+    dger(-2.0, v, v @ Q, a=Q, overwrite_a=True)
+
+
+def known_spectrum_kinship(rng: np.random.Generator, n: int, markers: int | None = None):
+    """A kinship matrix with a known eigendecomposition, built in O(n^2 log n).
+
+    The spectrum is that of G G^T / k + 1e-3 I for standardized genotypes G
+    (n x k, k = markers, default n/2): k eigenvalues spread over the
+    Marchenko-Pastur support [(sqrt(n/k) - 1)^2, (sqrt(n/k) + 1)^2] plus 1e-3,
+    and n - k eigenvalues equal to 1e-3 (a degenerate cluster, as in a real
+    kinship of rank k).  The eigenvectors are Q = H1 H2 F: F the orthonormal
+    DCT-II matrix (dense, delocalised columns) and H1, H2 Householder
+    reflectors along random directions.  Phi = Q diag(d) Q^T is formed as
+    H1 H2 (F d F^T) H2 H1 with F d F^T = dct(d * idct(I)), then symmetrised.
+
+    Returns (Phi, W, Z): W ascending, Z the matching columns of Q, so that
+    (W, Z) is an exact eigendecomposition of Phi up to the rounding of its
+    construction (|Phi Z - Z W| ~ 1e-15 |Phi|)."""
+    import scipy.fft as sfft
+    k = min(n, markers or max(1, n // 2))
+    r = n / k
+    lo, hi = (np.sqrt(r) - 1.0) ** 2, (np.sqrt(r) + 1.0) ** 2
+    lam = np.full(n, 1e-3)
+    lam[:k] += rng.uniform(lo, hi, size=k)
+    d = lam[rng.permutation(n)]
+    v1 = rng.standard_normal(n)
+    v1 /= np.linalg.norm(v1)
+    v2 = rng.standard_normal(n)
+    v2 /= np.linalg.norm(v2)
+    eye = np.eye(n, order="F")
+    Ft = sfft.idct(eye, axis=0, norm="ortho", workers=-1)          # F^T (columns F^-1 e_j)
+    Ft *= d[:, None]
+    Phi = np.asfortranarray(sfft.dct(Ft, axis=0, norm="ortho", workers=-1))  # F d F^T
+    del Ft
+    _reflect_sym(Phi, v2)
+    _reflect_sym(Phi, v1)
+    Phi += Phi.T  # exactly symmetric: fl(a + b) = fl(b + a)
+    Phi *= 0.5
+    Q = np.asfortranarray(sfft.dct(eye, axis=0, norm="ortho", workers=-1))   # F
+    del eye
+    _reflect_left(Q, v2)
+    _reflect_left(Q, v1)
+    idx = np.argsort(d, kind="stable")
+    return Phi, d[idx].copy(), np.asfortranarray(Q[:, idx])
+
+
+def make_problem_known_spectrum(n: int, m: int, t: int, wXL: int = 3, wXR: int = 1, seed: int = 0,
+                                markers: int | None = None):
+    """As make_problem with h ~ U(0.1, 0.9), sigma ~ U(0.5, 2), but the
+    kinship from known_spectrum_kinship, so that an FP64 reference can use
+    the exact eigendecomposition at any n.  Traits y_j = Z (sqrt(sigma_j
+    (h_j W + 1 - h_j)) * N(0, I)), i.e. covariance sigma_j (h_j Phi + (1 - h_j) I).
+    Returns (Problem, W, Z)."""
+    rng = np.random.default_rng(seed)
+    Phi, W, Z = known_spectrum_kinship(rng, n, markers)
+    hv = rng.uniform(0.1, 0.9, size=t)
+    sv = rng.uniform(0.5, 2.0, size=t)
+    XL = np.empty((n, wXL))
+    XL[:, 0] = 1.0
+    if wXL > 1:
+        XL[:, 1:] = rng.standard_normal((n, wXL - 1))
+    XR = hardcall_genotypes(rng, n, m * wXR)
+    sd = np.sqrt(sv[None, :] * (hv[None, :] * W[:, None] + (1.0 - hv[None, :])))
+    Y = Z @ (sd * rng.standard_normal((n, t)))
+    pb = Problem(n=n, m=m, t=t, wXL=wXL, wXR=wXR, Phi=Phi, h=hv, sigma=sv, XL=XL, XR=XR, Y=Y,
+                 meta={"seed": seed, "kinship": "known spectrum"})
+    return pb, W, Z
+
+
 FILES = ("Phi.in", "H.in", "Sig.in", "XL.in", "XR.in", "Y.in")
 
 

@@ -42,7 +42,7 @@ EXPORTS = (
     "fglsgpu_batch_create", "fglsgpu_batch_destroy", "fglsgpu_batch_params", "fglsgpu_batch_step",
     "fglsgpu_batch_sync", "fglsgpu_batch_stream", "fglsgpu_batch_last_error", "fglsgpu_batch_profile",
     "fglsgpu_batch_profile_read", "fglsgpu_run_block_device_packed", "fglsgpu_run_snps_compact",
-    "fglsgpu_reml_fit", "fglsgpu_set_hsigma",
+    "fglsgpu_reml_fit", "fglsgpu_set_hsigma", "fglsgpu_set_wait_limit",
 )
 PROF_CLASSES = ("genotypes", "split_gemm", "selfgram", "solve", "fp64_gemm", "trsm", "gram", "spare")
 
@@ -111,6 +111,7 @@ def lib():
     L.fglsgpu_reml.argtypes = [P, P, P]
     L.fglsgpu_reml_fit.argtypes = [P, C.c_double, C.c_double, I, P, P, P, P]
     L.fglsgpu_set_hsigma.argtypes = [P, P, P]
+    L.fglsgpu_set_wait_limit.argtypes = [P, LL]
     L.fglsgpu_pvalues_device.argtypes = [P, P, P, I, LL, LL, P, LL]
     L.fglsgpu_batch_create.argtypes = [C.POINTER(CohortDesc), I, C.POINTER(BatchConfig), C.POINTER(P)]
     L.fglsgpu_batch_destroy.argtypes = [P]
@@ -207,6 +208,10 @@ class Engine:
              self.L.fglsgpu_run_block_device_u8 if u8 else self.L.fglsgpu_run_block_device)
         self._check(f(self._h, C.c_void_p(xr_ptr), int(x), C.c_void_p(b_ptr), C.c_void_p(v_ptr),
                       int(bstride), int(vstride)))
+
+    def set_wait_limit(self, ns=0):
+        """Limit of one tcgen05 pipeline wait in ns (0: the 2 s default)."""
+        self._check(self.L.fglsgpu_set_wait_limit(self._h, int(ns)))
 
     def set_precision(self, precision):
         self._check(self.L.fglsgpu_set_precision(self._h, PRECISION[precision]))

@@ -215,6 +215,16 @@ int fglsgpu_set_hsigma(fglsgpu_engine *e, const double *h, const double *sigma);
  * needs select_trait again). */
 int fglsgpu_set_precision(fglsgpu_engine *e, int precision);
 
+/* Limit of one pipeline wait (on an mbarrier: a TMA copy landing, an MMA
+ * finishing, an epilogue draining TMEM) inside the split path's tcgen05
+ * kernels, in nanoseconds; 0 restores the default of 2 s.  A wait that
+ * runs out makes the kernel set an error word, let its own copies and MMAs
+ * finish, free its TMEM and return; the next fglsgpu_sync (or the status
+ * check of a host-API call) reports FGLSGPU_ETIMEOUT, clears the word and
+ * the engine runs normally again.  No counterpart in the reference (its
+ * only device work is cuBLAS, src/fgls_chol_gpu.c:550). */
+int fglsgpu_set_wait_limit(fglsgpu_engine *e, long long ns);
+
 /* Per-kernel-class device time, measured with CUDA events recorded on the
  * engine's compute stream around each class of launches. */
 #define FGLSGPU_PROF_GENOTYPES 0  /* genotype widening / BF16 operand build     */
@@ -260,7 +270,8 @@ int fglsgpu_selftest_split_gemm(int M, int K, int N, int slices, const double *A
  * The kernel's scratch lives in a fixed 5.8 MB array inside the library
  * (held by every GPU that loads it): M <= 256, K <= 2048, N <= 512,
  * slices <= 9, else FGLSGPU_EINVAL.  Runs on `stream` (a cudaStream_t, NULL
- * for the default stream) and returns after it finished.  Calls share the
+ * for the default stream), reads the kernel's error word back and returns
+ * after the stream has finished (it synchronizes the stream).  Calls share the
  * array: calls that overlap on the GPU race; serialise them.  The first call
  * on a device sets up the array's address and should come before any stream
  * capture.  No counterpart in the reference. */

@@ -4,14 +4,16 @@
 # as the parity checker and the timed CPU baseline.  Nothing here is part of
 # the shipped library.
 #
-#   usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+#   usage: oracle/build_ref.sh [REFERENCE_ROOT]
+#   (default: $FGLS_REFERENCE_ROOT, else DEFAULT_REF below)
 #
 # The reference links a Fortran-ABI BLAS/LAPACK (src/blas.h, src/lapack.h).
 # This image has no system BLAS; scipy ships OpenBLAS with every symbol
 # prefixed "scipy_".  We rename the undefined references in OUR objects with
 # objcopy and link against that library.  Outputs go to oracle/_ref/ only.
 set -euo pipefail
-REF=${1:-/root/reference}
+DEFAULT_REF=/root/reference
+REF=${1:-${FGLS_REFERENCE_ROOT:-$DEFAULT_REF}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 if [ ! -d "$REF/src" ]; then

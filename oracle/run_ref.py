@@ -14,6 +14,19 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 DRIVER = os.path.join(HERE, "_ref", "driver.x")
 
 
+def reference_root() -> str:
+    """Root of the reference checkout whose sources build_ref.sh compiles:
+    $FGLS_REFERENCE_ROOT, else the default that build_ref.sh names."""
+    env = os.environ.get("FGLS_REFERENCE_ROOT")
+    if env:
+        return env
+    with open(os.path.join(HERE, "build_ref.sh")) as f:
+        for line in f:
+            if line.startswith("DEFAULT_REF="):
+                return line.split("=", 1)[1].strip().strip('"')
+    return ""
+
+
 def available() -> bool:
     return os.path.exists(DRIVER)
 

@@ -33,6 +33,18 @@ def load_golden(name):
     return pb, str(z["variant"]), xb, B, V
 
 
+def report(case, **values):
+    """Appends one JSON line {case, values} to the file named by
+    FGLS_TEST_REPORT (when set), so that a run can keep the measured errors
+    behind each tolerance; does nothing otherwise."""
+    path = os.environ.get("FGLS_TEST_REPORT")
+    if not path:
+        return
+    import json
+    with open(path, "a") as f:
+        f.write(json.dumps({"case": case, **values}, default=float) + "\n")
+
+
 @pytest.fixture(scope="session")
 def has_gpu():
     try:

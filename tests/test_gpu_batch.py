@@ -3,12 +3,13 @@ the oracle's chol restatement (src/fgls_chol.c:251-438), through ragged
 steps, graph replay, idle cohorts and the autotuner.
 
 Tolerances are those of the single-problem split chol path: beta within
-1e-10 of the FP64 oracle on the (|beta| + SE) scale and 1e-9 normwise, SE
+1e-10 of the FP64 oracle on the (|beta| + SE) scale and normwise, SE
 within 1e-10 relative.
 """
 import numpy as np
 import pytest
 
+from conftest import report
 from oracle import fgls_oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -66,7 +67,8 @@ def check(pbs, out):
         Br, Vr = O.fgls_chol(pb)
         d = O.compare(B, V, Br, Vr)
         assert d["finite"] and d["upper_abs_max"] == 0.0, (pb.n, d)
-        assert d["beta_se_scaled"] <= 1e-10 and d["beta_normwise"] <= 1e-9, (pb.n, pb.p, d)
+        report(f"batch_n{pb.n}_p{pb.p}", **d)
+        assert d["beta_se_scaled"] <= 1e-10 and d["beta_normwise"] <= 1e-10, (pb.n, pb.p, d)
         assert d["se_rel"] <= 1e-10, (pb.n, pb.p, d)
 
 

@@ -5,9 +5,11 @@ points).
 Tolerances (FP64 path):
 * chol: beta normwise per (trait, SNP) <= 1e-12, standard errors element-wise
   <= 1e-12, off-diagonal covariances normwise <= 1e-12, strict upper == 0.
-* eigen: |dbeta_k| / (|beta_k| + SE_k) <= 1e-11 and SE <= 1e-11: the
-  eigenvector route amplifies rounding on near-zero coefficients (the
-  reference's own chol and eigen outputs differ by ~2e-12 normwise there).
+* eigen: |dbeta_k| / (|beta_k| + SE_k) <= 1e-12, SE and off-diagonal
+  covariances <= 1e-12 (measured at most 2e-13, 2e-14 and 5e-15 over these
+  cases and at n = 10000).  Beta is not gated normwise: the eigenvector route
+  amplifies rounding on near-zero coefficients (measured up to 1.8e-12
+  normwise; the reference's own chol and eigen outputs differ by ~6e-13 there).
 """
 import os
 import tempfile
@@ -15,16 +17,18 @@ import tempfile
 import numpy as np
 import pytest
 
-from conftest import golden_cases, load_golden
+from conftest import golden_cases, load_golden, report
 from oracle import fgls_oracle as O
 
 pytestmark = pytest.mark.gpu
 
 CHOL_TOL = dict(beta_normwise=1e-12, se_rel=1e-12, v_offdiag_normwise=1e-12)
-EIGEN_TOL = dict(beta_se_scaled=1e-11, se_rel=1e-11, v_offdiag_normwise=1e-11)
+EIGEN_TOL = dict(beta_se_scaled=1e-12, se_rel=1e-12, v_offdiag_normwise=1e-12)
 
 
-def check(d, tol):
+def check(d, tol, case=None):
+    if case:
+        report(case, **d)
     assert d["finite"], d
     assert d["upper_abs_max"] == 0.0, d
     for k, v in tol.items():
@@ -51,7 +55,7 @@ def test_engine_vs_reference_golden(name):
     pb, var, xb, Bref, Vref = load_golden(name)
     variant = "chol" if var == "c" else "eigen"
     B, V = run_engine(pb, variant, xb)
-    check(O.compare(B, V, Bref, Vref), CHOL_TOL if var == "c" else EIGEN_TOL)
+    check(O.compare(B, V, Bref, Vref), CHOL_TOL if var == "c" else EIGEN_TOL, f"golden_engine_{name}")
 
 
 @pytest.mark.parametrize("name", golden_cases())
@@ -84,7 +88,8 @@ def test_engine_vs_oracle_shapes(n, m, t, wXL, wXR, xb, variant):
     pb = datagen.make_problem(n, m, t, wXL=wXL, wXR=wXR, seed=n + m, hsig_uniform=True)
     B, V = run_engine(pb, variant, xb)
     Br, Vr = O.fgls_chol(pb, xb) if variant == "chol" else O.fgls_eigen(pb)
-    check(O.compare(B, V, Br, Vr), CHOL_TOL if variant == "chol" else EIGEN_TOL)
+    check(O.compare(B, V, Br, Vr), CHOL_TOL if variant == "chol" else EIGEN_TOL,
+          f"shapes_{variant}_n{n}_m{m}_t{t}_wxl{wXL}_wxr{wXR}")
 
 
 def test_chol_larger_n_vs_oracle():

@@ -52,7 +52,30 @@ def test_chol_and_eigen_oracles_agree():
     assert d["beta_se_scaled"] < 1e-11 and d["se_rel"] < 1e-11, d
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/test_cases/test_XL"), reason="reference fixture absent")
+def test_known_spectrum_kinship_is_exact():
+    """The generator's (W, Z) is an eigendecomposition of its Phi to rounding,
+    its spectrum has the degenerate 1e-3 cluster of a rank-n/2 kinship, and
+    the oracle gives the same results from it as from scipy's dsyevr."""
+    from fgls_gb300 import datagen
+    pb, W, Z = datagen.make_problem_known_spectrum(240, 40, 3, seed=8)
+    nrm = np.abs(W).max()
+    assert np.all(np.diff(W) >= 0) and np.sum(W == 1e-3) == 120
+    assert np.abs(pb.Phi @ Z - Z * W).max() <= 1e-14 * nrm
+    assert np.abs(Z.T @ Z - np.eye(pb.n)).max() <= 1e-14
+    assert np.abs(pb.Phi - pb.Phi.T).max() == 0.0
+    assert np.abs(Z).max() < 0.5  # delocalised eigenvectors
+    B1, V1 = O.fgls_eigen(pb, W, Z)
+    B2, V2 = O.fgls_eigen(pb)
+    d = O.compare(B1, V1, B2, V2)
+    assert d["beta_se_scaled"] < 1e-12 and d["se_rel"] < 1e-12, d
+
+
+def _reference_fixture():
+    from oracle import run_ref
+    return os.path.join(run_ref.reference_root(), "test_cases", "test_XL")
+
+
+@pytest.mark.skipif(not os.path.isdir(_reference_fixture()), reason="reference fixture absent")
 def test_oracle_on_reference_fixture_inputs():
     """The reference's own fixture inputs (test_cases/test_XL: n=500, t=20,
     wXL=3; its XR.in is missing) with a synthetic XR, run through the
@@ -61,7 +84,7 @@ def test_oracle_on_reference_fixture_inputs():
     from fgls_gb300 import datagen
     if not run_ref.available():
         pytest.skip("reference driver not built")
-    src = "/root/reference/test_cases/test_XL"
+    src = _reference_fixture()
     n, t, wXL, m = 500, 4, 3, 64
     d = tempfile.mkdtemp()
     for f in ("Phi.in", "H.in", "Sig.in", "XL.in", "Y.in"):
