@@ -23,6 +23,17 @@
 // (src/fgls_chol.c:467,474).  FGLS_STOP_AFTER=k (host-side interruption for
 // tests) exits with status 3 after k newly journaled blocks.
 //
+// Genotype file formats (FGLS_XR_FORMAT, opt-in; the reference reads FP64
+// only, src/fgls_chol.c:333-337):
+//   f64 (default)  the reference's XR.in: m*wXR columns of n doubles;
+//   u8             the same layout with one byte (0/1/2) per individual;
+//   bed            a SNP-major PLINK .bed file: the magic bytes 6c 1b 01, then
+//                  m*wXR columns of ceil(n/4) bytes, 2 bits per individual
+//                  (00 -> 2, 10 -> 1, 11 -> 0 copies of the first allele,
+//                  01 missing: an error naming the SNP and the individual).
+// Only the bytes of the chosen format cross the host link (8x or 32x fewer
+// than FP64); the device widens them per block.
+//
 // Errors print "[Error]: <msg>" and exit(EXIT_FAILURE) like the reference's
 // error_msg(msg, 1) (src/common.c:11-17).  Unlike the reference's sync_read,
 // which prints and continues on a short read (src/io.c:13-16), a short read
@@ -101,9 +112,34 @@ struct Item {
   bool read;       // from disk (else from the HBM cache)
 };
 
+enum { XR_F64 = 0, XR_U8 = 1, XR_BED = 2 };
+
+int xr_format() {
+  const char* f = getenv("FGLS_XR_FORMAT");
+  if (!f || !*f || !strcmp(f, "f64")) return XR_F64;
+  if (!strcmp(f, "u8")) return XR_U8;
+  if (!strcmp(f, "bed")) return XR_BED;
+  die(std::string("FGLS_XR_FORMAT=") + f + ": expected f64, u8 or bed");
+}
+
+// First missing call (2-bit code 01) of a .bed body region of `cols`
+// columns starting at column c0: (column, individual), or (-1, -1).
+std::pair<long long, int> find_missing_bed(int fd, off_t data_off, int n, long long c0, long long cols) {
+  const long long bpc = (n + 3) / 4;
+  std::vector<unsigned char> col((size_t)bpc);
+  for (long long c = c0; c < c0 + cols; c++) {
+    if (!pread_full(fd, col.data(), (size_t)bpc, data_off + (off_t)(c * bpc))) break;
+    for (int k = 0; k < n; k++)
+      if (((col[k >> 2] >> (2 * (k & 3))) & 3) == 1) return {c, k};
+  }
+  return {-1, -1};
+}
+
 struct Slot {
-  double *hX = nullptr, *hB = nullptr, *hV = nullptr;
-  double *dX = nullptr, *dB = nullptr, *dV = nullptr;
+  unsigned char* hX = nullptr;  // genotype bytes of one block (format of the XR file)
+  double *hB = nullptr, *hV = nullptr;
+  unsigned char* dX = nullptr;
+  double *dB = nullptr, *dV = nullptr;
   cudaEvent_t evH{}, evC{}, evD{};
   std::thread reader;
   bool read_ok = true;
@@ -147,6 +183,14 @@ int run_variant(int variant, int n, int p, int m, int t, int wXL, int wXR, int x
 
   int xr_fd = open(XR_path, O_RDONLY);
   if (xr_fd < 0) die(std::string("cannot open XR file ") + XR_path + ": " + strerror(errno));
+  const int fmt = xr_format();
+  off_t xr_off = 0;  // first genotype byte of the file
+  if (fmt == XR_BED) {
+    unsigned char magic[3] = {0, 0, 0};
+    if (!pread_full(xr_fd, magic, 3, 0) || magic[0] != 0x6c || magic[1] != 0x1b || magic[2] != 0x01)
+      die(std::string("XR file ") + XR_path + " is not a SNP-major PLINK .bed (magic bytes 6c 1b 01)");
+    xr_off = 3;
+  }
   // resume journal: header line, then one "<trait> <first SNP>" line per finished block
   const char* rs = getenv("FGLS_RESUME");
   const bool resume = rs && atoi(rs) != 0;
@@ -188,18 +232,19 @@ int run_variant(int variant, int n, int p, int m, int t, int wXL, int wXR, int x
   }
 
   const int nt = variant == FGLSGPU_VARIANT_EIGEN ? t : 1;
-  const long long colb = (long long)n * wXR;  // doubles per SNP
+  const long long bpc = fmt == XR_F64 ? 8LL * n : fmt == XR_U8 ? (long long)n : (long long)(n + 3) / 4;
+  const long long colb = bpc * wXR;  // genotype bytes per SNP
   cudaStream_t comp = (cudaStream_t)fglsgpu_stream(e);
   cudaStream_t h2d, d2h;
   cuda_check(cudaStreamCreateWithFlags(&h2d, cudaStreamNonBlocking), "stream");
   cuda_check(cudaStreamCreateWithFlags(&d2h, cudaStreamNonBlocking), "stream");
 
   // Keep XR resident in HBM across chol traits when it fits.
-  double* dXall = nullptr;
+  unsigned char* dXall = nullptr;
   if (variant == FGLSGPU_VARIANT_CHOL && t > 1 && done.empty()) {
     size_t fr = 0, tot = 0;
     cudaMemGetInfo(&fr, &tot);
-    const size_t need = sizeof(double) * (size_t)colb * m;
+    const size_t need = (size_t)colb * m;
     if (need + ((size_t)4 << 30) < fr) {
       if (cudaMalloc((void**)&dXall, need) != cudaSuccess) {
         cudaGetLastError();
@@ -210,10 +255,10 @@ int run_variant(int variant, int n, int p, int m, int t, int wXL, int wXR, int x
 
   Slot sl2[2];
   for (Slot& s : sl2) {
-    cuda_check(cudaMallocHost((void**)&s.hX, sizeof(double) * colb * x_b), "pinned XR slot");
+    cuda_check(cudaMallocHost((void**)&s.hX, (size_t)colb * x_b), "pinned XR slot");
     cuda_check(cudaMallocHost((void**)&s.hB, sizeof(double) * nt * x_b * p), "pinned B slot");
     cuda_check(cudaMallocHost((void**)&s.hV, sizeof(double) * nt * x_b * p * p), "pinned V slot");
-    cuda_check(cudaMalloc((void**)&s.dX, sizeof(double) * colb * x_b), "XR slot");
+    cuda_check(cudaMalloc((void**)&s.dX, (size_t)colb * x_b), "XR slot");
     cuda_check(cudaMalloc((void**)&s.dB, sizeof(double) * nt * x_b * p), "B slot");
     cuda_check(cudaMalloc((void**)&s.dV, sizeof(double) * nt * x_b * p * p), "V slot");
     cuda_check(cudaEventCreateWithFlags(&s.evH, cudaEventDisableTiming), "event");
@@ -242,8 +287,8 @@ int run_variant(int variant, int n, int p, int m, int t, int wXL, int wXR, int x
     const Item& it = items[i];
     s.read_ok = true;
     if (!it.read) return;
-    s.reader = std::thread([&s, xr_fd, colb, it]() {
-      s.read_ok = pread_full(xr_fd, s.hX, sizeof(double) * colb * it.x, (off_t)(sizeof(double) * colb * it.ib));
+    s.reader = std::thread([&s, xr_fd, xr_off, colb, it]() {
+      s.read_ok = pread_full(xr_fd, s.hX, (size_t)colb * it.x, xr_off + (off_t)(colb * it.ib));
     });
   };
   auto write_out = [&](int i) {
@@ -271,6 +316,20 @@ int run_variant(int variant, int n, int p, int m, int t, int wXL, int wXR, int x
     }
   };
 
+  // Device failures are read at trait ends (chol) and at the end; a missing
+  // call in a .bed file is reported with its SNP and individual, found by
+  // scanning the file on the host (the device only knows the block).
+  auto sync_check = [&](fglsgpu_engine* eng) {
+    const int rc = fglsgpu_sync(eng);
+    if (rc == FGLSGPU_OK) return;
+    if (rc == FGLSGPU_EINVAL && fmt == XR_BED) {
+      const auto miss = find_missing_bed(xr_fd, xr_off, n, 0, (long long)m * wXR);
+      if (miss.first >= 0)
+        die(std::string("missing genotype (2-bit code 01) in ") + XR_path + " at SNP " +
+            std::to_string(miss.first / wXR) + ", individual " + std::to_string(miss.second));
+    }
+    die(fglsgpu_last_error(eng));
+  };
   if (!items.empty()) start_read(0);
   int cur_trait = -1;
   for (size_t i = 0; i < items.size(); i++) {
@@ -278,18 +337,18 @@ int run_variant(int variant, int n, int p, int m, int t, int wXL, int wXR, int x
     Slot& o = sl2[(i + 1) & 1];
     const Item& it = items[i];
     if (variant == FGLSGPU_VARIANT_CHOL && it.trait != cur_trait) {
-      if (cur_trait >= 0) eng_check(e, fglsgpu_sync(e));  // report device failures of the finished trait
+      if (cur_trait >= 0) sync_check(e);  // report device failures of the finished trait
       eng_check(e, fglsgpu_select_trait(e, it.trait));
       cur_trait = it.trait;
     }
-    const double* src;
+    const unsigned char* src;
     if (it.read) {
       s.reader.join();
       if (!s.read_ok)
         die(std::string("short read of XR file ") + XR_path + " at SNP " + std::to_string(it.ib));
-      double* dst = dXall ? dXall + it.ib * colb : s.dX;
+      unsigned char* dst = dXall ? dXall + it.ib * colb : s.dX;
       cuda_check(cudaStreamWaitEvent(h2d, s.evC, 0), "wait");
-      cuda_check(cudaMemcpyAsync(dst, s.hX, sizeof(double) * colb * it.x, cudaMemcpyHostToDevice, h2d), "XR upload");
+      cuda_check(cudaMemcpyAsync(dst, s.hX, (size_t)colb * it.x, cudaMemcpyHostToDevice, h2d), "XR upload");
       cuda_check(cudaEventRecord(s.evH, h2d), "event");
       cuda_check(cudaStreamWaitEvent(comp, s.evH, 0), "wait");
       src = dst;
@@ -297,7 +356,13 @@ int run_variant(int variant, int n, int p, int m, int t, int wXL, int wXR, int x
       src = dXall + it.ib * colb;
     }
     cuda_check(cudaStreamWaitEvent(comp, s.evD, 0), "wait");
-    eng_check(e, fglsgpu_run_block_device(e, src, it.x, s.dB, s.dV, (long long)it.x * p, (long long)it.x * p * p));
+    const long long bs = (long long)it.x * p, vs = (long long)it.x * p * p;
+    if (fmt == XR_F64)
+      eng_check(e, fglsgpu_run_block_device(e, (const double*)src, it.x, s.dB, s.dV, bs, vs));
+    else if (fmt == XR_U8)
+      eng_check(e, fglsgpu_run_block_device_u8(e, src, it.x, s.dB, s.dV, bs, vs));
+    else
+      eng_check(e, fglsgpu_run_block_device_packed(e, src, it.x, s.dB, s.dV, bs, vs));
     cuda_check(cudaEventRecord(s.evC, comp), "event");
     cuda_check(cudaStreamWaitEvent(d2h, s.evC, 0), "wait");
     cuda_check(cudaMemcpyAsync(s.hB, s.dB, sizeof(double) * nt * it.x * p, cudaMemcpyDeviceToHost, d2h), "B download");
@@ -311,7 +376,7 @@ int run_variant(int variant, int n, int p, int m, int t, int wXL, int wXR, int x
     if (i >= 1) write_out((int)i - 1);
   }
   if (!items.empty()) write_out((int)items.size() - 1);
-  eng_check(e, fglsgpu_sync(e));
+  sync_check(e);
 
   for (Slot& s : sl2) {
     if (s.reader.joinable()) s.reader.join();

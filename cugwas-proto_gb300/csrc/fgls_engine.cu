@@ -44,7 +44,8 @@ struct fglsgpu_engine {
   double *dGYL = nullptr, *dGR = nullptr;
   double *dB[2]{}, *dV[2]{};
   double *dSE[2]{}, *dP[2]{};  // compact outputs (allocated on first use)
-  unsigned char* dU8 = nullptr;
+  unsigned char* dU8 = nullptr;  // unpacked 2-bit genotypes (FP64 path)
+  double* dXw = nullptr;         // byte genotypes widened to FP64 (FP64 path)
   DevStatus* dst = nullptr;
   DevStatus* hst = nullptr;
   int* hst_wait = nullptr;  // pinned copy of the split plan's wait error word
@@ -148,7 +149,7 @@ void free_all(fglsgpu_engine* e) {
                   e->dQ,   e->dGYL, e->dGR,  e->dB[0], e->dB[1], e->dV[0], e->dV[1], e->dU8, e->dst,
                   e->aWc, e->aAYLc, e->aAYLs, e->atopc, e->atops, e->areml, e->aGYLc, e->aGYLs, e->aGRc,
                   e->aGRs, e->acontrib, e->ag, e->agR, e->aacc, e->aU, e->aV2, e->dSE[0], e->dSE[1], e->dP[0],
-                  e->dP[1]};
+                  e->dP[1], e->dXw};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (e->hst) cudaFreeHost(e->hst);
@@ -215,10 +216,18 @@ void stage_hook(void* ctx, int cls, int begin, cudaStream_t st) {
   }
 }
 
-// Compute one block already in device memory (FP64 genotypes at dXin,
-// n x x*wXR) into dB/dV with the given trait strides, on e->comp.
-int compute_block(fglsgpu_engine* e, const double* dXin, const unsigned char* dXu8, int x, double* dB, double* dV,
-                  long long bstr, long long vstr, long long snp_base) {
+// Genotype formats of a block in device memory: FP64, bytes (n values per
+// column) or 2-bit packed (ceil(n/4) bytes per column, PLINK .bed body).
+enum { GENO_F64 = 0, GENO_U8 = 1, GENO_PACKED = 2 };
+
+long long geno_bytes_per_col(int fmt, int n) {
+  return fmt == GENO_F64 ? 8LL * n : fmt == GENO_U8 ? (long long)n : (long long)(n + 3) / 4;
+}
+
+// Compute one block already in device memory (n x x*wXR genotypes in format
+// `fmt` at dX) into dB/dV with the given trait strides, on e->comp.
+int compute_block(fglsgpu_engine* e, const void* dX, int fmt, int x, double* dB, double* dV, long long bstr,
+                  long long vstr, long long snp_base) {
   const fglsgpu_config& c = e->cfg;
   const int n = c.n, wXL = c.wXL, wXR = c.wXR, p = e->p;
   const int t = c.variant == FGLSGPU_VARIANT_EIGEN ? c.t : 1;
@@ -226,8 +235,16 @@ int compute_block(fglsgpu_engine* e, const double* dXin, const unsigned char* dX
   cudaStream_t s = e->comp;
   if (c.variant == FGLSGPU_VARIANT_CHOL && e->trait_sel < 0)
     return fail(e, FGLSGPU_ESTATE, "fglsgpu_select_trait must precede run_block (chol)");
+  const double* dXin = fmt == GENO_F64 ? (const double*)dX : nullptr;
+  const unsigned char* dXu8 = fmt == GENO_U8 ? (const unsigned char*)dX : nullptr;
   if (split(e)) {
-    ENG_TRY(e, ozaki_block(e->oz, s, dXin, dXu8, x, e->dGR, stage_hook, e), "split block");
+    GenoBlock gb;
+    gb.f64 = dXin;
+    gb.u8 = dXu8;
+    gb.packed = fmt == GENO_PACKED ? (const unsigned char*)dX : nullptr;
+    gb.st = e->dst;
+    gb.snp_base = snp_base;
+    ENG_TRY(e, ozaki_block(e->oz, s, gb, x, e->dGR, stage_hook, e), "split block");
     long long ld = 0;
     const double* gyl = ozaki_gram_rows(e->oz, &ld);
     Prof pr(e, FGLSGPU_PROF_SOLVE, s);
@@ -236,10 +253,17 @@ int compute_block(fglsgpu_engine* e, const double* dXin, const unsigned char* dX
             "solve");
     return FGLSGPU_OK;
   }
+  if (fmt == GENO_PACKED) {
+    Prof pr(e, FGLSGPU_PROF_GENOTYPES, s);
+    if (!e->dU8) ENG_TRY(e, dalloc(&e->dU8, (size_t)c.x_b * c.wXR * c.n), "genotype bytes");
+    ENG_TRY(e, unpack_2bit(s, (const unsigned char*)dX, n, cols, wXR, e->dU8, e->dst, snp_base), "unpack genotypes");
+    dXu8 = e->dU8;
+  }
   if (dXu8) {
     Prof pr(e, FGLSGPU_PROF_GENOTYPES, s);
-    ENG_TRY(e, u8_to_f64(s, dXu8, e->dX[1], (long long)cols * n), "widen genotypes");
-    dXin = e->dX[1];
+    if (!e->dXw) ENG_TRY(e, dalloc(&e->dXw, (size_t)c.x_b * c.wXR * c.n), "widened genotypes");
+    ENG_TRY(e, u8_to_f64(s, dXu8, e->dXw, (long long)cols * n), "widen genotypes");
+    dXin = e->dXw;
   }
   if (c.variant == FGLSGPU_VARIANT_CHOL) {
     {
@@ -473,7 +497,7 @@ int fglsgpu_run_block_device(fglsgpu_engine* e, const double* dXR, int x_inc, do
   if (!dXR || !dB || !dV) return fail(e, FGLSGPU_EINVAL, "null block pointer");
   ENG_TRY(e, cudaSetDevice(e->cfg.device), "cudaSetDevice");
   // Device failures accumulate in the status word until fglsgpu_sync.
-  return compute_block(e, dXR, nullptr, x_inc, dB, dV, bstr, vstr, 0);
+  return compute_block(e, dXR, GENO_F64, x_inc, dB, dV, bstr, vstr, 0);
 }
 
 int fglsgpu_run_block_device_u8(fglsgpu_engine* e, const unsigned char* dXR, int x_inc, double* dB, double* dV,
@@ -483,7 +507,7 @@ int fglsgpu_run_block_device_u8(fglsgpu_engine* e, const unsigned char* dXR, int
   if (x_inc <= 0 || x_inc > e->cfg.x_b) return fail(e, FGLSGPU_EINVAL, "x_inc=%d outside [1, %d]", x_inc, e->cfg.x_b);
   ENG_TRY(e, cudaSetDevice(e->cfg.device), "cudaSetDevice");
   if (!dXR || !dB || !dV) return fail(e, FGLSGPU_EINVAL, "null block pointer");
-  return compute_block(e, nullptr, dXR, x_inc, dB, dV, bstr, vstr, 0);
+  return compute_block(e, dXR, GENO_U8, x_inc, dB, dV, bstr, vstr, 0);
 }
 
 int fglsgpu_run_block_device_packed(fglsgpu_engine* e, const unsigned char* dXR2, int x_inc, double* dB, double* dV,
@@ -493,10 +517,7 @@ int fglsgpu_run_block_device_packed(fglsgpu_engine* e, const unsigned char* dXR2
   if (x_inc <= 0 || x_inc > e->cfg.x_b) return fail(e, FGLSGPU_EINVAL, "x_inc=%d outside [1, %d]", x_inc, e->cfg.x_b);
   if (!dXR2 || !dB || !dV) return fail(e, FGLSGPU_EINVAL, "null block pointer");
   ENG_TRY(e, cudaSetDevice(e->cfg.device), "cudaSetDevice");
-  const long long cols = (long long)x_inc * e->cfg.wXR;
-  if (!e->dU8) ENG_TRY(e, dalloc(&e->dU8, (size_t)e->cfg.x_b * e->cfg.wXR * e->cfg.n), "genotype bytes");
-  ENG_TRY(e, unpack_2bit(e->comp, dXR2, e->cfg.n, cols, e->cfg.wXR, e->dU8, e->dst, 0), "unpack genotypes");
-  return compute_block(e, nullptr, e->dU8, x_inc, dB, dV, bstr, vstr, 0);
+  return compute_block(e, dXR2, GENO_PACKED, x_inc, dB, dV, bstr, vstr, 0);
 }
 
 int fglsgpu_sync(fglsgpu_engine* e) {
@@ -522,7 +543,7 @@ int fglsgpu_run_block(fglsgpu_engine* e, const double* XR, int x_inc, double* B,
   ENG_TRY(e, cudaMemcpyAsync(e->dX[0], XR, sizeof(double) * c.n * (size_t)x_inc * c.wXR, cudaMemcpyHostToDevice, s),
           "XR upload");
   const long long db = (long long)x_inc * p, dv = (long long)x_inc * p * p;
-  rc = compute_block(e, e->dX[0], nullptr, x_inc, e->dB[0], e->dV[0], db, dv, 0);
+  rc = compute_block(e, e->dX[0], GENO_F64, x_inc, e->dB[0], e->dV[0], db, dv, 0);
   if (rc) return rc;
   const int nt = out_traits(e);
   ENG_TRY(e, cudaMemcpy2DAsync(B, sizeof(double) * bstr, e->dB[0], sizeof(double) * db, sizeof(double) * db, nt,
@@ -543,8 +564,10 @@ int fglsgpu_run_block(fglsgpu_engine* e, const double* XR, int x_inc, double* B,
 
 namespace {
 
-// Whole-job pipeline over host XR: full (V) or compact (SE, P) outputs.
-int run_snps_impl(fglsgpu_engine* e, const double* XR, long long m, double* B, double* V, double* SE, double* P) {
+// Whole-job pipeline over host XR (format `fmt`): full (V) or compact (SE,
+// P) outputs.
+int run_snps_impl(fglsgpu_engine* e, const void* XR, int fmt, long long m, double* B, double* V, double* SE,
+                  double* P) {
   const bool compact = V == nullptr;
   const fglsgpu_config& c = e->cfg;
   if (c.variant == FGLSGPU_VARIANT_CHOL && e->trait_sel < 0)
@@ -568,7 +591,8 @@ int run_snps_impl(fglsgpu_engine* e, const double* XR, long long m, double* B, d
   int rc = reset_status(e);
   if (rc) return rc;
   const int p = e->p, nt = out_traits(e);
-  const long long colb = (long long)c.n * c.wXR;  // doubles per SNP
+  const long long colb = geno_bytes_per_col(fmt, c.n) * c.wXR;  // genotype bytes per SNP
+  const unsigned char* xr = (const unsigned char*)XR;
   // Blocks of x_b SNPs, the first two of x_b/4 and x_b/2: the first upload
   // is the only one no compute hides, so it is kept short.
   long long ib = 0;
@@ -578,13 +602,13 @@ int run_snps_impl(fglsgpu_engine* e, const double* XR, long long m, double* B, d
     const int x = (int)std::min<long long>(std::min(want, c.x_b), m - ib);
     // slot k's input is free once block b-2's compute finished
     ENG_TRY(e, cudaStreamWaitEvent(e->h2d, e->evC[k], 0), "wait");
-    ENG_TRY(e, cudaMemcpyAsync(e->dX[k], XR + ib * colb, sizeof(double) * colb * x, cudaMemcpyHostToDevice, e->h2d),
+    ENG_TRY(e, cudaMemcpyAsync(e->dX[k], xr + ib * colb, (size_t)colb * x, cudaMemcpyHostToDevice, e->h2d),
             "XR upload");
     ENG_TRY(e, cudaEventRecord(e->evH[k], e->h2d), "event");
     ENG_TRY(e, cudaStreamWaitEvent(e->comp, e->evH[k], 0), "wait");
     ENG_TRY(e, cudaStreamWaitEvent(e->comp, e->evD[k], 0), "wait");  // outputs of block b-2 downloaded
     const long long db = (long long)x * p, dv = (long long)x * p * p;
-    rc = compute_block(e, e->dX[k], nullptr, x, e->dB[k], e->dV[k], db, dv, ib);
+    rc = compute_block(e, e->dX[k], fmt, x, e->dB[k], e->dV[k], db, dv, ib);
     if (rc) return rc;
     if (compact)
       ENG_TRY(e, snp_compact(e->comp, x, nt, p, e->dB[k], db, e->dV[k], dv, e->dSE[k], e->dP[k], db), "compact");
@@ -622,7 +646,21 @@ int fglsgpu_run_snps(fglsgpu_engine* e, const double* XR, long long m, double* B
   if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
   if (!e->problem_set) return fail(e, FGLSGPU_ESTATE, "set_problem must precede run_snps");
   if (m <= 0 || !XR || !B || !V) return fail(e, FGLSGPU_EINVAL, "invalid run_snps arguments");
-  return run_snps_impl(e, XR, m, B, V, nullptr, nullptr);
+  return run_snps_impl(e, XR, GENO_F64, m, B, V, nullptr, nullptr);
+}
+
+int fglsgpu_run_snps_u8(fglsgpu_engine* e, const unsigned char* XR, long long m, double* B, double* V) {
+  if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
+  if (!e->problem_set) return fail(e, FGLSGPU_ESTATE, "set_problem must precede run_snps");
+  if (m <= 0 || !XR || !B || !V) return fail(e, FGLSGPU_EINVAL, "invalid run_snps_u8 arguments");
+  return run_snps_impl(e, XR, GENO_U8, m, B, V, nullptr, nullptr);
+}
+
+int fglsgpu_run_snps_packed(fglsgpu_engine* e, const unsigned char* XR2, long long m, double* B, double* V) {
+  if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
+  if (!e->problem_set) return fail(e, FGLSGPU_ESTATE, "set_problem must precede run_snps");
+  if (m <= 0 || !XR2 || !B || !V) return fail(e, FGLSGPU_EINVAL, "invalid run_snps_packed arguments");
+  return run_snps_impl(e, XR2, GENO_PACKED, m, B, V, nullptr, nullptr);
 }
 
 int fglsgpu_run_snps_compact(fglsgpu_engine* e, const double* XR, long long m, double* B, double* SE, double* P) {
@@ -635,7 +673,7 @@ int fglsgpu_run_snps_compact(fglsgpu_engine* e, const double* XR, long long m, d
     if (!e->dSE[k]) ENG_TRY(e, dalloc(&e->dSE[k], per), "compact buffers");
     if (!e->dP[k]) ENG_TRY(e, dalloc(&e->dP[k], per), "compact buffers");
   }
-  return run_snps_impl(e, XR, m, B, nullptr, SE, P);
+  return run_snps_impl(e, XR, GENO_F64, m, B, nullptr, SE, P);
 }
 
 int fglsgpu_set_precision(fglsgpu_engine* e, int precision) {

@@ -1020,6 +1020,35 @@ __global__ void __launch_bounds__(256) genotypes_f8_kernel(int K, int cols, cons
   for (int k = threadIdx.x; k < K; k += blockDim.x) g[k] = geno_f8(col[k]);
 }
 
+// 2-bit packed genotype columns (SNP-major PLINK .bed body: ceil(K/4) bytes a
+// column, codes 00 -> 2, 10 -> 1, 11 -> 0, 01 = missing) straight to the E4M3
+// operand, four individuals per thread and step; a missing call sets the
+// status word (FGLSGPU_EINVAL, individual, SNP) and enters as 0.
+__global__ void __launch_bounds__(256) genotypes_packed_f8_kernel(int K, const uint8_t* __restrict__ src,
+                                                                    uint8_t* __restrict__ G, int Kpad, int wXR,
+                                                                    DevStatus* st, long long snp_base) {
+  const long long c = blockIdx.x;
+  const int bpc = (K + 3) / 4;
+  const uint8_t* col = src + c * bpc;
+  uint8_t* g = G + c * Kpad;
+  const uint32_t e0 = geno_f8((unsigned char)0), e1 = geno_f8((unsigned char)1), e2 = geno_f8((unsigned char)2);
+  for (int b = threadIdx.x; b < bpc; b += blockDim.x) {
+    const uint32_t v = col[b];
+    uint32_t w = 0;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      const uint32_t code = (v >> (2 * i)) & 3u;
+      if (code == 1u && 4 * b + i < K) set_status(st, FGLSGPU_EINVAL, 4 * b + i, snp_base + c / wXR);
+      w |= (code == 0u ? e2 : code == 2u ? e1 : e0) << (8 * i);
+    }
+    if (4 * b + 3 < K) {
+      *(uint32_t*)(g + 4 * b) = w;  // Kpad is a multiple of 128: 4-byte aligned
+    } else {
+      for (int i = 0; 4 * b + i < K; i++) g[4 * b + i] = (uint8_t)(w >> (8 * i));
+    }
+  }
+}
+
 __global__ void eye_kernel(int n, double* A) {
   const long long total = (long long)n * n;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
@@ -1307,6 +1336,14 @@ cudaError_t load_genotypes(OzakiPlan* p, cudaStream_t s, const T* X, int x) {
   return cudaGetLastError();
 }
 
+cudaError_t load_genotypes_packed(OzakiPlan* p, cudaStream_t s, const uint8_t* X2, int x, DevStatus* st,
+                                  long long snp_base) {
+  if (x <= 0) return cudaSuccess;
+  genotypes_packed_f8_kernel<<<x, 256, 0, s>>>(p->n, X2, p->G, p->Kpad, p->wXR, st, snp_base);
+  note_launch();
+  return cudaGetLastError();
+}
+
 cudaError_t selfgram(OzakiPlan* p, cudaStream_t s, int col0, int xq, int t, double* GR, long long ldg) {
   const float2* A = (const float2*)(p->C + (long long)col0 * p->Mpad);
   if (!p->tq || col0 != 0)
@@ -1387,15 +1424,17 @@ cudaError_t ozaki_set_chol(OzakiPlan* p, cudaStream_t s, const double* L, const 
   return cudaGetLastError();
 }
 
-cudaError_t ozaki_block(OzakiPlan* p, cudaStream_t s, const double* X, const unsigned char* Xu8, int x,
-                        double* GR, StageHook hook, void* ctx) {
+cudaError_t ozaki_block(OzakiPlan* p, cudaStream_t s, const GenoBlock& X, int x, double* GR, StageHook hook,
+                        void* ctx) {
   const int t = p->eigen ? p->t : 1;
   const int tri = p->eigen ? 0 : p->n;
   auto mark = [&](int cls, int begin, cudaStream_t st) {
     if (hook) hook(ctx, cls, begin, st);
   };
   mark(FGLSGPU_PROF_GENOTYPES, 1, s);
-  FGLS_CUDA_TRY(Xu8 ? load_genotypes<unsigned char>(p, s, Xu8, x) : load_genotypes<double>(p, s, X, x));
+  FGLS_CUDA_TRY(X.packed ? load_genotypes_packed(p, s, X.packed, x, X.st, X.snp_base)
+                : X.u8     ? load_genotypes<unsigned char>(p, s, X.u8, x)
+                           : load_genotypes<double>(p, s, X.f64, x));
   mark(FGLSGPU_PROF_GENOTYPES, 0, s);
   for (int x0 = 0; x0 < x; x0 += p->sub) {
     const int xq = std::min(p->sub, x - x0);

@@ -21,14 +21,26 @@ void ozaki_destroy(OzakiPlan* p);
 cudaError_t ozaki_set_eigen(OzakiPlan* p, cudaStream_t s, const double* Z, const double* AYL, const double* dinv);
 // chol: L (n x n lower), WY = [y~ | XL~] (n x (1+wXL)) of the selected trait
 cudaError_t ozaki_set_chol(OzakiPlan* p, cudaStream_t s, const double* L, const double* WY);
-// One genotype block (FP64 X or byte Xu8, n x x): E4M3 operand build, the
-// tcgen05 split GEMM C = [Z^T ; U^T] X (chol: [L^-1 ; U^T] X), and the
-// quadratic Gram terms GR[i + j*x] = sum_l C[l,i]^2 d_j(l) (chol: d = 1),
-// all on stream s.  `hook(ctx, class, begin, stream)`
-// brackets each stage (FGLSGPU_PROF_* classes) for timing; may be null.
+// A genotype block on the device in one of three formats (exactly one
+// pointer set): FP64 or bytes, n values per column, or 2-bit packed as a
+// SNP-major PLINK .bed body (ceil(n/4) bytes per column; a missing call sets
+// st to FGLSGPU_EINVAL with the individual and snp_base + SNP).
+struct DevStatus;
+struct GenoBlock {
+  const double* f64 = nullptr;
+  const unsigned char* u8 = nullptr;
+  const unsigned char* packed = nullptr;
+  DevStatus* st = nullptr;
+  long long snp_base = 0;
+};
+// One genotype block (n x x): E4M3 operand build, the tcgen05 split GEMM
+// C = [Z^T ; U^T] X (chol: [L^-1 ; U^T] X), and the quadratic Gram terms
+// GR[i + j*x] = sum_l C[l,i]^2 d_j(l) (chol: d = 1), all on stream s.
+// `hook(ctx, class, begin, stream)` brackets each stage (FGLSGPU_PROF_*
+// classes) for timing; may be null.
 typedef void (*StageHook)(void* ctx, int cls, int begin, cudaStream_t s);
-cudaError_t ozaki_block(OzakiPlan* p, cudaStream_t s, const double* X, const unsigned char* Xu8, int x,
-                        double* GR, StageHook hook, void* ctx);
+cudaError_t ozaki_block(OzakiPlan* p, cudaStream_t s, const GenoBlock& X, int x, double* GR, StageHook hook,
+                        void* ctx);
 // sliced MMA operations per genotype column (2 * slices * rows * K)
 double ozaki_flops_per_snp(const OzakiPlan* p);
 

@@ -562,19 +562,25 @@ __global__ void u8_to_f64_kernel(const unsigned char* __restrict__ in, double* _
 // 2-bit packed hard calls, SNP-major like a PLINK .bed body: column c holds
 // ceil(n/4) bytes, individual k in bits 2(k%4)..2(k%4)+1 of byte k/4.  Codes:
 // 00 -> 2, 10 -> 1, 11 -> 0 (copies of the first allele), 01 = missing (status
-// FGLSGPU_EINVAL with the individual and the SNP, value 0).
-__global__ void unpack_2bit_kernel(const unsigned char* __restrict__ in, int n, long long cols, int wXR,
-                                   unsigned char* __restrict__ out, DevStatus* st, long long snp_base) {
-  const long long bpc = (n + 3) / 4;
-  const long long total = cols * n;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
-       e += (long long)gridDim.x * blockDim.x) {
-    const int k = (int)(e % n);
-    const long long c = e / n;
-    const unsigned code = (in[c * bpc + (k >> 2)] >> (2 * (k & 3))) & 3u;
-    unsigned char v = code == 0u ? 2 : (code == 2u ? 1 : 0);
-    if (code == 1u) set_status(st, FGLSGPU_EINVAL, k, snp_base + c / wXR);
-    out[e] = v;
+// FGLSGPU_EINVAL with the individual and the SNP, value 0).  One CTA per
+// column, one packed byte (four individuals) per thread and step.
+__global__ void __launch_bounds__(256) unpack_2bit_kernel(const unsigned char* __restrict__ in, int n, int wXR,
+                                                          unsigned char* __restrict__ out, DevStatus* st,
+                                                          long long snp_base) {
+  const long long c = blockIdx.x;
+  const int bpc = (n + 3) / 4;
+  const unsigned char* col = in + c * bpc;
+  unsigned char* o = out + c * n;
+  for (int b = threadIdx.x; b < bpc; b += blockDim.x) {
+    const unsigned v = col[b];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      const int k = 4 * b + i;
+      if (k >= n) break;
+      const unsigned code = (v >> (2 * i)) & 3u;
+      if (code == 1u) set_status(st, FGLSGPU_EINVAL, k, snp_base + c / wXR);
+      o[k] = (unsigned char)(code == 0u ? 2 : (code == 2u ? 1 : 0));
+    }
   }
 }
 
@@ -584,10 +590,8 @@ std::atomic<long long> g_launches{0};
 
 cudaError_t unpack_2bit(cudaStream_t s, const unsigned char* in, int n, long long cols, int wXR, unsigned char* out,
                         DevStatus* st, long long snp_base) {
-  const long long total = cols * n;
-  const int blocks = (int)std::min<long long>((total + 255) / 256, 152LL * 32);
-  if (blocks <= 0) return cudaSuccess;
-  unpack_2bit_kernel<<<blocks, 256, 0, s>>>(in, n, cols, wXR, out, st, snp_base);
+  if (cols <= 0) return cudaSuccess;
+  unpack_2bit_kernel<<<(unsigned)cols, 256, 0, s>>>(in, n, wXR, out, st, snp_base);
   note_launch();
   return cudaGetLastError();
 }

@@ -240,3 +240,25 @@ def pack_2bit(X: np.ndarray) -> np.ndarray:
     code = np.concatenate([code, np.full((cols, pad), 3, np.uint8)], axis=1).reshape(cols, -1, 4)
     return (code[..., 0] | (code[..., 1] << 2) | (code[..., 2] << 4) | (code[..., 3] << 6)).astype(np.uint8)
 
+
+
+BED_MAGIC = bytes((0x6C, 0x1B, 0x01))  # PLINK .bed, SNP-major
+
+
+def write_xr(pb: Problem, path: str, fmt: str = "f64") -> str:
+    """XR in one of the drop-in's genotype file formats (FGLS_XR_FORMAT):
+    'f64' (the reference's XR.in), 'u8' (one byte per individual, same
+    column order) or 'bed' (SNP-major PLINK .bed: magic bytes, then the
+    2-bit body of pack_2bit, column i*wXR + c = SNP i, column c)."""
+    G = np.asfortranarray(pb.XR).T  # (m*wXR, n)
+    if fmt == "f64":
+        G.astype("<f8").tofile(path)
+    elif fmt == "u8":
+        np.ascontiguousarray(G.astype(np.uint8)).tofile(path)
+    elif fmt == "bed":
+        with open(path, "wb") as f:
+            f.write(BED_MAGIC)
+            f.write(pack_2bit(G.astype(np.int16)).tobytes())
+    else:
+        raise ValueError(fmt)
+    return path

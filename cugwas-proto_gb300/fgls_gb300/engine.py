@@ -42,7 +42,8 @@ EXPORTS = (
     "fglsgpu_batch_create", "fglsgpu_batch_destroy", "fglsgpu_batch_params", "fglsgpu_batch_step",
     "fglsgpu_batch_sync", "fglsgpu_batch_stream", "fglsgpu_batch_last_error", "fglsgpu_batch_profile",
     "fglsgpu_batch_profile_read", "fglsgpu_run_block_device_packed", "fglsgpu_run_snps_compact",
-    "fglsgpu_reml_fit", "fglsgpu_set_hsigma", "fglsgpu_set_wait_limit",
+    "fglsgpu_reml_fit", "fglsgpu_set_hsigma", "fglsgpu_set_wait_limit", "fglsgpu_run_snps_u8",
+    "fglsgpu_run_snps_packed",
 )
 PROF_CLASSES = ("genotypes", "split_gemm", "selfgram", "solve", "fp64_gemm", "trsm", "gram", "spare")
 
@@ -87,6 +88,8 @@ def lib():
     L.fglsgpu_run_block.argtypes = [P, P, I, P, P, LL, LL]
     L.fglsgpu_run_snps.argtypes = [P, P, LL, P, P]
     L.fglsgpu_run_snps_compact.argtypes = [P, P, LL, P, P, P]
+    L.fglsgpu_run_snps_u8.argtypes = [P, P, LL, P, P]
+    L.fglsgpu_run_snps_packed.argtypes = [P, P, LL, P, P]
     L.fglsgpu_run_block_device.argtypes = [P, P, I, P, P, LL, LL]
     L.fglsgpu_run_block_device_u8.argtypes = [P, P, I, P, P, LL, LL]
     L.fglsgpu_run_block_device_packed.argtypes = [P, P, I, P, P, LL, LL]
@@ -188,6 +191,25 @@ class Engine:
         V = np.empty((nt, m, p, p)) if V is None else V
         self._check(self.L.fglsgpu_run_snps(self._h, _ptr(XR), m, _ptr(B), _ptr(V)))
         return B, V.transpose(0, 1, 3, 2)
+
+    def run_snps_genotypes(self, G, packed=False, B=None, V=None):
+        """Whole job from hard calls: G (m*wXR columns, n) uint8 in the XR
+        column order (packed=False), or its 2-bit SNP-major .bed body
+        (m*wXR columns, ceil(n/4) bytes; packed=True)."""
+        G = np.ascontiguousarray(G, dtype=np.uint8)
+        m = G.shape[0] // self.wXR
+        nt, p = self.out_traits, self.p
+        B = np.empty((nt, m, p)) if B is None else B
+        V = np.empty((nt, m, p, p)) if V is None else V
+        f = self.L.fglsgpu_run_snps_packed if packed else self.L.fglsgpu_run_snps_u8
+        self._check(f(self._h, _ptr(G), m, _ptr(B), _ptr(V)))
+        return B, V.transpose(0, 1, 3, 2)
+
+    def run_snps_genotypes_ptr(self, g_ptr, m, b_ptr, v_ptr, packed=False):
+        """Host pointers (e.g. pinned torch tensors): genotypes (bytes or
+        2-bit packed), B, V."""
+        f = self.L.fglsgpu_run_snps_packed if packed else self.L.fglsgpu_run_snps_u8
+        self._check(f(self._h, C.c_void_p(g_ptr), int(m), C.c_void_p(b_ptr), C.c_void_p(v_ptr)))
 
     def run_snps_compact(self, XR):
         """B, SE, P each (traits, m, p)."""

@@ -124,6 +124,18 @@ int fglsgpu_run_block(fglsgpu_engine *e, const double *XR, int x_inc, double *B,
  * buffering, src/fgls_chol.c:327-487). */
 int fglsgpu_run_snps(fglsgpu_engine *e, const double *XR, long long m, double *B, double *V);
 
+/* As fglsgpu_run_snps with the genotypes as bytes (hard calls 0/1/2, the XR
+ * layout with one byte per individual): 8x fewer bytes over the host link.
+ * No counterpart in the reference (it reads FP64 only, src/fgls_chol.c:333-337). */
+int fglsgpu_run_snps_u8(fglsgpu_engine *e, const unsigned char *XR, long long m, double *B, double *V);
+
+/* As fglsgpu_run_snps with the genotypes packed 2 bits per individual, the
+ * body of a SNP-major PLINK .bed file (the layout fglsgpu_run_block_device_packed
+ * describes: ceil(n/4) bytes per column, codes 00 -> 2, 10 -> 1, 11 -> 0,
+ * 01 missing -> FGLSGPU_EINVAL naming the SNP and individual): 32x fewer
+ * bytes over the host link than FP64.  No counterpart in the reference. */
+int fglsgpu_run_snps_packed(fglsgpu_engine *e, const unsigned char *XR2, long long m, double *B, double *V);
+
 /* As fglsgpu_run_snps with a compact output: instead of V (p*p doubles per
  * test) the standard errors SE and the two-sided normal p-values P of all p
  * coefficients, both in the B layout (trait j, SNP i, coefficient k at

@@ -283,3 +283,55 @@ def test_run_snps_compact_matches_full_output(variant):
     assert np.array_equal(B, Bc)
     assert np.array_equal(SE, V[..., idx, idx])
     assert np.allclose(P, erfc(np.abs(B / SE) / np.sqrt(2.0)), rtol=1e-13, atol=1e-300)
+
+
+@pytest.mark.parametrize("variant,precision", [("eigen", "split"), ("eigen", "fp64"), ("chol", "split"),
+                                               ("chol", "fp64")])
+def test_run_snps_from_bytes_and_packed_matches_fp64(variant, precision):
+    """fglsgpu_run_snps_u8 / _packed (host genotypes as bytes or 2-bit .bed
+    body through the pinned pipeline, widened on the device) give results
+    bit-identical to fglsgpu_run_snps on the same calls as FP64."""
+    from fgls_gb300 import Engine, datagen
+    pb = datagen.make_problem(301, 700, 40 if variant == "eigen" else 2, seed=23, hsig_uniform=True)
+    G = np.ascontiguousarray(pb.XR.T.astype(np.uint8))
+    with Engine(pb.n, 3, 1, pb.t, 256, variant=variant, precision=precision) as e:
+        e.set_problem(pb.Phi, pb.XL, pb.Y, pb.h, pb.sigma)
+        e.select_trait(1)
+        B, V = e.run_snps(pb.XR)
+        B1, V1 = e.run_snps_genotypes(G)
+        B2, V2 = e.run_snps_genotypes(datagen.pack_2bit(G), packed=True)
+    assert np.array_equal(B, B1) and np.array_equal(V, V1)
+    assert np.array_equal(B, B2) and np.array_equal(V, V2)
+
+
+@pytest.mark.parametrize("variant", ["chol", "eigen"])
+def test_dropin_reads_bed_and_byte_genotype_files(variant):
+    """FGLS_XR_FORMAT=bed (SNP-major PLINK .bed) and =u8 give the same
+    B.out/V.out bytes as the reference's FP64 XR.in; a missing call is an
+    error naming the SNP and the individual; a file without the .bed magic is
+    refused."""
+    from fgls_gb300 import FGLSError, datagen, fgls_chol, fgls_eigen
+    pb = datagen.make_problem(203, 300, 3, seed=29, hsig_uniform=True)
+    d = tempfile.mkdtemp()
+    paths = datagen.write_problem(pb, d)
+    fn = fgls_chol if variant == "chol" else fgls_eigen
+    env = {"FGLS_PRECISION": "split"} if variant == "eigen" else {}
+
+    def run(xr, tag, fmt):
+        fn(pb.n, pb.p, pb.m, pb.t, pb.wXL, pb.wXR, 128, 1, 2, paths["Phi.in"], paths["H.in"], paths["Sig.in"],
+           paths["XL.in"], xr, paths["Y.in"], os.path.join(d, tag + ".B"), os.path.join(d, tag + ".V"),
+           env={**env, "FGLS_XR_FORMAT": fmt})
+        return [np.fromfile(os.path.join(d, tag + ext)) for ext in (".B", ".V")]
+
+    ref = run(paths["XR.in"], "f64", "f64")
+    for fmt in ("u8", "bed"):
+        out = run(datagen.write_xr(pb, os.path.join(d, "XR." + fmt), fmt), fmt, fmt)
+        assert all(np.array_equal(a, b) for a, b in zip(ref, out)), fmt
+    Gm = np.ascontiguousarray(pb.XR.T).astype(np.int16)
+    Gm[211, 17] = -1
+    with open(os.path.join(d, "miss.bed"), "wb") as f:
+        f.write(datagen.BED_MAGIC + datagen.pack_2bit(Gm).tobytes())
+    with pytest.raises(FGLSError, match="missing genotype .* SNP 211, individual 17"):
+        run(os.path.join(d, "miss.bed"), "miss", "bed")
+    with pytest.raises(FGLSError, match="not a SNP-major PLINK .bed"):
+        run(os.path.join(d, "XR.u8"), "bad", "bed")

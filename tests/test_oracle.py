@@ -135,3 +135,20 @@ def test_oracle_reml_fit_is_a_maximum():
         if lo < h[j] < hi:
             assert abs(dll[j]) <= 1e-8 * abs(ll[j])
         assert abs(O.reml_profiled(W, ZtXL, ZtY[:, j], h[j])[2] - s[j]) <= 1e-14 * s[j]
+
+
+def test_bed_writer_follows_the_plink_bit_layout():
+    """datagen.write_xr(..., 'bed'): magic 6c 1b 01, then per SNP ceil(n/4)
+    bytes, individual k in bits 2(k%4).. of byte k/4, codes 00 = 2, 10 = 1,
+    11 = 0 copies of the first allele (01 = missing), padding codes 11."""
+    from fgls_gb300 import datagen
+    pb = datagen.make_problem(10, 4, 1, seed=3)
+    d = tempfile.mkdtemp()
+    raw = open(datagen.write_xr(pb, os.path.join(d, "x.bed"), "bed"), "rb").read()
+    assert raw[:3] == bytes((0x6C, 0x1B, 0x01)) and len(raw) == 3 + 4 * 3
+    body = np.frombuffer(raw[3:], np.uint8).reshape(4, 3)
+    for i in range(4):
+        for k in range(12):
+            code = (body[i, k // 4] >> (2 * (k % 4))) & 3
+            want = 3 if k >= 10 else {2: 0, 1: 2, 0: 3}[int(pb.XR[k, i])]
+            assert code == want, (i, k, code, want)
