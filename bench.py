@@ -147,6 +147,20 @@ def genotype_block(x, n, seed, dev):
     return X.double()
 
 
+def pack_2bit_device(X):
+    """(cols, n) hard calls on the device -> (cols, ceil(n/4)) bytes, the
+    SNP-major PLINK .bed body (codes 2 -> 00, 1 -> 10, 0 -> 11, padding 11),
+    as datagen.pack_2bit does on the host."""
+    import torch
+    cols, n = X.shape
+    code = torch.where(X == 2, 0, torch.where(X == 1, 2, 3)).to(torch.uint8)
+    pad = (-n) % 4
+    if pad:
+        code = torch.cat([code, torch.full((cols, pad), 3, dtype=torch.uint8, device=X.device)], 1)
+    code = code.view(cols, -1, 4)
+    return code[..., 0] | (code[..., 1] << 2) | (code[..., 2] << 4) | (code[..., 3] << 6)
+
+
 def rank_block_seeds(rank, pool):
     """Genotype-block seeds of one rank: ranks shard the SNP blocks (weak
     scaling), so no two ranks process the same block."""
@@ -251,6 +265,31 @@ def cpu_port_throughput(Z, W, XL, Y, h, s, X_host, budget_s, min_reps=1, steps=N
     return len(times) * x * Y.shape[1] / tot, tot / len(times), len(times)
 
 
+def cpu_chol_throughput(Phi, XL, y, h, sigma, X_host, budget_s, wXR=1):
+    """The oracle's restatement of fgls_chol's per-block loop
+    (src/fgls_chol.c:365-438: TRSM, per-SNP Gram and solve) on the host cores
+    for one trait, repeated over the SNP sample for about budget_s seconds;
+    the per-trait factorization and null model (src/fgls_chol.c:251-325) are
+    set up once, outside the timing.  Returns (tests/s, seconds, reps)."""
+    import scipy.linalg as sla
+    from oracle import fgls_oracle as O
+    n = Phi.shape[0]
+    M = h * sigma * Phi
+    M[np.diag_indices(n)] += (1.0 - h) * sigma
+    L = np.linalg.cholesky(M)
+    wXL = XL.shape[1]
+    XLt, yt, B_t, V_tl, rs = O.null_model_chol(L, XL, y, wXL)
+    times = []
+    t0 = time.perf_counter()
+    while not times or time.perf_counter() - t0 < budget_s:
+        a = time.perf_counter()
+        Xt = sla.solve_triangular(L, X_host, lower=True)
+        O.snp_solve(B_t, V_tl, XLt, yt, Xt, wXL, wXR, rs)
+        times.append(time.perf_counter() - a)
+    tot = sum(times)
+    return len(times) * X_host.shape[1] // wXR / tot, tot, len(times)
+
+
 def orthogonal_basis(n, seed):
     """Dense orthogonal n x n matrix (three Householder reflectors), used by
     the reference arm where no device eigensolver may run."""
@@ -344,6 +383,15 @@ def run_chol(args):
             B, _ = read_outputs(d, m_e2e, t, p)
             e2e[prec] = {"value": m_e2e * t / wall, "unit": UNIT, "wall_s": wall, "snps": m_e2e,
                          "finite": bool(np.isfinite(B).all())}
+    cpu = None
+    if not args.no_cpu:
+        xs = 256
+        Xc = pool[0][:xs].cpu().numpy().T.copy()
+        cv, csec, creps = cpu_chol_throughput(Phi, XL, Y[:, 0], float(h[0]), float(s[0]), Xc, args.cpu_seconds)
+        cpu = {"value": cv, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{creps} x {xs} SNPs at n={n}, t=1: oracle restatement of fgls_chol's per-block loop "
+                         f"(TRSM + per-SNP Gram and solve, numpy/OpenBLAS, all host threads; the per-trait "
+                         f"Cholesky outside the timing), {csec:.1f} s"}
     flops_trsm = float(n) * n * xb
     trsm_ms = out["fp64"]["kernel_ms_per_step"].get("trsm")
     line = {
@@ -363,7 +411,7 @@ def run_chol(args):
                 "d2h_bytes_per_step": xb * (p + p * p) * 8,
                 "api": "fgls_chol file entry point, XR read from a local file through the pinned ring, "
                        "setup included", "split": e2e["split"], "fp64": e2e["fp64"]},
-        "gpu_launches": out["fp64"]["launches"], "cpu_baseline": None,
+        "gpu_launches": out["fp64"]["launches"], "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)
 
@@ -412,10 +460,63 @@ def run_adjoint(args):
         ms = e0.elapsed_time(e1)
         res[name] = {"tests_per_s": args.steps * xb * t / (ms / 1e3), "ms_per_block": ms / args.steps,
                      "launches": launch_count() - l0}
+    # end to end through the C ABI: pinned host genotypes and cotangent in,
+    # forward B and the accumulated gradients out, copies inside the timing
+    Xh = pool[0].cpu().pin_memory()
+    Bbh = bbar.cpu().pin_memory()
+    Bh = torch.empty(t * xb * p, dtype=torch.float64, pin_memory=True)
+    Xd = torch.empty_like(pool[1])
+    Bbd = torch.empty_like(bbar)
+    E = 3
+    eng.sync()
+    a = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for _ in range(E):
+            Xd.copy_(Xh, non_blocking=True)
+            Bbd.copy_(Bbh, non_blocking=True)
+            eng.run_block_device(Xd.data_ptr(), xb, dB.data_ptr(), dV.data_ptr(), xb * p, xb * p * p)
+            eng.adjoint_block_device(Xd.data_ptr(), xb, Bbd.data_ptr(), xb * p)
+            Bh.copy_(dB, non_blocking=True)
+    stream.synchronize()
+    dh_e, ds_e, dY_e = eng.adjoint_read()
+    e2e_s = time.perf_counter() - a
+    e2e = {"value": E * xb * t / e2e_s, "unit": UNIT, "h2d_bytes_per_step": xb * n * 8 + t * xb * p * 8,
+           "d2h_bytes_per_step": t * xb * p * 8 + 2 * t * 8, "blocks": E,
+           "api": "fglsgpu_run_block_device + fglsgpu_adjoint_block_device from pinned host buffers, "
+                  "fglsgpu_adjoint_read"}
+    del Xh, Bbh, Bh, Xd, Bbd
     dh, ds, dY = eng.adjoint_read()
     ll, dll = eng.reml()
+    cpu = None
+    if not args.no_cpu:
+        # the oracle's FP64 forward (beta) and adjoint on the device's
+        # eigendecomposition, over a sample of SNPs
+        from oracle import fgls_oracle as O
+        W, Z = eng.eigen()
+        xs = 64
+        Xc = pool[0][:xs].cpu().numpy().T.copy()
+        Bb = bbar.view(t, xb, p)[:, :xs].cpu().numpy()
+        reps, tot = 0, 0.0
+        while reps == 0 or tot < args.cpu_seconds:
+            a = time.perf_counter()
+            O.eigen_betas(Z, W, XL, Y, h, s, Xc)
+            O.eigen_adjoint(Z, W, XL, Y, h, s, Xc, Bb)
+            tot += time.perf_counter() - a
+            reps += 1
+        cpu = {"value": reps * xs * t / tot, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{reps} x ({xs} SNPs x {t} traits) at n={n}: oracle FP64 forward (beta) + adjoint "
+                         f"(numpy/OpenBLAS, all host threads), {tot:.1f} s"}
+        del Z
     eng.close()
     both = 1.0 / (1.0 / res["forward"]["tests_per_s"] + 1.0 / res["adjoint"]["tests_per_s"])
+    # FP64 work per block (GEMM-shaped terms; nq = t (1 + wXL)): forward Z^T X
+    # 2 n^2 x, Gram terms 2 n x (nq + t); adjoint recomputes Z^T X and three
+    # weightings of the Gram terms, and accumulates R g (2 n t x)
+    nq = t * (1 + WXL)
+    fwd_flops = 2.0 * n * n * xb + 2.0 * n * xb * (nq + t)
+    adj_flops = 2.0 * n * n * xb + 6.0 * n * xb * (nq + t) + 2.0 * n * t * xb
+    step_s = (res["forward"]["ms_per_block"] + res["adjoint"]["ms_per_block"]) / 1e3
+    achieved = (fwd_flops + adj_flops) / step_s / 1e12
     line = {
         "metric": "SNP×trait tests/s, fgls_eigen FP64 forward + adjoint on 1 GB300 (n=5000, t=16)",
         "value": both, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": 2,
@@ -426,7 +527,13 @@ def run_adjoint(args):
                    "job_s_estimate": 100000 * t / both + setup,
                    "grad_finite": bool(np.isfinite(dh).all() and np.isfinite(dY).all()),
                    "reml_dll_dh": [float(v) for v in dll[:4]]},
-        "gpu_launches": res["forward"]["launches"] + res["adjoint"]["launches"], "cpu_baseline": None,
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": 1.25, "unit": "TFLOP/s",
+                     "frac": achieved / 1.25, "traffic": None,
+                     "kernel": "dgemm_kernel (Z^T X and the Gram GEMMs of forward and adjoint)",
+                     "peak_source": "nominal GB300 FP64 (no measured FP64 peak)",
+                     "work": f"{(fwd_flops + adj_flops) / 1e12:.3f} TFLOP of FP64 GEMM work per block of {xb} SNPs"},
+        "e2e": e2e,
+        "gpu_launches": res["forward"]["launches"] + res["adjoint"]["launches"], "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)
 
@@ -566,6 +673,23 @@ def run_cohorts(args):
     e2e_s = time.perf_counter() - a
     b.sync()
     e2e_tests = E * sum(xb * c["t"] for c in co)
+    cpu = None
+    if not args.no_cpu:
+        # the oracle's fgls_chol block loop (TRSM + per-SNP Gram and solve) on
+        # every 4th cohort in order of size, one trait, 64 SNPs each
+        order = sorted(range(C), key=lambda i: co[i]["n"])[::4]
+        xs, tests, tot = 64, 0, 0.0
+        for i in order:
+            c = co[i]
+            Xc = X[i][0][:xs].cpu().numpy().T.astype(np.float64)
+            _, sec, reps = cpu_chol_throughput(c["Phi"], c["XL"], c["Y"][:, 0], float(c["h"][0]),
+                                               float(c["sigma"][0]), Xc, 0.0)
+            tests += reps * xs
+            tot += sec
+        cpu = {"value": tests / tot, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{len(order)} cohorts (every 4th by n) x {xs} SNPs x 1 trait: oracle restatement of "
+                         f"fgls_chol's per-block loop (numpy/OpenBLAS, all host threads; per-trait Cholesky "
+                         f"outside the timing), {tot:.1f} s"}
     # release every tensor that touched the batch's stream before the stream goes
     del Xh, Bh, Vh, Xd, X, dB, dV, stream
     import gc
@@ -592,7 +716,7 @@ def run_cohorts(args):
                 "h2d_bytes_per_step": xb * sum(c["n"] for c in co),
                 "d2h_bytes_per_step": sum(T * xb * (c["p"] + c["p"] ** 2) * 8 for c in co),
                 "api": "fglsgpu_batch_step (host pinned u8 genotypes -> host B/V)", "steps": E},
-        "gpu_launches": launches, "clocks": clocks, "cpu_baseline": None,
+        "gpu_launches": launches, "clocks": clocks, "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)
 
@@ -811,7 +935,24 @@ def run_eigen(args, rank, world, local, dist):
         e2e_runs.append(max_over_ranks(time.perf_counter() - a, dist, dev))
     e2e_s = statistics.median(e2e_runs)
     e2e_value = aggregate_throughput(world, E, xb, t, e2e_s)
-    del Xh, Bh, Vh
+    # the same blocks as hard calls packed 2 bits per individual (SNP-major
+    # PLINK .bed body) through fglsgpu_run_snps_packed: 32x fewer input bytes
+    B_f64 = Bh.clone()
+    Xpk = torch.empty((E * xb, (n + 3) // 4), dtype=torch.uint8, pin_memory=True)
+    for i in range(E):
+        Xpk[i * xb:(i + 1) * xb].copy_(pack_2bit_device(pool[i % len(pool)]))
+    eng.run_snps_genotypes_ptr(Xpk.data_ptr(), xb, Bh.data_ptr(), Vh.data_ptr(), packed=True)  # warm
+    pk_runs = []
+    for _ in range(3):
+        a = time.perf_counter()
+        eng.run_snps_genotypes_ptr(Xpk.data_ptr(), E * xb, Bh.data_ptr(), Vh.data_ptr(), packed=True)
+        pk_runs.append(max_over_ranks(time.perf_counter() - a, dist, dev))
+    e2e_packed = {"value": aggregate_throughput(world, E, xb, t, statistics.median(pk_runs)), "unit": UNIT,
+                  "h2d_bytes_per_step": xb * ((n + 3) // 4), "d2h_bytes_per_step": t * xb * (p + p * p) * 8,
+                  "api": "fglsgpu_run_snps_packed (host pinned 2-bit SNP-major .bed body -> host B/V)",
+                  "calls": [aggregate_throughput(world, E, xb, t, x) for x in pk_runs], "stat": "median of 3 calls",
+                  "beta_identical_to_fp64_input": bool(torch.equal(Bh, B_f64))}
+    del Xh, Bh, Vh, Xpk, B_f64
 
     # variance components of every trait re-estimated on the device (REML,
     # sigma profiled out, h on a 64-point grid refined to the gradient root)
@@ -882,7 +1023,8 @@ def run_eigen(args, rank, world, local, dist):
         "e2e": {"value": e2e_value if gate_ok else None, "unit": UNIT, "h2d_bytes_per_step": xb * n * 8,
                 "d2h_bytes_per_step": t * xb * (p + p * p) * 8,
                 "api": "fglsgpu_run_snps (host pinned FP64 XR -> host B/V)", "blocks": E,
-                "calls": [aggregate_throughput(world, E, xb, t, x) for x in e2e_runs], "stat": "median of 3 calls"},
+                "calls": [aggregate_throughput(world, E, xb, t, x) for x in e2e_runs], "stat": "median of 3 calls",
+                "packed_genotypes": e2e_packed},
         "gpu_launches": launches,
         "clocks": clocks,
         "cpu_baseline": cpu,

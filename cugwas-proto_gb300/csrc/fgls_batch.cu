@@ -10,8 +10,10 @@
 //
 // Per step (one launch each, whatever the number of cohorts):
 //   1. grouped_genotypes: every cohort's block -> its BF16 operand
-//   2. ozaki_grouped_gemm_kernel: all tiles of all problems (longest first)
-//      -> X~ = L^-1 X (R^2 as float pairs) and the Gram rows x~'y~, x~'XL~
+//   2. ozaki_grouped_gemm_kernel: one persistent launch (a CTA per SM) over
+//      the tiles of all problems, listed longest first and taken from a
+//      launch-wide counter -> X~ = L^-1 X (R^2 as float pairs) and the Gram
+//      rows x~'y~, x~'XL~
 //   3. unit_gram_grouped: x~'x~ per (problem, SNP) in double-FP32
 //   4. snp_solve_grouped<p>: per distinct p, the p x p solves of all problems
 // The per-step inputs (genotype pointer, SNP count, output pointers of each
@@ -554,6 +556,9 @@ int fglsgpu_batch_create(const fglsgpu_cohort* cohorts, int count, const fglsgpu
     B_CHECK(dalloc(&q.GR, b->ncap), "Gram");
     B_CHECK(dalloc(&q.ref, (size_t)PROBE * k.p), "probe reference");
   }
+  // the memsets above ran on the legacy default stream, which does not order
+  // against the batch's non-blocking streams: finish them first
+  B_CHECK(cudaDeviceSynchronize(), "operand initialisation");
   // one-off FP64 setup of every problem: the traits of a cohort run
   // concurrently on NS streams, each with its own scratch and status word
   {
@@ -582,6 +587,7 @@ int fglsgpu_batch_create(const fglsgpu_cohort* cohorts, int count, const fglsgpu
     if (e == cudaSuccess) e = dalloc(&ci.Phi, (size_t)nmax * nmax);
     if (e == cudaSuccess) e = dalloc(&ci.XL, (size_t)nmax * wmax);
     if (e == cudaSuccess) e = dalloc(&ci.Y, ymax);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();  // the scratch status words' memsets
     if (e != cudaSuccess) return fail_scratch(e, "setup scratch");
     cudaEvent_t up = nullptr;
     if ((e = cudaEventCreateWithFlags(&up, cudaEventDisableTiming)) != cudaSuccess)

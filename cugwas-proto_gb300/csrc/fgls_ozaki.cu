@@ -14,7 +14,8 @@
 // runs at twice the BF16 rate: 9 five-bit slices (45 bits) cost 4.5 BF16
 // slice-equivalents where 6 eight-bit BF16 slices (48 bits) cost 6.
 //
-// Kernel ozaki_gemm_kernel (one 128 x 256 output tile per CTA, 10 warps):
+// Kernel ozaki_gemm_kernel (persistent: one CTA per SM takes 128 x 256
+// output tiles from a launch-wide counter, 10 warps):
 //   warp 0      TMA producer: per K-step of 64 bytes (64 digits), two A-slice
 //               tiles (128 x 64) and one genotype tile (256 x 64), 64B-swizzled,
 //               six 32 KB stages (the grouped launch: K-steps of 128, 128B
@@ -311,13 +312,97 @@ __device__ __forceinline__ float2 square_pair(long long V, float fscale) {
   return make_float2(ah, al);
 }
 
-// One 128 x 256 output tile (m_tile, n_tile) of problem g.  The tensor maps
-// are kernel parameters (single problem) or live in global memory (grouped
-// launch, written by the host before the launch: acquired through the
-// tensormap proxy before their first use).
-template <int KB, int ESZ>
-__device__ __forceinline__ void gemm_tile(const CUtensorMap* tmA, const CUtensorMap* tmB, const GemmArgs g,
-                                          const int m_tile, const int n_tile, const bool global_maps) {
+// One 128 x 256 output tile of a split GEMM as the three roles see it: its
+// problem, position, valid columns this launch, and whether it is skipped
+// (no valid columns).  The problem's arguments are read in place through
+// args(prob) (kernel parameters or a table in global memory), never copied
+// as a whole per tile: a per-tile copy of the argument struct made the
+// compiler spill the epilogue.
+struct TileRef {
+  int prob, m_tile, n_tile, N;
+  bool skip;
+};
+
+// Single problem: tile index -> (m_tile, n_tile) in grouped rasterization
+// (GROUP_M row tiles share the column tiles resident in L2); for the
+// triangular L^-1 operand the row order is reversed so that the longest
+// tiles (row tile i has ~i + 1 K-blocks) come first.
+struct SingleTiles {
+  const CUtensorMap* tmA;
+  const CUtensorMap* tmB;
+  const GemmArgs* g;  // kernel parameter
+  static constexpr bool global_maps = false;
+  __device__ __forceinline__ int count() const { return g->tiles_m * g->tiles_n; }
+  // uniform tiles are dealt statically; the triangular L^-1 operand's tiles
+  // (row tile i has ~i + 1 K-blocks) from the counter
+  __device__ __forceinline__ bool dynamic() const { return g->tri_rows > 0; }
+  __device__ __forceinline__ const GemmArgs& args(int) const { return *g; }
+  __device__ __forceinline__ int* err() const { return g->err; }
+  __device__ __forceinline__ uint64_t wait_ns() const { return g->wait_ns; }
+  __device__ __forceinline__ const CUtensorMap* mapA(int) const { return tmA; }
+  __device__ __forceinline__ const CUtensorMap* mapB(int) const { return tmB; }
+  __device__ __forceinline__ TileRef tile(int t) const {
+    const int per_group = GROUP_M * g->tiles_n;
+    const int first_m = (t / per_group) * GROUP_M;
+    const int gsz = min(g->tiles_m - first_m, GROUP_M);
+    int m_tile = first_m + (t % per_group) % gsz;
+    if (g->tri_rows > 0) m_tile = g->tiles_m - 1 - m_tile;
+    return TileRef{0, m_tile, (t % per_group) / gsz, g->N, false};
+  }
+};
+
+// Many independent problems: a host-built table of tiles (longest problems
+// first); the valid columns of each cohort this launch are cols[cohort];
+// tensor maps in global memory, written by the host before the launch.
+struct GroupedTiles {
+  const GroupedTile* tiles;
+  const GroupedProblem* probs;
+  const CUtensorMap* maps;
+  const int* cols;
+  int ntiles;
+  static constexpr bool global_maps = true;
+  __device__ __forceinline__ int count() const { return ntiles; }
+  __device__ __forceinline__ bool dynamic() const { return true; }
+  __device__ __forceinline__ const GemmArgs& args(int prob) const { return probs[prob].g; }
+  __device__ __forceinline__ int* err() const { return probs[0].g.err; }  // shared by all problems
+  __device__ __forceinline__ uint64_t wait_ns() const { return probs[0].g.wait_ns; }
+  __device__ __forceinline__ const CUtensorMap* mapA(int prob) const { return maps + 2 * prob; }
+  __device__ __forceinline__ const CUtensorMap* mapB(int prob) const { return maps + 2 * prob + 1; }
+  __device__ __forceinline__ TileRef tile(int i) const {
+    const GroupedTile tl = tiles[i];
+    const int N = cols[probs[tl.prob].cohort];
+    return TileRef{tl.prob, tl.m_tile, tl.n_tile, N, tl.n_tile * BN >= N};
+  }
+};
+
+// The producer thread of each CTA picks its next tile and publishes the
+// index to the CTA's MMA thread and epilogue warps through a small ring in
+// shared memory (tq_full / tq_empty barriers); an index past the end (-1)
+// tells them to stop.  Tiles of uneven cost (grouped problems, the
+// triangular L^-1 operand) are taken from a launch-wide counter, so that
+// tiles listed longest first balance like the hardware block scheduler would,
+// without a CTA launch per tile; uniform tiles are dealt statically in
+// rounds of gridDim.x, forward in even rounds and backward in odd ones
+// (measured 2 % faster than the counter on the eigen operand).  The counter
+// pair (next tile, finished CTAs) starts at zero; the last CTA to finish
+// zeroes it again for the next launch on the stream, so no reset is enqueued.
+constexpr int TQ = 4;                // tile-queue slots
+constexpr int TQ_CONSUMERS = 1 + 8;  // the MMA thread and lane 0 of each epilogue warp
+
+// Persistent split GEMM: each CTA takes tiles from the launch-wide counter
+// until none are left; per tile, (S + 1) / 2 passes of two slices each.  Per
+// pass the epilogue reads both accumulators from TMEM 32 columns at a time,
+// combines them exactly in int32 (q = P_2p * BASE + P_2p+1), folds q into
+// the int64 partial sums in C (V = V * BASE^2 + q; on the last pass the FP64
+// / squared float-pair output) and then hands TMEM back to the MMA warp.
+// Between tiles the producer keeps loading the next tile's operands, so a
+// CTA never drains its ring, and TMEM is allocated and the barriers
+// initialised once per CTA.  (Releasing TMEM before the C round trip, with
+// q held in registers, measured slower: within 168 registers a thread keeps
+// too few partial-sum loads in flight for the round trip to finish within
+// one pass of MMAs.)
+template <int KB, int ESZ, class Src>
+__device__ __forceinline__ void gemm_persistent(const Src& src, int* tile_counter) {
   using R = GemmRing<KB, ESZ>;
   constexpr int BASE = ESZ == 1 ? 32 : 256;  // digit base: FP8 five-bit, BF16 eight-bit digits
   extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -327,14 +412,15 @@ __device__ __forceinline__ void gemm_tile(const CUtensorMap* tmA, const CUtensor
   uint64_t* tfull = empty + R::STAGES;
   uint64_t* tempty = tfull + 1;
   uint64_t* drain = tempty + 1;
-  uint32_t* tbase_slot = (uint32_t*)(drain + 1);
+  uint64_t* tq_full = drain + 1;
+  uint64_t* tq_empty = tq_full + TQ;
+  volatile int* tq_id = (volatile int*)(tq_empty + TQ);
+  uint32_t* tbase_slot = (uint32_t*)(tq_id + TQ);
   volatile int* abort_flag = (volatile int*)(tbase_slot + 1);
+  static_assert((R::STAGES * 2 + 3 + 2 * TQ) * 8 + TQ * 4 + 8 <= 256, "barriers fit the 256-byte tail");
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = m_tile * BM, n0 = n_tile * BN;
-  const int passes = (g.S + 1) / 2;
-  int nk = g.Kpad / KB;
-  if (m0 + BM <= g.tri_rows) nk = min(nk, (m0 + BM + KB - 1) / KB);  // zero upper part of L^-1
+  const int ntiles = src.count();
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < R::STAGES; s++) {
@@ -344,6 +430,10 @@ __device__ __forceinline__ void gemm_tile(const CUtensorMap* tmA, const CUtensor
     mbar_init(tfull, 1);
     mbar_init(tempty, THREADS - 64);
     mbar_init(drain, 1);
+    for (int s = 0; s < TQ; s++) {
+      mbar_init(&tq_full[s], 1);
+      mbar_init(&tq_empty[s], TQ_CONSUMERS);
+    }
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -365,25 +455,61 @@ __device__ __forceinline__ void gemm_tile(const CUtensorMap* tmA, const CUtensor
       int issued[R::STAGES];
       uint32_t issued_phase[R::STAGES];
       for (int s = 0; s < R::STAGES; s++) issued[s] = 0;
-      if (global_maps) {
-        asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;" ::"l"((uint64_t)tmA) : "memory");
-        asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;" ::"l"((uint64_t)tmB) : "memory");
-      }
       bool ok = true;
-      for (int p = 0; p < passes && ok; p++) {
-        const int s0 = 2 * p, s1 = 2 * p + 1;
-        const bool two = s1 < g.S;
-        for (int kb = 0; kb < nk; kb++) {
-          if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, g.err, 1, g.wait_ns)) { ok = false; break; }
-          issued[stage] = 0;
-          uint8_t* sb = smem + stage * R::STAGE;
-          mbar_expect_tx(&full[stage], (two ? 2 * R::A : R::A) + R::B);
-          tma_load_2d(sb, tmA, kb * KB, s0 * g.Mpad + m0, &full[stage]);
-          if (two) tma_load_2d(sb + R::A, tmA, kb * KB, s1 * g.Mpad + m0, &full[stage]);
-          tma_load_2d(sb + 2 * R::A, tmB, kb * KB, g.col0 + n0, &full[stage]);
-          issued[stage] = 1;
-          issued_phase[stage] = phase;
-          if (++stage == R::STAGES) { stage = 0; phase ^= 1; }
+      int last_prob = -1;
+      int tq = 0;
+      uint32_t tqph = 0;
+      const bool dyn = src.dynamic();
+      int kdeal = 0;
+#pragma unroll 1
+      while (ok) {
+        int it;
+        if (dyn) {
+          it = atomicAdd(tile_counter, 1);
+        } else {
+          const int base = kdeal * (int)gridDim.x;
+          it = base >= ntiles ? ntiles
+                              : base + ((kdeal & 1) ? (int)gridDim.x - 1 - (int)blockIdx.x : (int)blockIdx.x);
+          kdeal++;
+        }
+        if (it >= ntiles) it = -1;
+        // publish the tile to the MMA thread and the epilogue warps
+        if (!mbar_wait(&tq_empty[tq], tqph ^ 1, abort_flag, src.err(), 5, src.wait_ns())) { ok = false; break; }
+        tq_id[tq] = it;
+        mbar_arrive(&tq_full[tq]);
+        if (++tq == TQ) { tq = 0; tqph ^= 1; }
+        if (it < 0) break;
+        const TileRef T = src.tile(it);
+        if (T.skip) continue;
+        const GemmArgs& g = src.args(T.prob);
+        const CUtensorMap* tmA = src.mapA(T.prob);
+        const CUtensorMap* tmB = src.mapB(T.prob);
+        if (Src::global_maps && T.prob != last_prob) {
+          asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;" ::"l"((uint64_t)tmA) : "memory");
+          asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;" ::"l"((uint64_t)tmB) : "memory");
+          last_prob = T.prob;
+        }
+        const int m0 = T.m_tile * BM, n0 = T.n_tile * BN;
+        const int passes = (g.S + 1) / 2;
+        int nk = g.Kpad / KB;
+        if (m0 + BM <= g.tri_rows) nk = min(nk, (m0 + BM + KB - 1) / KB);  // zero upper part of L^-1
+#pragma unroll 1
+        for (int p = 0; p < passes && ok; p++) {
+          const int s0 = 2 * p, s1 = 2 * p + 1;
+          const bool two = s1 < g.S;
+#pragma unroll 1
+          for (int kb = 0; kb < nk; kb++) {
+            if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, g.err, 1, g.wait_ns)) { ok = false; break; }
+            issued[stage] = 0;
+            uint8_t* sb = smem + stage * R::STAGE;
+            mbar_expect_tx(&full[stage], (two ? 2 * R::A : R::A) + R::B);
+            tma_load_2d(sb, tmA, kb * KB, s0 * g.Mpad + m0, &full[stage]);
+            if (two) tma_load_2d(sb + R::A, tmA, kb * KB, s1 * g.Mpad + m0, &full[stage]);
+            tma_load_2d(sb + 2 * R::A, tmB, kb * KB, g.col0 + n0, &full[stage]);
+            issued[stage] = 1;
+            issued_phase[stage] = phase;
+            if (++stage == R::STAGES) { stage = 0; phase ^= 1; }
+          }
         }
       }
       if (!ok) {
@@ -395,37 +521,56 @@ __device__ __forceinline__ void gemm_tile(const CUtensorMap* tmA, const CUtensor
   } else if (warp == 1) {
     if (lane == 0) {
       int stage = 0;
-      uint32_t phase = 0;
+      uint32_t phase = 0, q = 0;  // q: passes issued by this CTA (accumulator phase)
       bool ok = true;
       bool any = false;
-      for (int p = 0; p < passes && ok; p++) {
-        const bool two = 2 * p + 1 < g.S;
-        if (!mbar_wait(tempty, (p & 1) ^ 1, abort_flag, g.err, 2, g.wait_ns)) { ok = false; break; }
-        tc_fence_after();
-        for (int kb = 0; kb < nk; kb++) {
-          if (!mbar_wait(&full[stage], phase, abort_flag, g.err, 3, g.wait_ns)) { ok = false; break; }
+      int tq = 0;
+      uint32_t tqph = 0;
+#pragma unroll 1
+      while (ok) {
+        if (!mbar_wait(&tq_full[tq], tqph, abort_flag, src.err(), 6, src.wait_ns())) { ok = false; break; }
+        const int it = tq_id[tq];
+        mbar_arrive(&tq_empty[tq]);
+        if (++tq == TQ) { tq = 0; tqph ^= 1; }
+        if (it < 0) break;
+        const TileRef T = src.tile(it);
+        if (T.skip) continue;
+        const GemmArgs& g = src.args(T.prob);
+        const int m0 = T.m_tile * BM;
+        const int passes = (g.S + 1) / 2;
+        int nk = g.Kpad / KB;
+        if (m0 + BM <= g.tri_rows) nk = min(nk, (m0 + BM + KB - 1) / KB);
+#pragma unroll 1
+        for (int p = 0; p < passes && ok; p++, q++) {
+          const bool two = 2 * p + 1 < g.S;
+          if (!mbar_wait(tempty, (q & 1) ^ 1, abort_flag, g.err, 2, g.wait_ns)) { ok = false; break; }
           tc_fence_after();
-          uint8_t* sb = smem + stage * R::STAGE;
-          const uint64_t a0 = desc_gemm<R::ROW>(sb), a1 = desc_gemm<R::ROW>(sb + R::A),
-                         b = desc_gemm<R::ROW>(sb + 2 * R::A);
+#pragma unroll 1
+          for (int kb = 0; kb < nk; kb++) {
+            if (!mbar_wait(&full[stage], phase, abort_flag, g.err, 3, g.wait_ns)) { ok = false; break; }
+            tc_fence_after();
+            uint8_t* sb = smem + stage * R::STAGE;
+            const uint64_t a0 = desc_gemm<R::ROW>(sb), a1 = desc_gemm<R::ROW>(sb + R::A),
+                           b = desc_gemm<R::ROW>(sb + 2 * R::A);
 #pragma unroll
-          for (int k = 0; k < R::ROW / 32; k++) {  // 32 bytes of K per MMA (32 FP8 or 16 BF16 digits)
-            const uint64_t koff = (uint64_t)((k * 32) >> 4);
-            const uint32_t acc = (kb > 0 || k > 0) ? 1u : 0u;
-            if constexpr (ESZ == 1) {
-              mma_f8(tbase, a0 + koff, b + koff, IDESC, acc);
-              if (two) mma_f8(tbase + 256, a1 + koff, b + koff, IDESC, acc);
-            } else {
-              mma_bf16(tbase, a0 + koff, b + koff, IDESC_BF16, acc);
-              if (two) mma_bf16(tbase + 256, a1 + koff, b + koff, IDESC_BF16, acc);
+            for (int kk = 0; kk < R::ROW / 32; kk++) {  // 32 bytes of K per MMA (32 FP8 or 16 BF16 digits)
+              const uint64_t koff = (uint64_t)((kk * 32) >> 4);
+              const uint32_t acc = (kb > 0 || kk > 0) ? 1u : 0u;
+              if constexpr (ESZ == 1) {
+                mma_f8(tbase, a0 + koff, b + koff, IDESC, acc);
+                if (two) mma_f8(tbase + 256, a1 + koff, b + koff, IDESC, acc);
+              } else {
+                mma_bf16(tbase, a0 + koff, b + koff, IDESC_BF16, acc);
+                if (two) mma_bf16(tbase + 256, a1 + koff, b + koff, IDESC_BF16, acc);
+              }
             }
+            any = true;
+            mma_commit(&empty[stage]);
+            if (++stage == R::STAGES) { stage = 0; phase ^= 1; }
           }
-          any = true;
-          mma_commit(&empty[stage]);
-          if (++stage == R::STAGES) { stage = 0; phase ^= 1; }
+          if (!ok) break;
+          mma_commit(tfull);
         }
-        if (!ok) break;
-        mma_commit(tfull);
       }
       if (!ok && any) {
         // all MMAs issued by this thread complete before TMEM is released
@@ -438,96 +583,121 @@ __device__ __forceinline__ void gemm_tile(const CUtensorMap* tmA, const CUtensor
     // epilogue: warps 2..9.  Warp w reads TMEM lane quarter w % 4 (the
     // quarter a warp may access is fixed by its rank modulo 4) and column
     // half (w - 2) / 4; thread = one output row.
-    const int q = warp & 3;
+    const int lq = warp & 3;
     const int cbeg = ((warp - 2) >> 2) * (BN / 2);
-    const int row = q * 32 + lane;
-    const int r = m0 + row;
-    const bool rvalid = r < g.M;
-    const double scale = rvalid ? g.row_scale[r] : 0.0;
-    const bool sq = r < g.sq_rows;
-    const float fscale = (float)scale;  // power of two: exact while >= 2^-149
-    const int ncols = rvalid ? min(BN, g.N - n0) : 0;  // valid columns of this tile for this row
-    long long* crow = (long long*)(g.C + (long long)r + (long long)(g.col0 + n0) * g.ldc);
-    const int cend = min(cbeg + BN / 2, ncols);
-    for (int p = 0; p < passes; p++) {
-      const bool two = 2 * p + 1 < g.S;
-      const bool last = p == passes - 1;
-      // pull this row's partial sums into L2 while the pass's MMAs run
-      if (p > 0)
-        for (int c = cbeg; c < cend; c++)
-          asm volatile("prefetch.global.L2 [%0];" ::"l"(crow + (long long)c * g.ldc));
-      int ok = 1;
-      if (lane == 0) ok = mbar_wait(tfull, p & 1, abort_flag, g.err, 4, g.wait_ns) ? 1 : 0;
-      ok = __shfl_sync(0xffffffffu, ok, 0);  // warp-uniform: tcgen05.ld is .sync.aligned
-      if (!ok) break;
-      tc_fence_after();
+    const int row = lq * 32 + lane;
+    const uint32_t ta = tbase + ((uint32_t)(lq * 32) << 16) + (uint32_t)cbeg;
+    uint32_t q = 0;
+    bool ok = true;
+    int tq = 0;
+    uint32_t tqph = 0;
 #pragma unroll 1
-      for (int ch = 0; ch < BN / 64; ch++) {
-        const int c0 = cbeg + ch * 32;
-        long long prev[32];
-        if (p > 0) {
-          // all 32 partial sums in flight at once, before the TMEM reads
-#pragma unroll
-          for (int j = 0; j < 32; j++) prev[j] = (c0 + j < cend) ? __ldcg(crow + (long long)(c0 + j) * g.ldc) : 0;
-        }
-        uint32_t v0[32], v1[32];
-        const uint32_t ta = tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
-        tmem_ld32(ta, v0);
-        if (two) tmem_ld32(ta + 256, v1);
-        tmem_ld_wait();
-#pragma unroll
-        for (int j = 0; j < 32; j++) {
-          if (c0 + j >= cend) break;
-          int qv = exact_f2i(__uint_as_float(v0[j])) * BASE;
-          if (two) qv += exact_f2i(__uint_as_float(v1[j]));
-          long long* cp = crow + (long long)(c0 + j) * g.ldc;
-          const long long V = (p == 0) ? (long long)qv : prev[j] * (long long)(BASE * BASE) + (long long)qv;
-          if (!last)
-            *cp = V;
-          else if (sq)
-            *(float2*)cp = square_pair(V, fscale);
-          else
-            *(double*)cp = (double)V * scale;
+    while (ok) {
+      int it = 0, okq = 1;
+      if (lane == 0) {
+        okq = mbar_wait(&tq_full[tq], tqph, abort_flag, src.err(), 7, src.wait_ns()) ? 1 : 0;
+        if (okq) {
+          it = tq_id[tq];
+          mbar_arrive(&tq_empty[tq]);
         }
       }
-      tc_fence_before();
-      mbar_arrive(tempty);
+      okq = __shfl_sync(0xffffffffu, okq, 0);
+      it = __shfl_sync(0xffffffffu, it, 0);
+      if (!okq) { ok = false; break; }
+      if (++tq == TQ) { tq = 0; tqph ^= 1; }
+      if (it < 0) break;
+      const TileRef T = src.tile(it);
+      if (T.skip) continue;
+      const GemmArgs& g = src.args(T.prob);
+      const int m0 = T.m_tile * BM, n0 = T.n_tile * BN;
+      const int r = m0 + row;
+      const bool rvalid = r < g.M;
+      const double scale = rvalid ? g.row_scale[r] : 0.0;
+      const bool sq = r < g.sq_rows;
+      const float fscale = (float)scale;  // power of two: exact while >= 2^-149
+      const int ncols = rvalid ? min(BN, T.N - n0) : 0;  // valid columns of this tile for this row
+      const int cend = min(BN / 2, ncols - cbeg);        // of this thread's half (may be <= 0)
+      long long* crow = (long long*)(g.C + (long long)r + (long long)(g.col0 + n0 + cbeg) * g.ldc);
+      const int passes = (g.S + 1) / 2;
+#pragma unroll 1
+      for (int p = 0; p < passes; p++, q++) {
+        const bool two = 2 * p + 1 < g.S;
+        const bool last = p == passes - 1;
+        // pull this row's partial sums (written a pass ago, since evicted by
+        // the operand stream) back into L2 while the pass's MMAs run
+        if (p > 0)
+          for (int c = 0; c < cend; c++)
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(crow + (long long)c * g.ldc));
+        int okw = 1;
+        if (lane == 0) okw = mbar_wait(tfull, q & 1, abort_flag, g.err, 4, g.wait_ns) ? 1 : 0;
+        okw = __shfl_sync(0xffffffffu, okw, 0);  // warp-uniform: tcgen05.ld is .sync.aligned
+        if (!okw) { ok = false; break; }
+        tc_fence_after();
+#pragma unroll 1
+        for (int ch = 0; ch < BN / 64; ch++) {
+          const int c0 = ch * 32;
+          long long prev[32];
+          if (p > 0) {
+            // all 32 partial sums in flight at once, before the TMEM reads
+#pragma unroll
+            for (int j = 0; j < 32; j++) prev[j] = (c0 + j < cend) ? __ldcg(crow + (long long)(c0 + j) * g.ldc) : 0;
+          }
+          uint32_t v0[32], v1[32];
+          tmem_ld32(ta + c0, v0);
+          if (two) tmem_ld32(ta + 256 + c0, v1);
+          tmem_ld_wait();
+#pragma unroll
+          for (int j = 0; j < 32; j++) {
+            if (c0 + j >= cend) break;
+            int qv = exact_f2i(__uint_as_float(v0[j])) * BASE;
+            if (two) qv += exact_f2i(__uint_as_float(v1[j]));
+            long long* cp = crow + (long long)(c0 + j) * g.ldc;
+            const long long V = (p == 0) ? (long long)qv : prev[j] * (long long)(BASE * BASE) + (long long)qv;
+            if (!last)
+              *cp = V;
+            else if (sq)
+              *(float2*)cp = square_pair(V, fscale);
+            else
+              *(double*)cp = (double)V * scale;
+          }
+        }
+        tc_fence_before();
+        mbar_arrive(tempty);
+      }
     }
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(512) : "memory");
+  // the last CTA out zeroes the counters for the next launch (every CTA has
+  // then stopped fetching tiles)
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(tile_counter + 1, 1) == (int)gridDim.x - 1) {
+      atomicExch(tile_counter, 0);
+      atomicExch(tile_counter + 1, 0);
+    }
+  }
 }
 
+// Single problem: at most one CTA per SM (launch with min(tiles, SMs) CTAs);
+// tile_counter: two ints, zero before the first launch.
 __global__ void __launch_bounds__(THREADS, 1)
     ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                      const GemmArgs g) {
-  // grouped rasterization: GROUP_M row tiles share the resident column tiles
-  const int tile = blockIdx.x;
-  const int per_group = GROUP_M * g.tiles_n;
-  const int group = tile / per_group;
-  const int first_m = group * GROUP_M;
-  const int gsz = min(g.tiles_m - first_m, GROUP_M);
-  int m_tile = first_m + (tile % per_group) % gsz;
-  const int n_tile = (tile % per_group) / gsz;
-  // triangular L^-1: row tile i has ~i + 1 K-blocks, so start with the
-  // longest tiles and let the short ones fill the last wave
-  if (g.tri_rows > 0) m_tile = g.tiles_m - 1 - m_tile;
-  gemm_tile<GBK, 1>(&tmA, &tmB, g, m_tile, n_tile, false);
+                      const __grid_constant__ GemmArgs g, int* tile_counter) {
+  const SingleTiles src{&tmA, &tmB, &g};
+  gemm_persistent<GBK, 1>(src, tile_counter);
 }
 
-// Many independent problems in one launch: CTA b computes tiles[b] of
-// problem tiles[b].prob; its valid columns this launch are cols[cohort].
-// Tiles past a problem's valid columns exit before touching any resource.
+// Many independent problems in one persistent launch over a tile table;
+// tiles past a problem's valid columns this launch are skipped by all roles.
 __global__ void __launch_bounds__(THREADS, 1)
     ozaki_grouped_gemm_kernel(const GroupedTile* __restrict__ tiles, const GroupedProblem* __restrict__ probs,
-                              const CUtensorMap* __restrict__ maps, const int* __restrict__ cols) {
-  const GroupedTile tl = tiles[blockIdx.x];
-  GemmArgs g = probs[tl.prob].g;
-  g.N = cols[probs[tl.prob].cohort];
-  if (tl.n_tile * BN >= g.N) return;
-  gemm_tile<GRBK, 2>(maps + 2 * tl.prob, maps + 2 * tl.prob + 1, g, tl.m_tile, tl.n_tile, true);
+                              const CUtensorMap* __restrict__ maps, const int* __restrict__ cols, int ntiles,
+                              int* tile_counter) {
+  const GroupedTiles src{tiles, probs, maps, cols, ntiles};
+  gemm_persistent<GRBK, 2>(src, tile_counter);
 }
 
 // ---------------------------------------------------------------------------
@@ -1158,6 +1328,17 @@ cudaError_t make_map_u8(CUtensorMap* m, const void* base, long long K, long long
 
 int grid_for(long long total) { return (int)std::min<long long>((total + 255) / 256, 152LL * 32); }
 
+// CTAs of a persistent split-GEMM launch over `tiles` tiles: one per SM of
+// the current device (each CTA holds all 512 TMEM columns and most of the
+// shared memory), fewer when there are fewer tiles.
+int persistent_grid(int tiles) {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+      cudaSuccess || sms <= 0)
+    sms = 1;
+  return std::max(1, std::min(tiles, sms));
+}
+
 }  // namespace oz
 
 using namespace oz;
@@ -1233,13 +1414,13 @@ cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_
     chk(cudaGetDevice(&dev));
     chk(cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, dev));
   }
-  chk(cudaMalloc(&p->err, sizeof(int)));
+  chk(cudaMalloc(&p->err, 3 * sizeof(int)));  // [wait error word, GEMM tile counter, finished CTAs]
   if (!eigen) chk(cudaMalloc(&p->Linv, sizeof(double) * (size_t)n * n));
   if (!eigen) chk(cudaMalloc(&p->LinvT, sizeof(double) * (size_t)n * n));
   if (r == cudaSuccess) chk(cudaMemset(p->A, 0, (size_t)p->S * p->Mpad * p->Kpad));
   if (r == cudaSuccess) chk(cudaMemset(p->G, 0, (size_t)p->Ncap * p->Kpad));
   if (r == cudaSuccess) chk(cudaMemset(p->scale, 0, sizeof(double) * p->Mpad));
-  if (r == cudaSuccess) chk(cudaMemset(p->err, 0, sizeof(int)));
+  if (r == cudaSuccess) chk(cudaMemset(p->err, 0, 3 * sizeof(int)));
   if (r == cudaSuccess) chk(make_map(&p->mapA, p->A, p->Kpad, (long long)p->S * p->Mpad, BM));
   if (r == cudaSuccess) chk(make_map(&p->mapB, p->G, p->Kpad, p->Ncap, BN));
   if (r == cudaSuccess) chk(cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1274,6 +1455,9 @@ cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_
         for (int q = 0; q < 4; q++) p->qp.t[k][q] = (signed char)(t0 + q <= p->SQ + 1 - sd ? t0 + q : 0);
       }
   }
+  // the memsets above ran on the legacy default stream, which does not order
+  // against the caller's non-blocking streams: finish them before any launch
+  if (r == cudaSuccess) chk(cudaDeviceSynchronize());
   if (r != cudaSuccess) {
     ozaki_destroy(p);
     return r;
@@ -1323,7 +1507,8 @@ cudaError_t run_gemm(OzakiPlan* p, cudaStream_t s, int col0, int x, int tri_rows
   g.ldc = p->Mpad;
   g.err = p->err;
   g.wait_ns = p->wait_ns;
-  ozaki_gemm_kernel<<<g.tiles_m * g.tiles_n, THREADS, SMEM_BYTES, s>>>(p->mapA, p->mapB, g);
+  ozaki_gemm_kernel<<<persistent_grid(g.tiles_m * g.tiles_n), THREADS, SMEM_BYTES, s>>>(p->mapA, p->mapB, g,
+                                                                                        p->err + 1);
   note_launch();
   return cudaGetLastError();
 }
@@ -1548,6 +1733,7 @@ struct GroupedGemm {
   GroupedTile* tiles = nullptr;
   GroupedProblem* probs = nullptr;
   CUtensorMap* maps = nullptr;
+  int* counter = nullptr;  // tile counter and finished CTAs of the persistent launch
 };
 
 cudaError_t grouped_gemm_create(GroupedGemm** out, const GroupedGemmDesc* d, int count, int x_b, int* err) {
@@ -1601,6 +1787,9 @@ cudaError_t grouped_gemm_create(GroupedGemm** out, const GroupedGemmDesc* d, int
   chk(cudaMalloc(&gg->tiles, sizeof(GroupedTile) * tiles.size()));
   chk(cudaMalloc(&gg->probs, sizeof(GroupedProblem) * probs.size()));
   chk(cudaMalloc(&gg->maps, sizeof(CUtensorMap) * maps.size()));  // 256-byte aligned: >= the 64 a map needs
+  chk(cudaMalloc(&gg->counter, 2 * sizeof(int)));
+  if (r == cudaSuccess) chk(cudaMemset(gg->counter, 0, 2 * sizeof(int)));
+  if (r == cudaSuccess) chk(cudaDeviceSynchronize());  // the memset is on the legacy default stream
   if (r == cudaSuccess)
     chk(cudaMemcpy(gg->tiles, tiles.data(), sizeof(GroupedTile) * tiles.size(), cudaMemcpyHostToDevice));
   if (r == cudaSuccess)
@@ -1620,7 +1809,8 @@ cudaError_t grouped_gemm_create(GroupedGemm** out, const GroupedGemmDesc* d, int
 
 cudaError_t grouped_gemm_run(GroupedGemm* gg, cudaStream_t s, const int* dcols) {
   if (gg->ntiles == 0) return cudaSuccess;
-  ozaki_grouped_gemm_kernel<<<gg->ntiles, THREADS, GROUPED_SMEM_BYTES, s>>>(gg->tiles, gg->probs, gg->maps, dcols);
+  ozaki_grouped_gemm_kernel<<<persistent_grid(gg->ntiles), THREADS, GROUPED_SMEM_BYTES, s>>>(
+      gg->tiles, gg->probs, gg->maps, dcols, gg->ntiles, gg->counter);
   note_launch();
   return cudaGetLastError();
 }
@@ -1632,6 +1822,7 @@ void grouped_gemm_destroy(GroupedGemm* gg) {
   if (gg->tiles) cudaFree(gg->tiles);
   if (gg->probs) cudaFree(gg->probs);
   if (gg->maps) cudaFree(gg->maps);
+  if (gg->counter) cudaFree(gg->counter);
   delete gg;
 }
 
@@ -1663,13 +1854,13 @@ extern "C" int fglsgpu_selftest_split_gemm(int M, int K, int N, int S, const dou
   chk(cudaMalloc(&p.G, (size_t)p.Ncap * p.Kpad));
   chk(cudaMalloc(&p.scale, sizeof(double) * p.Mpad));
   chk(cudaMalloc(&p.C, sizeof(double) * (size_t)p.Mpad * p.Ncap));
-  chk(cudaMalloc(&p.err, sizeof(int)));
+  chk(cudaMalloc(&p.err, 3 * sizeof(int)));
   chk(cudaMalloc(&dA, sizeof(double) * (size_t)M * K));
   chk(cudaMalloc(&dX, sizeof(double) * (size_t)K * N));
   if (r == cudaSuccess) chk(cudaMemset(p.A, 0, (size_t)S * p.Mpad * p.Kpad));
   if (r == cudaSuccess) chk(cudaMemset(p.G, 0, (size_t)p.Ncap * p.Kpad));
   if (r == cudaSuccess) chk(cudaMemset(p.scale, 0, sizeof(double) * p.Mpad));
-  if (r == cudaSuccess) chk(cudaMemset(p.err, 0, sizeof(int)));
+  if (r == cudaSuccess) chk(cudaMemset(p.err, 0, 3 * sizeof(int)));
   if (r == cudaSuccess) chk(cudaMemcpy(dA, A, sizeof(double) * (size_t)M * K, cudaMemcpyHostToDevice));
   if (r == cudaSuccess) chk(cudaMemcpy(dX, X, sizeof(double) * (size_t)K * N, cudaMemcpyHostToDevice));
   if (r == cudaSuccess) chk(make_map(&p.mapA, p.A, p.Kpad, (long long)S * p.Mpad, BM));
@@ -1706,7 +1897,8 @@ extern "C" int fglsgpu_selftest_split_gemm(int M, int K, int N, int S, const dou
 // pool has reserved the memory), and code that must not change the device's
 // memory footprint between steps.  They pass device buffers for the inputs
 // and the output; the kernel's scratch (E4M3 slices of A, the E4M3 genotype
-// operand, per-row scales, an error word) lives in the file-scope array below,
+// operand, per-row scales, an error word and the GEMM's tile counters) lives
+// in the file-scope array below,
 // which every GPU that loads this library holds until the process exits.
 //
 // Limits (the array's size, 5.8 MB): M <= 256, K <= 2048, N <= 512,
@@ -1723,7 +1915,7 @@ constexpr int NA_MAX_M = 256, NA_MAX_K = 2048, NA_MAX_N = 512, NA_MAX_S = MAX_SL
 constexpr size_t NA_A_BYTES = (size_t)NA_MAX_S * NA_MAX_M * NA_MAX_K;   // E4M3 slices
 constexpr size_t NA_G_BYTES = (size_t)NA_MAX_N * NA_MAX_K;              // E4M3 genotypes
 constexpr size_t NA_SCALE_BYTES = (size_t)NA_MAX_M * 8;                     // row scales
-constexpr size_t NA_BYTES = NA_A_BYTES + NA_G_BYTES + NA_SCALE_BYTES + 256;  // + error word
+constexpr size_t NA_BYTES = NA_A_BYTES + NA_G_BYTES + NA_SCALE_BYTES + 256;  // + error word, tile counters
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
 
 constexpr int NA_MAX_DEVICES = 64;
@@ -1777,7 +1969,7 @@ extern "C" int fglsgpu_split_gemm_noalloc(int M, int K, int N, int slices, const
   chk(cudaMemsetAsync(p.A, 0, (size_t)slices * p.Mpad * p.Kpad, s));
   chk(cudaMemsetAsync(p.G, 0, (size_t)p.Ncap * p.Kpad, s));
   chk(cudaMemsetAsync(p.scale, 0, sizeof(double) * p.Mpad, s));
-  chk(cudaMemsetAsync(p.err, 0, sizeof(int), s));
+  chk(cudaMemsetAsync(p.err, 0, 3 * sizeof(int), s));  // error word and the GEMM's tile counters
   if (r == cudaSuccess) chk(make_map(&p.mapA, p.A, p.Kpad, (long long)slices * p.Mpad, BM));
   if (r == cudaSuccess) chk(make_map(&p.mapB, p.G, p.Kpad, p.Ncap, BN));
   if (r == cudaSuccess) {
@@ -1805,7 +1997,8 @@ extern "C" int fglsgpu_split_gemm_noalloc(int M, int K, int N, int slices, const
     g.sq_rows = 0;
     g.err = p.err;
     g.wait_ns = WAIT_NS;
-    ozaki_gemm_kernel<<<g.tiles_m * g.tiles_n, THREADS, SMEM_BYTES, s>>>(p.mapA, p.mapB, g);
+    ozaki_gemm_kernel<<<persistent_grid(g.tiles_m * g.tiles_n), THREADS, SMEM_BYTES, s>>>(p.mapA, p.mapB, g,
+                                                                                          p.err + 1);
     note_launch();
     chk(cudaGetLastError());
   }

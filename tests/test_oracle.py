@@ -152,3 +152,16 @@ def test_bed_writer_follows_the_plink_bit_layout():
             code = (body[i, k // 4] >> (2 * (k % 4))) & 3
             want = 3 if k >= 10 else {2: 0, 1: 2, 0: 3}[int(pb.XR[k, i])]
             assert code == want, (i, k, code, want)
+
+
+def test_device_packer_matches_the_host_packer():
+    """bench.pack_2bit_device (torch) writes the same .bed body bytes as
+    datagen.pack_2bit."""
+    import torch
+    import bench
+    from fgls_gb300 import datagen
+    rng = np.random.default_rng(2)
+    for n in (12, 13, 15):
+        G = rng.integers(0, 3, size=(7, n)).astype(np.uint8)
+        got = bench.pack_2bit_device(torch.from_numpy(G)).numpy()
+        assert np.array_equal(got, datagen.pack_2bit(G)), n
