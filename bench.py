@@ -318,6 +318,7 @@ def run_chol(args):
     n, xb, t = args.n, 4096, 1
     Phi, XL, Y, h, s = make_problem_gpu(n, t, 4321, dev, h=0.5, sigma=2.0)
     pool = [genotype_block(xb, n, 500 + i, dev) for i in range(2)]
+    torch.cuda.synchronize()  # the engine's streams do not wait for torch's
     p = WXL + WXR
     dB = torch.empty(xb * p, dtype=torch.float64, device=dev)
     dV = torch.empty(xb * p * p, dtype=torch.float64, device=dev)
@@ -435,6 +436,7 @@ def run_adjoint(args):
     pool = [genotype_block(xb, n, 700 + i, dev) for i in range(2)]
     g = torch.Generator(device=dev).manual_seed(5)
     bbar = torch.randn(t * xb * p, generator=g, device=dev, dtype=torch.float64)
+    torch.cuda.synchronize()  # the engine's streams do not wait for torch's
     dB = torch.empty(t * xb * p, dtype=torch.float64, device=dev)
     dV = torch.empty(t * xb * p * p, dtype=torch.float64, device=dev)
     stream = torch.cuda.ExternalStream(eng.stream(), device=dev)
@@ -538,6 +540,102 @@ def run_adjoint(args):
     print(json.dumps(line), flush=True)
 
 
+def run_kernels(args):
+    """The HBM-bound kernels around the split GEMM at the headline size
+    (n = 10000, t = 100, one 16384-SNP block), each timed with CUDA events on
+    the engine stream; achieved GB/s from the algorithmic bytes of each:
+    genotype operand build (FP64 and 2-bit packed input), batched p x p
+    solves with B/V emission, p-values, the compact beta/SE/p output, the
+    FP64 path's 2-bit unpack + widening, and the REML fit of all traits."""
+    import torch
+    from fgls_gb300 import Engine
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    n, t, xb, p = args.n, args.t, args.xb, WXL + WXR
+    pk, pk_kind = peaks()
+    hbm = float(pk.get("hbm_gbs", FALLBACK_PEAKS["hbm_gbs"]))
+    Phi, XL, Y, h, s = make_problem_gpu(n, t, 1234, dev)
+    eng = Engine(n, WXL, WXR, t, xb, variant="eigen", precision="split", slices=args.slices)
+    eng.set_problem(Phi, XL, Y, h, s)
+    X = genotype_block(xb, n, 100, dev)
+    Xpk = pack_2bit_device(X)
+    torch.cuda.synchronize()  # the engine's streams do not wait for torch's
+    dB = torch.empty(t * xb * p, dtype=torch.float64, device=dev)
+    dV = torch.empty(t * xb * p * p, dtype=torch.float64, device=dev)
+    stream = torch.cuda.ExternalStream(eng.stream(), device=dev)
+    reps = max(3, args.steps // 4)
+    out = {}
+
+    def timed(fn, reps=reps):
+        fn()
+        eng.sync()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        b.synchronize()
+        eng.sync()
+        return a.elapsed_time(b) / reps
+
+    def classes(fn, reps=reps):
+        fn()
+        eng.sync()
+        eng.profile(True)
+        for _ in range(reps):
+            fn()
+        eng.sync()
+        pr = eng.profile_read()
+        eng.profile(False)
+        return {k: v[0] / max(v[1], 1) for k, v in pr.items() if v[1]}
+
+    def gbs(nbytes, ms):
+        return {"ms": ms, "bytes": nbytes, "GB_s": nbytes / (ms / 1e3) / 1e9, "frac_of_hbm": nbytes / (ms / 1e3) / 1e9 / hbm}
+
+    Kpad = -(-n // 128) * 128
+    blk = lambda packed=False: eng.run_block_device(  # noqa: E731
+        (Xpk if packed else X).data_ptr(), xb, dB.data_ptr(), dV.data_ptr(), xb * p, xb * p * p, packed=packed)
+    c64 = classes(lambda: blk())
+    cpk = classes(lambda: blk(packed=True))
+    out["genotypes_f8_kernel (FP64 input)"] = gbs(xb * n * 8 + xb * Kpad, c64["genotypes"])
+    out["genotypes_packed_f8_kernel"] = gbs(xb * ((n + 3) // 4) + xb * Kpad, cpk["genotypes"])
+    # solves: per test the Gram terms in (1 + wXL + 1 doubles: x~'y~, x~'XL~, x~'x~) and B, V out
+    out["snp_solve_kernel"] = gbs(t * xb * ((1 + WXL + 1) + p + p * p) * 8, c64["solve"])
+    dP = torch.empty(t * xb * WXR, dtype=torch.float64, device=dev)
+    ms = timed(lambda: eng.pvalues_device(dB.data_ptr(), dV.data_ptr(), xb, xb * p, xb * p * p, dP.data_ptr(),
+                                          xb * WXR))
+    out["pvalues_kernel"] = gbs(t * xb * WXR * 3 * 8, ms)  # beta_k and SE_k in, p out
+    # FP64 path with packed input: 2-bit unpack + widening to FP64 (a smaller block: the FP64 GEMM is slow)
+    eng.set_precision("fp64")
+    x64 = 1024
+    c = classes(lambda: eng.run_block_device(Xpk.data_ptr(), x64, dB.data_ptr(), dV.data_ptr(), x64 * p,
+                                             x64 * p * p, packed=True), reps=2)
+    out["unpack_2bit_kernel + u8_to_f64_kernel (FP64 path)"] = gbs(x64 * ((n + 3) // 4) + x64 * n * (1 + 1 + 8),
+                                                                    c["genotypes"])
+    eng.set_precision("split")
+    # compact beta/SE/p output through the host API (pinned host genotypes, 2
+    # blocks); the snp_compact kernel's own time is in the launch list
+    Xh = torch.empty((2 * xb, n), dtype=torch.float64, pin_memory=True)
+    Xh[:xb].copy_(X)
+    Xh[xb:].copy_(X)
+    a = time.perf_counter()
+    eng.run_snps_compact(Xh.numpy().T)
+    out["run_snps_compact (host API, 2 blocks)"] = {"ms": (time.perf_counter() - a) * 1e3,
+                                                    "tests": 2 * xb * t, "note": "host-timed, copies included"}
+    eng.reml_fit()
+    a = time.perf_counter()
+    eng.reml_fit()
+    out["reml_fit_kernel"] = {"ms": (time.perf_counter() - a) * 1e3, "traits": t,
+                              "bytes_per_evaluation": (WXL + 2) * n * 8, "note": "host-timed, one launch"}
+    eng.close()
+    del Xh
+    line = {"metric": "HBM-bound kernels of the split eigen path (achieved GB/s)", "value": None, "unit": "GB/s",
+            "n_gpus": 1, "steps": reps, "warmup": 1, "higher_is_better": True, "data": "synthetic",
+            "config": {"workload": f"n={n} t={t} block of {xb} SNPs", "kernels": out,
+                       "hbm_peak_gbs": hbm, "peak_source": f"{pk_kind} hbm_gbs"}}
+    print(json.dumps(line), flush=True)
+
+
 COHORT_BUCKETS = ((500, 1000), (1000, 2000), (2000, 4000), (4000, 8001))
 
 
@@ -596,6 +694,7 @@ def run_cohorts(args):
     log(f"[bench] cohorts: data {gen_s:.1f}s, setup {setup_s:.1f}s, x_b={xb}, slices={S}, probe err {perr:.2e}")
     pool = 2
     X = [[genotype_block(xb, c["n"], c["seed"] + i, dev).to(torch.uint8) for i in range(pool)] for c in co]
+    torch.cuda.synchronize()  # the batch's stream does not wait for torch's
     dB = [torch.empty(T * xb * c["p"], dtype=torch.float64, device=dev) for c in co]
     dV = [torch.empty(T * xb * c["p"] ** 2, dtype=torch.float64, device=dev) for c in co]
     stream = torch.cuda.ExternalStream(b.stream(), device=dev)
@@ -763,7 +862,7 @@ def main():
     ap.add_argument("--n", type=int, default=N_IND)
     ap.add_argument("--t", type=int, default=T_TRAITS)
     ap.add_argument("--xb", type=int, default=16384)
-    ap.add_argument("--slices", type=int, default=9)
+    ap.add_argument("--slices", type=int, default=0)  # 0: the engine's probe autotuner picks 6..9
     ap.add_argument("--pool", type=int, default=4)
     ap.add_argument("--e2e-blocks", type=int, default=8)
     ap.add_argument("--fp64-snps", type=int, default=2048)
@@ -771,7 +870,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-snps", type=int, default=128)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="eigen", choices=["eigen", "cohorts", "chol", "adjoint"])
+    ap.add_argument("--workload", default="eigen", choices=["eigen", "cohorts", "chol", "adjoint", "kernels"])
     ap.add_argument("--cohorts", type=int, default=64)
     args = ap.parse_args()
 
@@ -788,6 +887,8 @@ def main():
         return run_chol(args)
     if args.workload == "adjoint":
         return run_adjoint(args)
+    if args.workload == "kernels":
+        return run_kernels(args)
 
     import torch
     dist = None
@@ -821,9 +922,12 @@ def run_eigen(args, rank, world, local, dist):
     t0 = time.perf_counter()
     eng.set_problem(Phi, XL, Y, h, s)
     setup_s = time.perf_counter() - t0
-    log(f"[bench] rank {rank}: data {gen_s:.1f}s, setup (eigendecomposition + operands) {setup_s:.1f}s")
+    S_used, S_err = eng.split_params()
+    log(f"[bench] rank {rank}: data {gen_s:.1f}s, setup (eigendecomposition + operands) {setup_s:.1f}s, "
+        f"slices {S_used} (probe err {S_err:.2e})")
 
     pool = [genotype_block(xb, n, sd, dev) for sd in rank_block_seeds(rank, args.pool)]
+    torch.cuda.synchronize()  # the engine's streams do not wait for torch's
     dB = torch.empty(t * xb * p, dtype=torch.float64, device=dev)
     dV = torch.empty(t * xb * p * p, dtype=torch.float64, device=dev)
     stream = torch.cuda.ExternalStream(eng.stream(), device=dev)
@@ -865,7 +969,7 @@ def run_eigen(args, rank, world, local, dist):
     # roofline of the dominant kernel, the tcgen05 split GEMM: sliced FP8 MMA
     # operations per launch = 2 S M_A n per SNP column, M_A = n + t (1 + wXL)
     M_A = n + t * (1 + WXL)
-    flops_snp = 2.0 * args.slices * M_A * n
+    flops_snp = 2.0 * S_used * M_A * n
     gemm_ms, gemm_n = prof["split_gemm"]
     gemm_s = gemm_ms / 1e3
     achieved = flops_snp * xb * args.steps / gemm_s / 1e12
@@ -877,12 +981,13 @@ def run_eigen(args, rank, world, local, dist):
     peak = 2.0 * float(pk.get(pk_key, FALLBACK_PEAKS[pk_key]))
     traffic = gemm_traffic(n, t, xb)
     Mpad, Kpad = -(-M_A // 128) * 128, -(-n // 128) * 128
-    algo_bytes = args.slices * Mpad * Kpad + xb * Kpad + 8 * Mpad * xb  # A slices + genotypes read, C written once
+    algo_bytes = S_used * Mpad * Kpad + xb * Kpad + 8 * Mpad * xb  # A slices + genotypes read, C written once
 
     # all-FP64 device path on the same problem (same eigendecomposition)
     eng.set_precision("fp64")
     x64 = min(args.fp64_snps, xb)
     Xp = pool[0][:x64].contiguous()
+    torch.cuda.synchronize()
     dB64 = torch.empty(t * x64 * p, dtype=torch.float64, device=dev)
     dV64 = torch.empty(t * x64 * p * p, dtype=torch.float64, device=dev)
     eng.run_block_device(Xp.data_ptr(), x64, dB64.data_ptr(), dV64.data_ptr(), x64 * p, x64 * p * p)
@@ -1000,7 +1105,9 @@ def run_eigen(args, rank, world, local, dist):
         "config": {
             "workload": f"fgls_eigen split-precision, n={n} p=4 t={t}, job m={M_JOB} SNPs, "
                         f"steps of x_b={xb} SNPs x {t} traits",
-            "n": n, "t": t, "p": 4, "m_job": M_JOB, "x_b": xb, "slices": args.slices,
+            "n": n, "t": t, "p": 4, "m_job": M_JOB, "x_b": xb, "slices": S_used,
+            "slices_choice": ("autotuned: smallest of 6..9 within 1e-10/8 of the FP64 path on a 256-SNP probe "
+                              f"block (probe beta error {S_err:.2e})" if args.slices == 0 else "given"),
             "genotype_input": "FP64 reference layout, resident in HBM",
             "l2": f"inputs larger than L2: {len(pool)} distinct {xb * n * 8 / 1e9:.2f} GB blocks cycled",
             "setup_s": setup_s, "job_s_estimate": M_JOB * t / value + setup_s,
@@ -1018,7 +1125,7 @@ def run_eigen(args, rank, world, local, dist):
                      "peak_source": f"2 x {pk_kind} {pk_key} (FP8 dense rate = 2 x BF16; "
                                     f"timed region {timed_s:.2f} s)",
                      "fp64_equivalent_tflops": 2.0 * M_A * n * xb * args.steps / gemm_s / 1e12,
-                     "work": f"2*{args.slices} slices*{M_A} rows*{n} K per SNP; {gemm_n} launches, "
+                     "work": f"2*{S_used} slices*{M_A} rows*{n} K per SNP; {gemm_n} launches, "
                              f"{gemm_ms / max(gemm_n, 1):.3f} ms each"},
         "e2e": {"value": e2e_value if gate_ok else None, "unit": UNIT, "h2d_bytes_per_step": xb * n * 8,
                 "d2h_bytes_per_step": t * xb * (p + p * p) * 8,

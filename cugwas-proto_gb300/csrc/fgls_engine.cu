@@ -17,6 +17,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cmath>
 #include <string>
 #include <vector>
 
@@ -51,6 +52,7 @@ struct fglsgpu_engine {
   int* hst_wait = nullptr;  // pinned copy of the split plan's wait error word
   OzakiPlan* oz = nullptr;  // split-precision state (eigen / chol)
   unsigned long long wait_ns = 0;  // limit of one tcgen05 pipeline wait (0: the 2 s default)
+  double tune_err = -1.0;          // probe-block beta error of the tuned slice count (-1: not tuned)
   std::vector<double> hh, hs;
   int trait_sel = -1;
   bool problem_set = false;
@@ -297,6 +299,118 @@ int compute_block(fglsgpu_engine* e, const void* dX, int fmt, int x, double* dB,
 
 int out_traits(const fglsgpu_engine* e) { return e->cfg.variant == FGLSGPU_VARIANT_EIGEN ? e->cfg.t : 1; }
 
+// Hard calls of a probe block: SNP i with allele frequency f_i in
+// [0.05, 0.5) and genotype Binomial(2, f_i), both from an integer hash of
+// (SNP, individual) (fixed, so the choice is reproducible).
+__device__ __forceinline__ unsigned probe_hash(unsigned h) {
+  h ^= h >> 16;
+  h *= 0x7feb352du;
+  h ^= h >> 15;
+  h *= 0x846ca68bu;
+  h ^= h >> 16;
+  return h;
+}
+__global__ void probe_genotypes_kernel(int n, int x, double* __restrict__ out) {
+  const int i = blockIdx.x;
+  const unsigned fi = 50 + probe_hash(0x9e3779b9u * (unsigned)(i + 1)) % 450;  // per mille
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const unsigned h1 = probe_hash((unsigned)i * 2654435761u ^ (unsigned)(2 * k + 1));
+    const unsigned h2 = probe_hash((unsigned)i * 2246822519u ^ (unsigned)(2 * k + 2));
+    out[(long long)i * n + k] = (double)((h1 % 1000 < fi) + (h2 % 1000 < fi));
+  }
+}
+
+// Slice autotuning (cfg.slices == 0): the split operand holds 9 five-bit
+// digit slices; a probe block of 256 SNPs runs through the all-FP64 path and
+// through the split path with the first 6, 7, 8 and 9 slices, and the
+// smallest count whose beta (normwise per trait and SNP) is within
+// TUNE_TOL / 8 of the FP64 result is kept.  Called after every build of the
+// split operands (they depend on the trait's weights or factor).
+constexpr double TUNE_TOL = 1e-10;
+constexpr int TUNE_SNPS = 256, TUNE_MIN_SLICES = 6;
+
+int tune_slices(fglsgpu_engine* e) {
+  fglsgpu_config& c = e->cfg;
+  if (!split(e) || !e->oz || c.slices != 0) return FGLSGPU_OK;
+  cudaStream_t s = e->comp;
+  const int n = c.n, p = e->p, nt = out_traits(e), xp = std::min(TUNE_SNPS, c.x_b);
+  int built = 0;
+  ozaki_slices(e->oz, &built);
+  double *dX = nullptr, *dBr = nullptr, *dVr = nullptr, *dBs = nullptr, *dVs = nullptr, *dW = nullptr, *dQ = nullptr;
+  cudaError_t r = cudaSuccess;
+  auto chk = [&](cudaError_t x) {
+    if (r == cudaSuccess) r = x;
+  };
+  chk(dalloc(&dX, (size_t)n * xp));
+  chk(dalloc(&dBr, (size_t)nt * xp * p));
+  chk(dalloc(&dVr, (size_t)nt * xp * p * p));
+  chk(dalloc(&dBs, (size_t)nt * xp * p));
+  chk(dalloc(&dVs, (size_t)nt * xp * p * p));
+  if (c.variant == FGLSGPU_VARIANT_EIGEN) {
+    chk(dalloc(&dW, (size_t)n * xp));
+    chk(dalloc(&dQ, (size_t)n * xp));
+  }
+  auto release = [&]() {
+    for (double* q : {dX, dBr, dVr, dBs, dVs, dW, dQ})
+      if (q) cudaFree(q);
+  };
+  if (r != cudaSuccess) {
+    release();
+    return cuda_fail(e, r, "slice probe buffers");
+  }
+  probe_genotypes_kernel<<<xp, 256, 0, s>>>(n, xp, dX);
+  note_launch();
+  int rc = reset_status(e);
+  // the FP64 reference on probe-sized work buffers
+  double* keepW = e->dWork;
+  double* keepQ = e->dQ;
+  if (c.variant == FGLSGPU_VARIANT_EIGEN) {
+    e->dWork = dW;
+    e->dQ = dQ;
+  }
+  c.precision = FGLSGPU_PREC_FP64;
+  if (!rc) rc = compute_block(e, dX, GENO_F64, xp, dBr, dVr, (long long)xp * p, (long long)xp * p * p, 0);
+  c.precision = FGLSGPU_PREC_SPLIT;
+  e->dWork = keepW;
+  e->dQ = keepQ;
+  std::vector<double> Br((size_t)nt * xp * p), Bs(Br.size());
+  if (!rc && cudaMemcpyAsync(Br.data(), dBr, sizeof(double) * Br.size(), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    rc = fail(e, FGLSGPU_ECUDA, "slice probe copy");
+  int chosen = built;
+  double err = -1.0;
+  for (int S = std::min(TUNE_MIN_SLICES, built); S <= built && !rc; S++) {
+    ENG_TRY(e, ozaki_set_run_slices(e->oz, s, S), "slice probe");
+    rc = compute_block(e, dX, GENO_F64, xp, dBs, dVs, (long long)xp * p, (long long)xp * p * p, 0);
+    if (rc) break;
+    ENG_TRY(e, cudaMemcpyAsync(Bs.data(), dBs, sizeof(double) * Bs.size(), cudaMemcpyDeviceToHost, s),
+            "slice probe copy");
+    ENG_TRY(e, cudaStreamSynchronize(s), "slice probe");
+    double worst = 0.0;
+    for (size_t q = 0; q < Br.size(); q += p) {
+      double d2 = 0.0, r2 = 0.0;
+      for (int k = 0; k < p; k++) {
+        const double d = Bs[q + k] - Br[q + k];
+        d2 += d * d;
+        r2 += Br[q + k] * Br[q + k];
+      }
+      const double rel = r2 > 0.0 ? std::sqrt(d2 / r2) : std::sqrt(d2);
+      worst = (rel > worst || rel != rel) ? rel : worst;
+    }
+    err = worst;
+    if (worst <= TUNE_TOL / 8) {
+      chosen = S;
+      break;
+    }
+  }
+  release();
+  if (!rc) rc = check_status(e, "slice probe");
+  if (rc) return rc;
+  ENG_TRY(e, ozaki_set_run_slices(e->oz, s, chosen), "slice choice");
+  ENG_TRY(e, cudaStreamSynchronize(s), "slice choice");
+  e->tune_err = err;
+  return FGLSGPU_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -447,6 +561,8 @@ int fglsgpu_set_problem(fglsgpu_engine* e, const double* Phi, const double* XL, 
       }
       ENG_TRY(e, ozaki_set_eigen(e->oz, s, e->dZ, e->dAYL, e->ddinv), "split operands");
       ENG_TRY(e, cudaStreamSynchronize(s), "split operands");
+      rc = tune_slices(e);
+      if (rc) return rc;
     }
   }
   ENG_TRY(e, cudaStreamSynchronize(s), "set_problem");
@@ -484,6 +600,12 @@ int fglsgpu_select_trait(fglsgpu_engine* e, int j) {
     ozaki_set_wait_limit(e->oz, e->wait_ns);
     ENG_TRY(e, ozaki_set_chol(e->oz, s, e->dL, e->dWY), "split operands");
     ENG_TRY(e, cudaStreamSynchronize(s), "split operands");
+    e->trait_sel = j;
+    rc = tune_slices(e);
+    if (rc) {
+      e->trait_sel = -1;
+      return rc;
+    }
   }
   e->trait_sel = j;
   return FGLSGPU_OK;
@@ -695,8 +817,17 @@ int fglsgpu_set_precision(fglsgpu_engine* e, int precision) {
     ozaki_set_wait_limit(e->oz, e->wait_ns);
     ENG_TRY(e, ozaki_set_eigen(e->oz, e->comp, e->dZ, e->dAYL, e->ddinv), "split operands");
     ENG_TRY(e, cudaStreamSynchronize(e->comp), "split operands");
+    const int rc = tune_slices(e);
+    if (rc) return rc;
   }
   if (c.variant == FGLSGPU_VARIANT_CHOL) e->trait_sel = -1;  // re-select: the operands differ per path
+  return FGLSGPU_OK;
+}
+
+int fglsgpu_split_params(fglsgpu_engine* e, int* slices, double* probe_err) {
+  if (!e) return fail(nullptr, FGLSGPU_EINVAL, "null engine");
+  if (slices) *slices = e->oz ? ozaki_slices(e->oz, nullptr) : 0;
+  if (probe_err) *probe_err = e->tune_err;
   return FGLSGPU_OK;
 }
 
@@ -905,6 +1036,9 @@ int fglsgpu_set_hsigma(fglsgpu_engine* e, const double* h, const double* sigma) 
     if (!e->oz) ENG_TRY(e, ozaki_create(&e->oz, c.n, c.t, c.wXL, c.wXR, c.x_b, c.slices, 1), "split plan");
     ozaki_set_wait_limit(e->oz, e->wait_ns);
     ENG_TRY(e, ozaki_set_eigen(e->oz, s, e->dZ, e->dAYL, e->ddinv), "split operands");
+    ENG_TRY(e, cudaStreamSynchronize(s), "split operands");
+    rc = tune_slices(e);
+    if (rc) return rc;
   }
   ENG_TRY(e, cudaStreamSynchronize(s), "set_hsigma");
   e->problem_set = true;

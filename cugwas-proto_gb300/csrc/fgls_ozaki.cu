@@ -1376,6 +1376,8 @@ struct OzakiPlan {
   CUtensorMap mapA, mapB;
   bool maps = false;
   int sub = 0;                      // SNPs per pipelined sub-block (multiple of BN)
+  int S_run = 0;                    // slices the GEMM uses: the first S_run of the S built
+  double* scale_run = nullptr;      // Mpad row scales for S_run slices (when S_run < S)
   unsigned long long wait_ns = WAIT_NS;  // limit of one wait in the tcgen05 kernels
 };
 
@@ -1390,6 +1392,7 @@ cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_
   p->wXR = wXR;
   p->x_b = x_b;
   p->S = slices > 0 ? std::min(slices, MAX_SLICES) : DEFAULT_SLICES;
+  p->S_run = p->S;
   p->eigen = eigen;
   p->nU = eigen ? t * (1 + wXL) : (1 + wXL);
   p->M = n + p->nU;
@@ -1403,6 +1406,7 @@ cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_
   chk(cudaMalloc(&p->A, (size_t)p->S * p->Mpad * p->Kpad));
   chk(cudaMalloc(&p->G, (size_t)p->Ncap * p->Kpad));
   chk(cudaMalloc(&p->scale, sizeof(double) * p->Mpad));
+  chk(cudaMalloc(&p->scale_run, sizeof(double) * p->Mpad));
   chk(cudaMalloc(&p->C, sizeof(double) * (size_t)p->Mpad * p->Ncap));
   chk(cudaMalloc(&p->U, sizeof(double) * (size_t)n * p->nU));
   chk(cudaMalloc(&p->D, sizeof(float2) * (size_t)n * t));
@@ -1469,7 +1473,7 @@ cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_
 
 void ozaki_destroy(OzakiPlan* p) {
   if (!p) return;
-  void* ptrs[] = {p->A,    p->G,     p->scale, p->C,     p->U,    p->D,    p->dmax, p->amax,
+  void* ptrs[] = {p->A,    p->G,     p->scale, p->scale_run, p->C, p->U, p->D,    p->dmax, p->amax,
                   p->part, p->Linv,  p->LinvT, p->err,   p->Adig, p->Ddig, p->aexp, p->dexp, p->qpart};
   for (void* q : ptrs)
     if (q) cudaFree(q);
@@ -1498,11 +1502,14 @@ cudaError_t run_gemm(OzakiPlan* p, cudaStream_t s, int col0, int x, int tri_rows
   g.col0 = col0;
   g.sq_rows = sq_rows;
   g.Kpad = p->Kpad;
-  g.S = p->S;
+  // slices in use: S_run (1..S) once set, else all S built; rescaled row
+  // scales exist only in plans made by ozaki_create
+  const int S_run = (p->S_run > 0 && p->S_run <= p->S && p->scale_run) ? p->S_run : p->S;
+  g.S = S_run;
   g.tiles_m = p->Mpad / BM;
   g.tiles_n = (x + BN - 1) / BN;
   g.tri_rows = tri_rows;
-  g.row_scale = p->scale;
+  g.row_scale = S_run == p->S ? p->scale : p->scale_run;
   g.C = p->C;
   g.ldc = p->Mpad;
   g.err = p->err;
@@ -1638,7 +1645,7 @@ double ozaki_flops_per_snp(const OzakiPlan* p) {
   // (chol: the zero upper part of L^-1 is skipped by 64-column K blocks)
   double rows_k = (double)p->M * p->n;
   if (!p->eigen) rows_k = (double)p->nU * p->n + 0.5 * (double)p->n * p->n;
-  return 2.0 * p->S * rows_k;
+  return 2.0 * p->S_run * rows_k;
 }
 
 // Gram operand view of the last block's output: rows [n, n + nU) of C.
@@ -1677,9 +1684,9 @@ cudaError_t split_chol_operand(cudaStream_t s, int n, int wXL, const double* L, 
 namespace {
 // per-row scale of an S-slice operand from that of the same digits cut at
 // S_built slices: 2^(e - 15 - 16 (passes - 1)) depends on the pass count only
-__global__ void rescale_rows_kernel(int rows, const double* __restrict__ built, int dpass, double* __restrict__ out) {
+__global__ void rescale_rows_kernel(int rows, const double* __restrict__ built, int bits, double* __restrict__ out) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r < rows) out[r] = ldexp(built[r], 16 * dpass);  // BF16 digits: 16 bits per slice pair
+  if (r < rows) out[r] = ldexp(built[r], bits);
 }
 
 template <typename T>
@@ -1713,9 +1720,26 @@ __global__ void grouped_genotypes_kernel(const GenoCohort* __restrict__ gc, cons
 cudaError_t split_rescale_rows(cudaStream_t s, int rows, const double* built_scale, int S_built, int S,
                                double* scale) {
   const int dpass = (S_built + 1) / 2 - (S + 1) / 2;
-  rescale_rows_kernel<<<(rows + 255) / 256, 256, 0, s>>>(rows, built_scale, dpass, scale);
+  rescale_rows_kernel<<<(rows + 255) / 256, 256, 0, s>>>(rows, built_scale, 16 * dpass, scale);  // 16 bits a BF16 pair
   note_launch();
   return cudaGetLastError();
+}
+
+cudaError_t ozaki_set_run_slices(OzakiPlan* p, cudaStream_t s, int S) {
+  S = std::max(1, std::min(S, p->S));
+  p->S_run = S;
+  if (S == p->S) return cudaSuccess;
+  // the first S five-bit digits of each row are its S-digit cut; with fewer
+  // slice pairs the Horner sum is 2^(10 (passes - passes_run)) smaller
+  const int dpass = (p->S + 1) / 2 - (S + 1) / 2;
+  rescale_rows_kernel<<<(p->Mpad + 255) / 256, 256, 0, s>>>(p->Mpad, p->scale, 10 * dpass, p->scale_run);
+  note_launch();
+  return cudaGetLastError();
+}
+
+int ozaki_slices(const OzakiPlan* p, int* built) {
+  if (built) *built = p->S;
+  return p->S_run;
 }
 
 cudaError_t grouped_genotypes(cudaStream_t s, const GenoCohort* dgc, const StepCohort* dsc, int cohorts, bool u8) {
@@ -1839,6 +1863,7 @@ extern "C" int fglsgpu_selftest_split_gemm(int M, int K, int N, int S, const dou
   OzakiPlan p;
   p.n = K;
   p.S = S;
+  p.S_run = S;
   p.M = M;
   p.Mpad = (M + BM - 1) / BM * BM;
   p.Kpad = (K + KALIGN - 1) / KALIGN * KALIGN;
@@ -1951,6 +1976,7 @@ extern "C" int fglsgpu_split_gemm_noalloc(int M, int K, int N, int slices, const
   OzakiPlan p;
   p.n = K;
   p.S = slices;
+  p.S_run = slices;
   p.M = M;
   p.Mpad = (M + BM - 1) / BM * BM;
   p.Kpad = (K + KALIGN - 1) / KALIGN * KALIGN;

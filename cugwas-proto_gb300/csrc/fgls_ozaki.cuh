@@ -51,6 +51,11 @@ const double* ozaki_gram_rows(const OzakiPlan* p, long long* ld);
 // kernel that gave up (0 = none).  It stays set, and later launches of the
 // plan abort, until the host reads and clears it.
 int* ozaki_error_word(OzakiPlan* p);
+// Use only the first S of the plan's digit slices in the GEMM (1..built;
+// after the operands are set: the row scales are derived from theirs).
+cudaError_t ozaki_set_run_slices(OzakiPlan* p, cudaStream_t s, int S);
+// Slices in use; *built (may be null) receives the slices the operand holds.
+int ozaki_slices(const OzakiPlan* p, int* built);
 // Limit of one pipeline wait in the plan's tcgen05 kernels (0: 2 s).
 void ozaki_set_wait_limit(OzakiPlan* p, unsigned long long ns);
 

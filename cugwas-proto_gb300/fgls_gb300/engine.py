@@ -43,7 +43,7 @@ EXPORTS = (
     "fglsgpu_batch_sync", "fglsgpu_batch_stream", "fglsgpu_batch_last_error", "fglsgpu_batch_profile",
     "fglsgpu_batch_profile_read", "fglsgpu_run_block_device_packed", "fglsgpu_run_snps_compact",
     "fglsgpu_reml_fit", "fglsgpu_set_hsigma", "fglsgpu_set_wait_limit", "fglsgpu_run_snps_u8",
-    "fglsgpu_run_snps_packed",
+    "fglsgpu_run_snps_packed", "fglsgpu_split_params",
 )
 PROF_CLASSES = ("genotypes", "split_gemm", "selfgram", "solve", "fp64_gemm", "trsm", "gram", "spare")
 
@@ -115,6 +115,7 @@ def lib():
     L.fglsgpu_reml_fit.argtypes = [P, C.c_double, C.c_double, I, P, P, P, P]
     L.fglsgpu_set_hsigma.argtypes = [P, P, P]
     L.fglsgpu_set_wait_limit.argtypes = [P, LL]
+    L.fglsgpu_split_params.argtypes = [P, C.POINTER(I), C.POINTER(C.c_double)]
     L.fglsgpu_pvalues_device.argtypes = [P, P, P, I, LL, LL, P, LL]
     L.fglsgpu_batch_create.argtypes = [C.POINTER(CohortDesc), I, C.POINTER(BatchConfig), C.POINTER(P)]
     L.fglsgpu_batch_destroy.argtypes = [P]
@@ -230,6 +231,12 @@ class Engine:
              self.L.fglsgpu_run_block_device_u8 if u8 else self.L.fglsgpu_run_block_device)
         self._check(f(self._h, C.c_void_p(xr_ptr), int(x), C.c_void_p(b_ptr), C.c_void_p(v_ptr),
                       int(bstride), int(vstride)))
+
+    def split_params(self):
+        """(slices in use, probe beta error of the autotuned choice or -1)."""
+        sl, err = C.c_int(), C.c_double()
+        self._check(self.L.fglsgpu_split_params(self._h, C.byref(sl), C.byref(err)))
+        return sl.value, err.value
 
     def set_wait_limit(self, ns=0):
         """Limit of one tcgen05 pipeline wait in ns (0: the 2 s default)."""

@@ -84,8 +84,10 @@ typedef struct {
   int x_b;       /* maximum SNPs per block                       */
   int variant;   /* FGLSGPU_VARIANT_*                            */
   int precision; /* FGLSGPU_PREC_*                               */
-  int slices;    /* split precision: 5-bit digit slices of the FP64 operand, 1..9
-                    (0 = 9, about 45 bits)                        */
+  int slices;    /* split precision: 5-bit digit slices of the FP64 operand, 1..9;
+                    0 = autotune: the operand is cut into 9 slices (about 45
+                    bits) and a 256-SNP probe block picks the smallest count
+                    in 6..9 whose beta is within 1e-10 / 8 of the FP64 path */
   int device;    /* CUDA device ordinal                          */
   int reserved;
 } fglsgpu_config;
@@ -145,7 +147,13 @@ int fglsgpu_run_snps_compact(fglsgpu_engine *e, const double *XR, long long m, d
                              double *P);
 
 /* Same with DEVICE pointers (XR, B, V already in HBM); asynchronous with
- * respect to the host: call fglsgpu_sync before reading B/V. */
+ * respect to the host: call fglsgpu_sync before reading B/V.  The engine
+ * computes on its own non-blocking stream (fglsgpu_stream), which does not
+ * wait for work queued on other streams, the legacy default stream
+ * included: the input must be complete when the call is made (synchronize
+ * the stream that produced it, or make the engine's stream wait on an event
+ * recorded after it).  The same holds for every fglsgpu_*_device call and
+ * for fglsgpu_batch_step. */
 int fglsgpu_run_block_device(fglsgpu_engine *e, const double *dXR, int x_inc, double *dB,
                              double *dV, long long b_trait_stride, long long v_trait_stride);
 
@@ -226,6 +234,12 @@ int fglsgpu_set_hsigma(fglsgpu_engine *e, const double *h, const double *sigma);
  * without redoing set_problem (eigen keeps its eigendecomposition; chol
  * needs select_trait again). */
 int fglsgpu_set_precision(fglsgpu_engine *e, int precision);
+
+/* The slice count the split path runs with (0 before the split operands
+ * exist) and, when it was autotuned (cfg.slices == 0), the probe block's
+ * largest normwise beta difference from the FP64 path at that count (-1
+ * otherwise).  No counterpart in the reference. */
+int fglsgpu_split_params(fglsgpu_engine *e, int *slices, double *probe_err);
 
 /* Limit of one pipeline wait (on an mbarrier: a TMA copy landing, an MMA
  * finishing, an epilogue draining TMEM) inside the split path's tcgen05

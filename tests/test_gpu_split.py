@@ -195,3 +195,32 @@ def test_expired_wait_is_reported_and_the_engine_recovers():
         B3, V3 = e.run_block(pb.XR[:, :256])
     assert np.array_equal(B1, B2) and np.array_equal(V1, V2)
     assert np.array_equal(B1[:, :256], B3) and np.array_equal(V1[:, :256], V3)
+
+
+@pytest.mark.parametrize("variant,t", [("eigen", 40), ("chol", 1)])
+def test_slice_autotune(variant, t):
+    """slices = 0: the operand is cut into 9 slices and a 256-SNP probe block
+    keeps the smallest count in 6..9 whose beta is within 1e-10 / 8 of the
+    FP64 path; the results at that count stay within 1e-10 of the oracle.
+    Given slices are used as they are (no probe)."""
+    from fgls_gb300 import Engine, datagen
+    pb = datagen.make_problem(400, 300, t, seed=41, hsig_uniform=True)
+    with Engine(pb.n, 3, 1, t, 256, variant=variant, precision="split", slices=0) as e:
+        e.set_problem(pb.Phi, pb.XL, pb.Y, pb.h, pb.sigma)
+        e.select_trait(0)
+        S, err = e.split_params()
+        B, V = e.run_snps(pb.XR)
+    report(f"slice_autotune_{variant}", slices=S, probe_err=err)
+    assert 6 <= S <= 9 and 0.0 <= err and (err <= 1e-10 / 8 or S == 9), (S, err)
+    if variant == "eigen":
+        Br, Vr = O.fgls_eigen(pb)
+    else:
+        pb1 = datagen.Problem(n=pb.n, m=pb.m, t=1, wXL=3, wXR=1, Phi=pb.Phi, h=pb.h[:1], sigma=pb.sigma[:1],
+                              XL=pb.XL, XR=pb.XR, Y=pb.Y[:, :1])
+        Br, Vr = O.fgls_chol(pb1, 256)
+    d = O.compare(B, V, Br, Vr)
+    assert d["beta_normwise"] <= 1e-10 and d["beta_se_scaled"] <= 1e-10 and d["se_rel"] <= 1e-10, (S, d)
+    with Engine(pb.n, 3, 1, t, 256, variant=variant, precision="split", slices=9) as e:
+        e.set_problem(pb.Phi, pb.XL, pb.Y, pb.h, pb.sigma)
+        e.select_trait(0)
+        assert e.split_params() == (9, -1.0)
