@@ -7,11 +7,16 @@
 // power-of-two scale 2^e_r:
 //   A[r, k] = 2^(e_r - 4) * sum_s d_s[r, k] * 2^(-5 s),   d_s integer in [-16, 16]
 // (round-to-nearest digits: each slice carries 5 bits, truncation error
-// <= 2^(e_r - 5 S)); every such digit is exact in E4M3.  Genotypes (0/1/2)
-// are exact in E4M3 too.  Every slice product P_s = d_s G^T is an integer
-// with |P_s| <= 16 * 2 * K < 2^20 for K <= 16383, so FP32 accumulation in
-// TMEM is exact and the result is bit-reproducible.  The kind::f8f6f4 MMA
-// runs at twice the BF16 rate: 9 five-bit slices (45 bits) cost 4.5 BF16
+// <= 2^(e_r - 5 S)).  Even slices hold d_s, odd slices d_s / 32; both are
+// exact in E4M3, and so are the genotypes (0/1/2).  One pass accumulates a
+// slice pair into ONE FP32 accumulator:
+//   v = sum_k (d_2p + d_2p+1 / 32) g_k = P_2p + P_2p+1 / 32.
+// With round-to-nearest digits d_2p + d_2p+1 / 32 = w - r / 32 for the
+// pair's leading remainder |w| <= 16 and the next one |r| <= 1/2, so
+// |v| <= (32 + 1/32) K < 2^19 for K <= FUSED_KMAX = 16368: v and every
+// partial sum are multiples of 2^-5 below 2^19, representable in FP32, and
+// the accumulation is exact and bit-reproducible.  The kind::f8f6f4 MMA runs
+// at twice the BF16 rate: 9 five-bit slices (45 bits) cost 4.5 BF16
 // slice-equivalents where 6 eight-bit BF16 slices (48 bits) cost 6.
 //
 // Kernel ozaki_gemm_kernel (persistent: one CTA per SM takes 128 x 256
@@ -21,13 +26,18 @@
 //               six 32 KB stages (the grouped launch: K-steps of 128, 128B
 //               swizzle, three 64 KB stages).
 //   warp 1      allocates 512 TMEM columns and issues tcgen05.mma
-//               (kind::f8f6f4, E4M3 x E4M3 -> F32, M=128 N=256 K=32): slice 2p
-//               into columns [0,256), slice 2p+1 into [256,512).
-//   warps 2-9   epilogue: tcgen05.ld the two accumulators, combine them
-//               exactly in int32 (q = P_2p * 32 + P_2p+1), Horner-accumulate
-//               the passes in int64 in the output buffer (V = V * 2^10 + q),
-//               and on the last pass write V * 2^(e_r - 9 - 10 (passes-1))
-//               as FP64.  |V| < 2^62 for S <= 9.
+//               (kind::f8f6f4, E4M3 x E4M3 -> F32, M=128 N=256 K=32): both
+//               slices of pass p into accumulator p % 2 (columns
+//               [256 (p % 2), 256 (p % 2) + 256)), so the MMAs of one pass run
+//               while the epilogue drains the previous one.
+//   warps 2-9   epilogue: tcgen05.ld the pass's accumulator, convert it
+//               exactly to the int32 q = 32 v = P_2p * 32 + P_2p+1,
+//               Horner-accumulate the passes in int64 in the output buffer
+//               (V = V * 2^10 + q), and on the last pass write
+//               V * 2^(e_r - 9 - 10 (passes-1)) as FP64.  |V| < 2^62 for S <= 9.
+// (The grouped launch's BF16 eight-bit digits would need 29 bits for a fused
+// pair: it accumulates slice 2p into columns [0,256) and 2p+1 into
+// [256,512) and combines them in the epilogue.)
 // Every mbarrier wait is bounded; on expiry the kernel raises an error flag,
 // drains its own in-flight copies and MMAs (bounded), frees TMEM and exits.
 //
@@ -102,6 +112,7 @@ constexpr int SMEM_BYTES = GemmRing<GBK, 1>::SMEM;          // FP8 digits
 constexpr int GROUPED_SMEM_BYTES = GemmRing<GRBK, 2>::SMEM;  // BF16 digits
 constexpr int THREADS = 320;  // producer, MMA, 8 epilogue warps
 constexpr int MAX_SLICES = 9;   // FP8 digit slices; |V| < 2^62 in the epilogue
+constexpr int FUSED_KMAX = 16368;  // K of the FP8 split GEMM: (32 + 1/32) K < 2^19
 constexpr int DEFAULT_SLICES = 9;
 constexpr int KALIGN = 128;     // K padding of the FP8 operands (one 128-byte row)
 constexpr int GROUP_M = 8;
@@ -278,6 +289,18 @@ __device__ __forceinline__ int exact_f2i(float f) {
   return __float_as_int(__fadd_rn(f, 12582912.0f)) - 0x4B400000;
 }
 
+// q = 32 v for a float v that is a multiple of 2^-5 with |v| < 2^19 (a fused
+// FP8 slice pair, P_2p + P_2p+1 / 32), exactly and without a conversion
+// instruction: h = rint(v) through the 1.5 * 2^23 addend (|v| < 2^22), the
+// remainder l = v - h in [-1/2, 1/2] is exact, and 32 l is an integer in
+// [-16, 16]; q = 32 h + 32 l, |q| < 2^24.
+__device__ __forceinline__ int fused_pair_f2i(float v) {
+  const float t = __fadd_rn(v, 12582912.0f);
+  const float l = __fsub_rn(v, __fsub_rn(t, 12582912.0f));
+  const float u = __fmaf_rn(l, 32.0f, 12582912.0f);
+  return (int)(((uint32_t)__float_as_int(t) - 0x4B400000u) * 32u + ((uint32_t)__float_as_int(u) - 0x4B400000u));
+}
+
 // An integer |x| < 2^22 as a float, exactly, without a conversion
 // instruction (the inverse of exact_f2i).
 __device__ __forceinline__ float exact_i2f(int x) { return __fsub_rn(__int_as_float(x + 0x4B400000), 12582912.0f); }
@@ -391,10 +414,14 @@ constexpr int TQ_CONSUMERS = 1 + 8;  // the MMA thread and lane 0 of each epilog
 
 // Persistent split GEMM: each CTA takes tiles from the launch-wide counter
 // until none are left; per tile, (S + 1) / 2 passes of two slices each.  Per
-// pass the epilogue reads both accumulators from TMEM 32 columns at a time,
-// combines them exactly in int32 (q = P_2p * BASE + P_2p+1), folds q into
-// the int64 partial sums in C (V = V * BASE^2 + q; on the last pass the FP64
-// / squared float-pair output) and then hands TMEM back to the MMA warp.
+// pass the epilogue reads the pass's accumulation from TMEM 32 columns at a
+// time, forms the exact int32 q = P_2p * BASE + P_2p+1, folds q into the
+// int64 partial sums in C (V = V * BASE^2 + q; on the last pass the FP64 /
+// squared float-pair output) and then hands the columns back to the MMA
+// warp.  FP8 digits (FUSED): both slices of a pass go into one 256-column
+// accumulator and passes alternate between the two halves of TMEM, so the
+// epilogue of one pass runs under the MMAs of the next.  BF16 digits: slice
+// 2p in columns [0,256), 2p+1 in [256,512), one pass at a time.
 // Between tiles the producer keeps loading the next tile's operands, so a
 // CTA never drains its ring, and TMEM is allocated and the barriers
 // initialised once per CTA.  (Releasing TMEM before the C round trip, with
@@ -409,15 +436,18 @@ __device__ __forceinline__ void gemm_persistent(const Src& src, int* tile_counte
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* full = (uint64_t*)(smem + R::STAGES * R::STAGE);
   uint64_t* empty = full + R::STAGES;
-  uint64_t* tfull = empty + R::STAGES;
-  uint64_t* tempty = tfull + 1;
-  uint64_t* drain = tempty + 1;
+  uint64_t* tfull = empty + R::STAGES;  // [2]: accumulator half ready for the epilogue
+  uint64_t* tempty = tfull + 2;         // [2]: accumulator half drained
+  uint64_t* drain = tempty + 2;
   uint64_t* tq_full = drain + 1;
   uint64_t* tq_empty = tq_full + TQ;
   volatile int* tq_id = (volatile int*)(tq_empty + TQ);
   uint32_t* tbase_slot = (uint32_t*)(tq_id + TQ);
   volatile int* abort_flag = (volatile int*)(tbase_slot + 1);
-  static_assert((R::STAGES * 2 + 3 + 2 * TQ) * 8 + TQ * 4 + 8 <= 256, "barriers fit the 256-byte tail");
+  static_assert((R::STAGES * 2 + 5 + 2 * TQ) * 8 + TQ * 4 + 8 <= 256, "barriers fit the 256-byte tail");
+  // FP8 five-bit digits: a slice pair accumulates exactly in one FP32
+  // accumulator (K <= FUSED_KMAX), so TMEM holds two passes
+  constexpr bool FUSED = ESZ == 1;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ntiles = src.count();
@@ -427,8 +457,10 @@ __device__ __forceinline__ void gemm_persistent(const Src& src, int* tile_counte
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(tfull, 1);
-    mbar_init(tempty, THREADS - 64);
+    for (int b = 0; b < 2; b++) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], THREADS - 64);
+    }
     mbar_init(drain, 1);
     for (int s = 0; s < TQ; s++) {
       mbar_init(&tq_full[s], 1);
@@ -521,7 +553,7 @@ __device__ __forceinline__ void gemm_persistent(const Src& src, int* tile_counte
   } else if (warp == 1) {
     if (lane == 0) {
       int stage = 0;
-      uint32_t phase = 0, q = 0;  // q: passes issued by this CTA (accumulator phase)
+      uint32_t phase = 0, q = 0;  // q: passes issued by this CTA (accumulator half and phase)
       bool ok = true;
       bool any = false;
       int tq = 0;
@@ -543,8 +575,12 @@ __device__ __forceinline__ void gemm_persistent(const Src& src, int* tile_counte
 #pragma unroll 1
         for (int p = 0; p < passes && ok; p++, q++) {
           const bool two = 2 * p + 1 < g.S;
-          if (!mbar_wait(tempty, (q & 1) ^ 1, abort_flag, g.err, 2, g.wait_ns)) { ok = false; break; }
+          const uint32_t buf = FUSED ? (q & 1) : 0;
+          const uint32_t par = FUSED ? ((q >> 1) & 1) : (q & 1);
+          if (!mbar_wait(&tempty[buf], par ^ 1, abort_flag, g.err, 2, g.wait_ns)) { ok = false; break; }
           tc_fence_after();
+          const uint32_t acc0 = tbase + 256 * buf;              // slice 2p
+          const uint32_t acc1 = FUSED ? acc0 : tbase + 256;     // slice 2p + 1
 #pragma unroll 1
           for (int kb = 0; kb < nk; kb++) {
             if (!mbar_wait(&full[stage], phase, abort_flag, g.err, 3, g.wait_ns)) { ok = false; break; }
@@ -557,11 +593,11 @@ __device__ __forceinline__ void gemm_persistent(const Src& src, int* tile_counte
               const uint64_t koff = (uint64_t)((kk * 32) >> 4);
               const uint32_t acc = (kb > 0 || kk > 0) ? 1u : 0u;
               if constexpr (ESZ == 1) {
-                mma_f8(tbase, a0 + koff, b + koff, IDESC, acc);
-                if (two) mma_f8(tbase + 256, a1 + koff, b + koff, IDESC, acc);
+                mma_f8(acc0, a0 + koff, b + koff, IDESC, acc);
+                if (two) mma_f8(acc1, a1 + koff, b + koff, IDESC, 1u);  // adds to slice 2p's sum
               } else {
-                mma_bf16(tbase, a0 + koff, b + koff, IDESC_BF16, acc);
-                if (two) mma_bf16(tbase + 256, a1 + koff, b + koff, IDESC_BF16, acc);
+                mma_bf16(acc0, a0 + koff, b + koff, IDESC_BF16, acc);
+                if (two) mma_bf16(acc1, a1 + koff, b + koff, IDESC_BF16, acc);
               }
             }
             any = true;
@@ -569,7 +605,7 @@ __device__ __forceinline__ void gemm_persistent(const Src& src, int* tile_counte
             if (++stage == R::STAGES) { stage = 0; phase ^= 1; }
           }
           if (!ok) break;
-          mma_commit(tfull);
+          mma_commit(&tfull[buf]);
         }
       }
       if (!ok && any) {
@@ -623,13 +659,15 @@ __device__ __forceinline__ void gemm_persistent(const Src& src, int* tile_counte
       for (int p = 0; p < passes; p++, q++) {
         const bool two = 2 * p + 1 < g.S;
         const bool last = p == passes - 1;
+        const uint32_t buf = FUSED ? (q & 1) : 0;
+        const uint32_t par = FUSED ? ((q >> 1) & 1) : (q & 1);
         // pull this row's partial sums (written a pass ago, since evicted by
         // the operand stream) back into L2 while the pass's MMAs run
         if (p > 0)
           for (int c = 0; c < cend; c++)
             asm volatile("prefetch.global.L2 [%0];" ::"l"(crow + (long long)c * g.ldc));
         int okw = 1;
-        if (lane == 0) okw = mbar_wait(tfull, q & 1, abort_flag, g.err, 4, g.wait_ns) ? 1 : 0;
+        if (lane == 0) okw = mbar_wait(&tfull[buf], par, abort_flag, g.err, 4, g.wait_ns) ? 1 : 0;
         okw = __shfl_sync(0xffffffffu, okw, 0);  // warp-uniform: tcgen05.ld is .sync.aligned
         if (!okw) { ok = false; break; }
         tc_fence_after();
@@ -643,14 +681,19 @@ __device__ __forceinline__ void gemm_persistent(const Src& src, int* tile_counte
             for (int j = 0; j < 32; j++) prev[j] = (c0 + j < cend) ? __ldcg(crow + (long long)(c0 + j) * g.ldc) : 0;
           }
           uint32_t v0[32], v1[32];
-          tmem_ld32(ta + c0, v0);
-          if (two) tmem_ld32(ta + 256 + c0, v1);
+          tmem_ld32(ta + 256 * buf + c0, v0);
+          if (!FUSED && two) tmem_ld32(ta + 256 + c0, v1);
           tmem_ld_wait();
 #pragma unroll
           for (int j = 0; j < 32; j++) {
             if (c0 + j >= cend) break;
-            int qv = exact_f2i(__uint_as_float(v0[j])) * BASE;
-            if (two) qv += exact_f2i(__uint_as_float(v1[j]));
+            int qv;
+            if constexpr (FUSED) {
+              qv = fused_pair_f2i(__uint_as_float(v0[j]));
+            } else {
+              qv = exact_f2i(__uint_as_float(v0[j])) * BASE;
+              if (two) qv += exact_f2i(__uint_as_float(v1[j]));
+            }
             long long* cp = crow + (long long)(c0 + j) * g.ldc;
             const long long V = (p == 0) ? (long long)qv : prev[j] * (long long)(BASE * BASE) + (long long)qv;
             if (!last)
@@ -662,7 +705,7 @@ __device__ __forceinline__ void gemm_persistent(const Src& src, int* tile_counte
           }
         }
         tc_fence_before();
-        mbar_arrive(tempty);
+        mbar_arrive(&tempty[buf]);
       }
     }
   }
@@ -984,7 +1027,7 @@ __global__ void __launch_bounds__(256) quadtc_combine_kernel(int x, int t, int N
 // sigma_i = 2^aexp[i] >= 2 max_l R2, then S signed base-32 digits of R2 / sigma_i
 // as E4M3 bytes at Ad[(s*Ncap + i)*Kq + l].  Digits from the exact float-pair
 // value: d = rint(hi), (hi, lo) = TwoSum(hi - d, lo), times 32.
-__device__ __forceinline__ uint32_t e4m3_digit(float d) {  // |d| <= 16, an integer: exact
+__device__ __forceinline__ uint32_t e4m3_digit(float d) {  // |d| <= 16 an integer (or one / 32): exact
   return (uint32_t)__nv_cvt_float_to_fp8(d, __NV_SATFINITE, __NV_E4M3);
 }
 constexpr int QD_THREADS = 256;
@@ -1143,8 +1186,8 @@ __global__ void __launch_bounds__(256) slice_rows_kernel(int K, int rows, const 
       const long long at = ((long long)s * Mpad + R) * Kpad + k;
       if constexpr (BF16D)
         ((__nv_bfloat16*)Aout)[at] = __double2bfloat16(d);  // |d| <= 128: exact
-      else
-        ((uint8_t*)Aout)[at] = (uint8_t)e4m3_digit((float)d);  // |d| <= 16: exact
+      else  // |d| <= 16: exact; odd slices hold d / 32, the weight of a fused pair's second slice
+        ((uint8_t*)Aout)[at] = (uint8_t)e4m3_digit((s & 1) ? (float)d * 0.03125f : (float)d);
       v = (v - d) * (double)(1 << LOG_BASE);
     }
   }
@@ -1384,7 +1427,7 @@ struct OzakiPlan {
 cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_b, int slices, int eigen) {
   *out = nullptr;
   if (wXR != 1) return cudaErrorNotSupported;  // split path: one column per SNP
-  if (n > 16383) return cudaErrorNotSupported;  // exactness bound of the FP32 accumulation
+  if (n > FUSED_KMAX) return cudaErrorNotSupported;  // exactness bound of the FP32 accumulation
   OzakiPlan* p = new OzakiPlan();
   p->n = n;
   p->t = t;
@@ -1859,7 +1902,7 @@ extern "C" int fglsgpu_selftest_split_gemm(int M, int K, int N, int S, const dou
                                            double* C) {
   using namespace fgls;
   using namespace fgls::oz;
-  if (M <= 0 || K <= 0 || K > 16383 || N <= 0 || S < 1 || S > MAX_SLICES) return FGLSGPU_EINVAL;
+  if (M <= 0 || K <= 0 || K > FUSED_KMAX || N <= 0 || S < 1 || S > MAX_SLICES) return FGLSGPU_EINVAL;
   OzakiPlan p;
   p.n = K;
   p.S = S;

@@ -87,7 +87,9 @@ typedef struct {
   int slices;    /* split precision: 5-bit digit slices of the FP64 operand, 1..9;
                     0 = autotune: the operand is cut into 9 slices (about 45
                     bits) and a 256-SNP probe block picks the smallest count
-                    in 6..9 whose beta is within 1e-10 / 8 of the FP64 path */
+                    in 6..9 whose beta is within 1e-10 / 8 of the FP64 path.
+                    The split path takes n <= 16368 (exact FP32 accumulation
+                    of a slice pair); larger n fails with FGLSGPU_ECUDA. */
   int device;    /* CUDA device ordinal                          */
   int reserved;
 } fglsgpu_config;
@@ -283,7 +285,7 @@ int fglsgpu_version(void);
 /* Diagnostic: runs the split-precision tensor-core GEMM used by
  * FGLSGPU_PREC_SPLIT on caller data.  C = A * X^T with A M x K (row-major
  * FP64, cut into `slices` 5-bit digit slices, 1..9), X K x N (column-major, integer
- * genotypes 0..2) and C M x N column-major, all host pointers; K <= 16383.
+ * genotypes 0..2) and C M x N column-major, all host pointers; K <= 16368.
  * No counterpart in the reference (its GEMMs are FP64 BLAS calls). */
 int fglsgpu_selftest_split_gemm(int M, int K, int N, int slices, const double *A, const double *X,
                                 double *C);

@@ -51,6 +51,31 @@ def test_split_gemm_exact_at_accumulator_limit():
     assert np.array_equal(C, _exact_product(Aint, 15, X))
 
 
+def test_split_gemm_exact_fused_pair_limit():
+    """A pass accumulates slices 2p and 2p+1 in one FP32 accumulator as
+    P_2p + P_2p+1 / 32.  Digits (15, 15, 15, 15) at K = 16000 with genotypes
+    mostly 2 put that sum near 2^19 with a fractional part in units of 2^-5:
+    all 24 bits of the FP32 significand are used, and the result must still
+    be exact.  Rows mix signs and digit patterns; half the columns take
+    random genotypes so that the fractional parts vary."""
+    from fgls_gb300.engine import split_gemm_selftest
+    K, M, N = 16000, 256, 512
+    rng = np.random.default_rng(3)
+    top = 15 * 2 ** 15 + 15 * 2 ** 10 + 15 * 2 ** 5 + 15      # digits 15, 15, 15, 15 (20 bits)
+    alt = 16 * 2 ** 15 - 1 * 2 ** 10 + 15 * 2 ** 5 - 13       # digits 16, -1, 15, -13
+    Aint = np.where(rng.random((M, K)) < 0.5, -top, top).astype(np.int64)
+    Aint[:64] = top
+    Aint[64:96] = -top
+    Aint[96:128] = alt
+    Aint[128:160] = -alt
+    Aint[:, 0] = np.where(Aint[:, 0] < 0, -alt, alt)  # every row's largest element starts with digit 16
+    X = np.full((K, N), 2)
+    X[:, 1::2] = rng.integers(0, 3, size=(K, N // 2))
+    X[: K // 3, 3::4] = 1
+    C = split_gemm_selftest(np.ldexp(Aint.astype(np.float64), -19), X, 4)
+    assert np.array_equal(C, _exact_product(Aint, 19, X))
+
+
 def test_split_gemm_fp64_accuracy():
     from fgls_gb300.engine import split_gemm_selftest
     rng = np.random.default_rng(7)
