@@ -21,10 +21,10 @@
 //
 // Kernel ozaki_gemm_kernel (persistent: one CTA per SM takes 128 x 256
 // output tiles from a launch-wide counter, 10 warps):
-//   warp 0      TMA producer: per K-step of 64 bytes (64 digits), two A-slice
-//               tiles (128 x 64) and one genotype tile (256 x 64), 64B-swizzled,
-//               six 32 KB stages (the grouped launch: K-steps of 128, 128B
-//               swizzle, three 64 KB stages).
+//   warp 0      TMA producer: per K-step of 128 bytes (128 digits), two
+//               A-slice tiles (128 x 128) and one genotype tile (256 x 128),
+//               128B-swizzled, three 64 KB stages (the grouped launch: 64 BF16
+//               digits, the same bytes).
 //   warp 1      allocates 512 TMEM columns and issues tcgen05.mma
 //               (kind::f8f6f4, E4M3 x E4M3 -> F32, M=128 N=256 K=32): both
 //               slices of pass p into accumulator p % 2 (columns
@@ -76,16 +76,16 @@ namespace oz {
 constexpr int BM = 128, BN = 256, BK = 64;
 constexpr int STAGES = 3;
 constexpr int A_TILE = BM * BK * 2;               // 16 KB
-// split GEMM ring for a K-step of KB one-byte digits (64: 64-byte rows, 64B
-// swizzle, 6 stages of 32 KB; 128: 128-byte rows, 128B swizzle, 3 stages of
-// 64 KB).  The smaller
-// stages keep more bytes in flight per SM for the same shared memory (the MMA
-// thread waits on stage arrivals, not on L2 bandwidth): 10.72 against
-// 11.20 ms per launch at n = 10000, x_b = 16384.  The grouped launch, whose
-// small cohorts have short K, stays at KB = 64 (32.3 against 32.8 ms per
-// step of the 64-cohort batch).
+// Split GEMM ring.  FP8 digits: a K-step of 128 digits, 128-byte rows with
+// 128B swizzle, three 64 KB stages; BF16 digits (grouped launches): 64
+// digits, again 128-byte rows, three 64 KB stages.  64-byte rows (64B
+// swizzle) allow six 32 KB stages in the same shared memory, and so more
+// bytes in flight, but the MMAs read 64B-swizzled operands more slowly: with
+// one accumulator per slice pair and double-buffered TMEM the split GEMM took
+// 8.99 ms per launch with 128-byte rows and 9.17 ms with 64-byte rows (n =
+// 10000, x_b = 16384; five 32 KB stages: 9.61 ms, seven: 9.13 ms).
 #ifndef FGLS_GEMM_BK
-#define FGLS_GEMM_BK 64
+#define FGLS_GEMM_BK 128
 #endif
 #ifndef FGLS_GROUPED_BK
 #define FGLS_GROUPED_BK 64
@@ -193,6 +193,46 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, in
       : "memory");
 }
 
+// 2-SM (cluster of two CTAs) forms.  `bar` below is a shared::cluster
+// address, possibly of the peer CTA's barrier (mapa).
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t cluster_addr(const void* p, uint32_t rank) {  // the same variable in CTA `rank`
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
+  return r;
+}
+// every thread of both CTAs (a superset of __syncthreads)
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait_cluster(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// a copy into this CTA's shared memory that completes on the barrier at
+// cluster address `bar` (the pair leader's)
+__device__ __forceinline__ void tma_load_2d_cg2(void* dst, const CUtensorMap* tm, int x, int y, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+      "[%4];" ::"r"(smem_u32(dst)),
+      "l"((uint64_t)tm), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
 __device__ __forceinline__ uint64_t desc_sw128(const void* p) {
   const uint32_t a = smem_u32(p);
   uint64_t d = 0;
@@ -236,6 +276,24 @@ __device__ __forceinline__ void mma_f8(uint32_t dt, uint64_t ad, uint64_t bd, ui
 }
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+// 2-SM MMA (issued by the pair leader; operands from both CTAs' shared
+// memory at the same offsets, accumulator in both CTAs' TMEM)
+__device__ __forceinline__ void mma_f8_cg2(uint32_t dt, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::2.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}" ::"r"(dt),
+      "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+      : "memory");
+}
+// arrive on the barrier at `bar`'s offset in each CTA of `mask` once the
+// leader's 2-SM MMAs so far have completed
+__device__ __forceinline__ void mma_commit_cg2(uint64_t* bar, uint16_t mask) {
+  asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+                   smem_u32(bar)),
+               "h"(mask)
                : "memory");
 }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
@@ -349,13 +407,18 @@ struct TileRef {
 // Single problem: tile index -> (m_tile, n_tile) in grouped rasterization
 // (GROUP_M row tiles share the column tiles resident in L2); for the
 // triangular L^-1 operand the row order is reversed so that the longest
-// tiles (row tile i has ~i + 1 K-blocks) come first.
+// tiles (row tile i has ~i + 1 K-blocks) come first.  In the 2-SM kernel a
+// tile index names row tiles 2i (rank 0) and 2i + 1 (rank 1) over one
+// column tile; with an odd tiles_m the last pair's second row tile lies past
+// the operand and its rows are never written.
 struct SingleTiles {
   const CUtensorMap* tmA;
   const CUtensorMap* tmB;
   const GemmArgs* g;  // kernel parameter
+  int pair_rank;      // CTA rank in the 2-SM kernel's pair, -1: one CTA per tile
   static constexpr bool global_maps = false;
-  __device__ __forceinline__ int count() const { return g->tiles_m * g->tiles_n; }
+  __device__ __forceinline__ int units_m() const { return pair_rank >= 0 ? (g->tiles_m + 1) >> 1 : g->tiles_m; }
+  __device__ __forceinline__ int count() const { return units_m() * g->tiles_n; }
   // uniform tiles are dealt statically; the triangular L^-1 operand's tiles
   // (row tile i has ~i + 1 K-blocks) from the counter
   __device__ __forceinline__ bool dynamic() const { return g->tri_rows > 0; }
@@ -365,10 +428,12 @@ struct SingleTiles {
   __device__ __forceinline__ const CUtensorMap* mapA(int) const { return tmA; }
   __device__ __forceinline__ const CUtensorMap* mapB(int) const { return tmB; }
   __device__ __forceinline__ TileRef tile(int t) const {
-    const int per_group = GROUP_M * g->tiles_n;
-    const int first_m = (t / per_group) * GROUP_M;
-    const int gsz = min(g->tiles_m - first_m, GROUP_M);
+    const int gm = pair_rank >= 0 ? GROUP_M / 2 : GROUP_M;  // row units (tiles or tile pairs) per group
+    const int per_group = gm * g->tiles_n;
+    const int first_m = (t / per_group) * gm;
+    const int gsz = min(units_m() - first_m, gm);
     int m_tile = first_m + (t % per_group) % gsz;
+    if (pair_rank >= 0) m_tile = 2 * m_tile + pair_rank;
     if (g->tri_rows > 0) m_tile = g->tiles_m - 1 - m_tile;
     return TileRef{0, m_tile, (t % per_group) / gsz, g->N, false};
   }
@@ -397,6 +462,51 @@ struct GroupedTiles {
     return TileRef{tl.prob, tl.m_tile, tl.n_tile, N, tl.n_tile * BN >= N};
   }
 };
+
+// One pass of the split GEMM's epilogue for one thread (one output row,
+// `cend` columns of its half tile from `crow`, stride ldc): read the pass's
+// sums from TMEM 32 columns at a time (FUSED: one accumulator holding
+// P_2p + P_2p+1 / 32 at `tacc`; else P_2p at `tacc` and P_2p+1 at `tacc2`),
+// form the exact int32 q = P_2p * BASE + P_2p+1, and fold it into the int64
+// partial sums in C (V = V * BASE^2 + q), or on the last pass write V times
+// the row scale (FP64, or squared as a float pair for rows `sq`).
+template <bool FUSED, int BASE>
+__device__ __forceinline__ void epilogue_pass(uint32_t tacc, uint32_t tacc2, bool two, int p, bool last, bool sq,
+                                              double scale, float fscale, long long* crow, long long ldc, int cend) {
+#pragma unroll 1
+  for (int ch = 0; ch < BN / 64; ch++) {
+    const int c0 = ch * 32;
+    long long prev[32];
+    if (p > 0) {
+      // all 32 partial sums in flight at once, before the TMEM reads
+#pragma unroll
+      for (int j = 0; j < 32; j++) prev[j] = (c0 + j < cend) ? __ldcg(crow + (long long)(c0 + j) * ldc) : 0;
+    }
+    uint32_t v0[32], v1[32];
+    tmem_ld32(tacc + c0, v0);
+    if (!FUSED && two) tmem_ld32(tacc2 + c0, v1);
+    tmem_ld_wait();
+#pragma unroll
+    for (int j = 0; j < 32; j++) {
+      if (c0 + j >= cend) break;
+      int qv;
+      if constexpr (FUSED) {
+        qv = fused_pair_f2i(__uint_as_float(v0[j]));
+      } else {
+        qv = exact_f2i(__uint_as_float(v0[j])) * BASE;
+        if (two) qv += exact_f2i(__uint_as_float(v1[j]));
+      }
+      long long* cp = crow + (long long)(c0 + j) * ldc;
+      const long long V = (p == 0) ? (long long)qv : prev[j] * (long long)(BASE * BASE) + (long long)qv;
+      if (!last)
+        *cp = V;
+      else if (sq)
+        *(float2*)cp = square_pair(V, fscale);
+      else
+        *(double*)cp = (double)V * scale;
+    }
+  }
+}
 
 // The producer thread of each CTA picks its next tile and publishes the
 // index to the CTA's MMA thread and epilogue warps through a small ring in
@@ -671,39 +781,7 @@ __device__ __forceinline__ void gemm_persistent(const Src& src, int* tile_counte
         okw = __shfl_sync(0xffffffffu, okw, 0);  // warp-uniform: tcgen05.ld is .sync.aligned
         if (!okw) { ok = false; break; }
         tc_fence_after();
-#pragma unroll 1
-        for (int ch = 0; ch < BN / 64; ch++) {
-          const int c0 = ch * 32;
-          long long prev[32];
-          if (p > 0) {
-            // all 32 partial sums in flight at once, before the TMEM reads
-#pragma unroll
-            for (int j = 0; j < 32; j++) prev[j] = (c0 + j < cend) ? __ldcg(crow + (long long)(c0 + j) * g.ldc) : 0;
-          }
-          uint32_t v0[32], v1[32];
-          tmem_ld32(ta + 256 * buf + c0, v0);
-          if (!FUSED && two) tmem_ld32(ta + 256 + c0, v1);
-          tmem_ld_wait();
-#pragma unroll
-          for (int j = 0; j < 32; j++) {
-            if (c0 + j >= cend) break;
-            int qv;
-            if constexpr (FUSED) {
-              qv = fused_pair_f2i(__uint_as_float(v0[j]));
-            } else {
-              qv = exact_f2i(__uint_as_float(v0[j])) * BASE;
-              if (two) qv += exact_f2i(__uint_as_float(v1[j]));
-            }
-            long long* cp = crow + (long long)(c0 + j) * g.ldc;
-            const long long V = (p == 0) ? (long long)qv : prev[j] * (long long)(BASE * BASE) + (long long)qv;
-            if (!last)
-              *cp = V;
-            else if (sq)
-              *(float2*)cp = square_pair(V, fscale);
-            else
-              *(double*)cp = (double)V * scale;
-          }
-        }
+        epilogue_pass<FUSED, BASE>(ta + 256 * buf, ta + 256, two, p, last, sq, scale, fscale, crow, g.ldc, cend);
         tc_fence_before();
         mbar_arrive(&tempty[buf]);
       }
@@ -729,8 +807,309 @@ __device__ __forceinline__ void gemm_persistent(const Src& src, int* tile_counte
 __global__ void __launch_bounds__(THREADS, 1)
     ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                       const __grid_constant__ GemmArgs g, int* tile_counter) {
-  const SingleTiles src{&tmA, &tmB, &g};
+  const SingleTiles src{&tmA, &tmB, &g, -1};
   gemm_persistent<GBK, 1>(src, tile_counter);
+}
+
+// ---------------------------------------------------------------------------
+// 2-SM split GEMM (FP8 digits, uniform tiles): a cluster of two CTAs on two
+// SMs computes 256 x 256 output tiles with tcgen05.mma.cta_group::2 (M =
+// 256, N = 256, K = 32).  CTA rank r holds rows 128 r .. 128 r + 127 of the
+// tile (its A-slice tiles in shared memory, its accumulators in TMEM) and
+// genotype rows 128 r .. 128 r + 127; the MMAs, issued by rank 0 (the
+// leader), read both CTAs' shared memory and write both CTAs' TMEM.  Each
+// CTA's shared memory thus holds half of the genotype tile where the one-SM
+// kernel holds all of it: a 48 KB stage (two 128 x 128 A-slice tiles and a
+// 128 x 128 genotype half, 128-byte K rows, 128B swizzle) carries the
+// operands of eight 128 x 256 x 32 MMAs per SM, against 64 KB in the one-SM
+// kernel, so four stages fit and a quarter fewer operand bytes move per MMA.
+//
+// Barriers: full[s] lives in the leader only (both CTAs' copies complete on
+// it; the leader arms it with both CTAs' bytes); empty[s] and tfull[b] live
+// in both CTAs and are released by the leader's multicast commits;
+// tempty[b] lives in the leader and counts one arrival per epilogue warp of
+// both CTAs.  Tiles are dealt statically per pair, so both CTAs know the
+// sequence without exchanging it; each CTA's producer still publishes it to
+// its own MMA thread (leader only) and epilogue warps.  Every wait is bounded.
+namespace p2 {
+constexpr int ROW = 128;            // bytes (FP8 digits) per K-step row
+constexpr int A = BM * ROW;         // 16 KB: one A-slice tile of this CTA
+constexpr int B = (BN / 2) * ROW;   // 16 KB: this CTA's half of the genotype tile
+constexpr int STAGE = 2 * A + B;    // 48 KB
+constexpr int STAGES = 4;
+constexpr int SMEM = STAGES * STAGE + 1024 + 256;
+// kind::f8f6f4: D=F32, A=B=E4M3, K-major, N=256, M=256 (the pair)
+constexpr uint32_t IDESC = (1u << 4) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
+constexpr int EPI_WARPS = 8;
+}  // namespace p2
+
+__device__ __forceinline__ void gemm_pair(const SingleTiles& src) {
+  constexpr int ROW = p2::ROW, A = p2::A, B = p2::B, STAGE = p2::STAGE, STAGES = p2::STAGES;
+  constexpr int EPI_WARPS = p2::EPI_WARPS;
+  constexpr uint32_t IDESC = p2::IDESC;
+  constexpr int BASE = 32;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + STAGES * STAGE);  // [STAGES], used in the leader
+  uint64_t* empty = full + STAGES;                       // [STAGES]
+  uint64_t* tfull = empty + STAGES;                      // [2]
+  uint64_t* tempty = tfull + 2;                          // [2], used in the leader
+  uint64_t* drain = tempty + 2;
+  uint64_t* tq_full = drain + 1;
+  uint64_t* tq_empty = tq_full + TQ;
+  volatile int* tq_id = (volatile int*)(tq_empty + TQ);
+  uint32_t* tbase_slot = (uint32_t*)(tq_id + TQ);
+  volatile int* abort_flag = (volatile int*)(tbase_slot + 1);
+  static_assert((STAGES * 2 + 5 + 2 * TQ) * 8 + TQ * 4 + 8 <= 256, "barriers fit the 256-byte tail");
+
+  const GemmArgs& g = *src.g;
+  const uint32_t rank = (uint32_t)src.pair_rank;
+  const bool lead = rank == 0;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ntiles = src.count();
+  const uint16_t BOTH = 0x3;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; b++) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], 2 * EPI_WARPS);
+    }
+    mbar_init(drain, 1);
+    for (int s = 0; s < TQ; s++) {
+      mbar_init(&tq_full[s], 1);
+      mbar_init(&tq_empty[s], lead ? 1 + EPI_WARPS : EPI_WARPS);  // the peer has no MMA thread
+    }
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {  // one warp of each CTA allocates the same columns in both
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tbase_slot)),
+                 "r"(512)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  cluster_sync();  // both CTAs' barriers are initialised before either signals the other's
+  tc_fence_after();
+  const uint32_t tbase = *tbase_slot;
+  const int deal_id = (int)(blockIdx.x >> 1), deal_n = (int)(gridDim.x >> 1);
+  const uint32_t lead_full = cluster_addr(full, 0);  // leader's full[0]; full[s] is 8 s bytes further
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      int issued[STAGES];
+      uint32_t issued_phase[STAGES];
+      for (int s = 0; s < STAGES; s++) issued[s] = 0;
+      bool ok = true;
+      int tq = 0;
+      uint32_t tqph = 0;
+      int kdeal = 0;
+#pragma unroll 1
+      while (ok) {
+        const int base = kdeal * deal_n;
+        int it = base >= ntiles ? ntiles : base + ((kdeal & 1) ? deal_n - 1 - deal_id : deal_id);
+        kdeal++;
+        if (it >= ntiles) it = -1;
+        if (!mbar_wait(&tq_empty[tq], tqph ^ 1, abort_flag, g.err, 5, g.wait_ns)) { ok = false; break; }
+        tq_id[tq] = it;
+        mbar_arrive(&tq_full[tq]);
+        if (++tq == TQ) { tq = 0; tqph ^= 1; }
+        if (it < 0) break;
+        const TileRef T = src.tile(it);
+        const int m0 = T.m_tile * BM, n0 = T.n_tile * BN;
+        const int passes = (g.S + 1) / 2;
+        const int nk = g.Kpad / ROW;
+#pragma unroll 1
+        for (int p = 0; p < passes && ok; p++) {
+          const int s0 = 2 * p, s1 = 2 * p + 1;
+          const bool two = s1 < g.S;
+#pragma unroll 1
+          for (int kb = 0; kb < nk; kb++) {
+            if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, g.err, 1, g.wait_ns)) { ok = false; break; }
+            issued[stage] = 0;
+            uint8_t* sb = smem + stage * STAGE;
+            const uint32_t fb = lead_full + 8u * (uint32_t)stage;
+            if (lead) mbar_expect_tx(&full[stage], 2 * ((two ? 2 * A : A) + B));  // both CTAs' bytes
+            tma_load_2d_cg2(sb, src.tmA, kb * ROW, s0 * g.Mpad + m0, fb);
+            if (two) tma_load_2d_cg2(sb + A, src.tmA, kb * ROW, s1 * g.Mpad + m0, fb);
+            tma_load_2d_cg2(sb + 2 * A, src.tmB, kb * ROW, g.col0 + n0 + (int)rank * (BN / 2), fb);
+            issued[stage] = 1;
+            issued_phase[stage] = phase;
+            if (++stage == STAGES) { stage = 0; phase ^= 1; }
+          }
+        }
+      }
+      if (ok) {
+        // every stage filled so far has been released by the leader's MMAs:
+        // no multicast commit is still on its way to this CTA
+#pragma unroll 1
+        for (int i = 0; i < STAGES; i++) {
+          if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, g.err, 8, g.wait_ns)) break;
+          if (++stage == STAGES) { stage = 0; phase ^= 1; }
+        }
+      } else if (lead) {
+        // the leader's barrier tracks both CTAs' copies of every stage it armed
+        for (int s = 0; s < STAGES; s++)
+          if (issued[s]) mbar_drain(&full[s], issued_phase[s]);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0 && lead) {
+      int stage = 0;
+      uint32_t phase = 0, q = 0;
+      bool ok = true;
+      bool any = false;
+      int tq = 0;
+      uint32_t tqph = 0;
+#pragma unroll 1
+      while (ok) {
+        if (!mbar_wait(&tq_full[tq], tqph, abort_flag, g.err, 6, g.wait_ns)) { ok = false; break; }
+        const int it = tq_id[tq];
+        mbar_arrive(&tq_empty[tq]);
+        if (++tq == TQ) { tq = 0; tqph ^= 1; }
+        if (it < 0) break;
+        const int passes = (g.S + 1) / 2;
+        const int nk = g.Kpad / ROW;
+#pragma unroll 1
+        for (int p = 0; p < passes && ok; p++, q++) {
+          const bool two = 2 * p + 1 < g.S;
+          const uint32_t buf = q & 1, par = (q >> 1) & 1;
+          // both CTAs' epilogues have drained this accumulator half
+          {
+            const uint64_t t0 = globaltimer_ns();
+            uint32_t spin = 0;
+            while (!mbar_try_wait_cluster(&tempty[buf], par ^ 1)) {
+              if ((++spin & 63) == 0 &&
+                  (*abort_flag || *(volatile int*)g.err || globaltimer_ns() - t0 > g.wait_ns)) {
+                *abort_flag = 1;
+                atomicCAS(g.err, 0, 2);
+                ok = false;
+                break;
+              }
+            }
+            if (!ok) break;
+          }
+          tc_fence_after();
+          const uint32_t acc = tbase + 256 * buf;
+#pragma unroll 1
+          for (int kb = 0; kb < nk; kb++) {
+            if (!mbar_wait(&full[stage], phase, abort_flag, g.err, 3, g.wait_ns)) { ok = false; break; }
+            tc_fence_after();
+            uint8_t* sb = smem + stage * STAGE;
+            const uint64_t a0 = desc_sw128(sb), a1 = desc_sw128(sb + A), b = desc_sw128(sb + 2 * A);
+#pragma unroll
+            for (int kk = 0; kk < ROW / 32; kk++) {  // 32 FP8 digits per MMA
+              const uint64_t koff = (uint64_t)((kk * 32) >> 4);
+              mma_f8_cg2(acc, a0 + koff, b + koff, IDESC, (kb > 0 || kk > 0) ? 1u : 0u);
+              if (two) mma_f8_cg2(acc, a1 + koff, b + koff, IDESC, 1u);  // adds to slice 2p's sum
+            }
+            any = true;
+            mma_commit_cg2(&empty[stage], BOTH);  // the stage is free in both CTAs
+            if (++stage == STAGES) { stage = 0; phase ^= 1; }
+          }
+          if (!ok) break;
+          mma_commit_cg2(&tfull[buf], BOTH);
+        }
+      }
+      if (!ok && any) {
+        // all MMAs issued by this thread complete before TMEM is released
+        mma_commit_cg2(drain, 0x1);
+        mbar_drain(drain, 0);
+      }
+    }
+    __syncwarp();
+  } else {
+    // epilogue: warps 2..9 of each CTA drain that CTA's 128 rows, as in the
+    // one-SM kernel; one arrival per warp on the leader's tempty
+    const int lq = warp & 3;
+    const int cbeg = ((warp - 2) >> 2) * (BN / 2);
+    const int row = lq * 32 + lane;
+    const uint32_t ta = tbase + ((uint32_t)(lq * 32) << 16) + (uint32_t)cbeg;
+    const uint32_t lead_tempty = cluster_addr(tempty, 0);
+    uint32_t q = 0;
+    bool ok = true;
+    int tq = 0;
+    uint32_t tqph = 0;
+#pragma unroll 1
+    while (ok) {
+      int it = 0, okq = 1;
+      if (lane == 0) {
+        okq = mbar_wait(&tq_full[tq], tqph, abort_flag, g.err, 7, g.wait_ns) ? 1 : 0;
+        if (okq) {
+          it = tq_id[tq];
+          mbar_arrive(&tq_empty[tq]);
+        }
+      }
+      okq = __shfl_sync(0xffffffffu, okq, 0);
+      it = __shfl_sync(0xffffffffu, it, 0);
+      if (!okq) { ok = false; break; }
+      if (++tq == TQ) { tq = 0; tqph ^= 1; }
+      if (it < 0) break;
+      const TileRef T = src.tile(it);
+      const int m0 = T.m_tile * BM, n0 = T.n_tile * BN;
+      const int r = m0 + row;
+      const bool rvalid = r < g.M;
+      const double scale = rvalid ? g.row_scale[r] : 0.0;
+      const bool sq = r < g.sq_rows;
+      const float fscale = (float)scale;
+      const int ncols = rvalid ? min(BN, T.N - n0) : 0;
+      const int cend = min(BN / 2, ncols - cbeg);
+      long long* crow = (long long*)(g.C + (long long)r + (long long)(g.col0 + n0 + cbeg) * g.ldc);
+      const int passes = (g.S + 1) / 2;
+#pragma unroll 1
+      for (int p = 0; p < passes; p++, q++) {
+        const bool two = 2 * p + 1 < g.S;
+        const bool last = p == passes - 1;
+        const uint32_t buf = q & 1, par = (q >> 1) & 1;
+        if (p > 0)
+          for (int c = 0; c < cend; c++)
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(crow + (long long)c * g.ldc));
+        int okw = 1;
+        if (lane == 0) okw = mbar_wait(&tfull[buf], par, abort_flag, g.err, 4, g.wait_ns) ? 1 : 0;
+        okw = __shfl_sync(0xffffffffu, okw, 0);
+        if (!okw) { ok = false; break; }
+        tc_fence_after();
+        epilogue_pass<true, BASE>(ta + 256 * buf, 0, two, p, last, sq, scale, fscale, crow, g.ldc, cend);
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive_cluster(lead_tempty + 8u * buf);
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  // the leader's MMAs, which write both CTAs' TMEM, are complete (its MMA
+  // thread drained or its epilogue consumed every pass) before either CTA
+  // releases TMEM
+  cluster_sync();
+  tc_fence_after();
+  if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(512) : "memory");
+  // neither CTA exits while the other may still signal its barriers or
+  // copy into its shared memory.  After an expired wait the peer's copies of
+  // a stage the leader never armed cannot be observed; both producers have
+  // stopped issuing once both CTAs pass the cluster barrier, so a short
+  // pause lets such copies land before the shared memory is released.
+  cluster_sync();
+  if (*abort_flag) {
+    const uint64_t t0 = globaltimer_ns();
+    while (globaltimer_ns() - t0 < 100000ull) {
+    }
+  }
+}
+
+// 2-SM launch: clusters of two CTAs, one pair of SMs per cluster, at most as
+// many clusters as fit at once (tiles are dealt statically per cluster).
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
+    ozaki_gemm2_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmBh,
+                       const __grid_constant__ GemmArgs g) {
+  const SingleTiles src{&tmA, &tmBh, &g, (int)cluster_rank()};
+  gemm_pair(src);
 }
 
 // Many independent problems in one persistent launch over a tile table;
@@ -1382,6 +1761,29 @@ int persistent_grid(int tiles) {
   return std::max(1, std::min(tiles, sms));
 }
 
+// Clusters of the 2-SM split GEMM (two CTAs, one per SM) that the current
+// device holds at once, queried once per device; 0 if none can launch.
+int pair_clusters() {
+  static std::atomic<int> known[64];  // clusters + 1; 0: not queried yet
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+  const int v = known[dev].load(std::memory_order_relaxed);
+  if (v > 0) return v - 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(2);
+  cfg.blockDim = dim3(THREADS);
+  cfg.dynamicSmemBytes = p2::SMEM;
+  int n = 0;
+  if (cudaFuncSetAttribute(ozaki_gemm2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, p2::SMEM) !=
+          cudaSuccess ||
+      cudaOccupancyMaxActiveClusters(&n, (void*)ozaki_gemm2_kernel, &cfg) != cudaSuccess) {
+    (void)cudaGetLastError();
+    n = 0;
+  }
+  known[dev].store(n + 1, std::memory_order_relaxed);
+  return n;
+}
+
 }  // namespace oz
 
 using namespace oz;
@@ -1417,6 +1819,8 @@ struct OzakiPlan {
   double* LinvT = nullptr;      // chol: n x n, (L^-1)^T (rows of L^-1 contiguous)
   int* err = nullptr;
   CUtensorMap mapA, mapB;
+  CUtensorMap mapBh;                // genotypes in 128-row boxes (2-SM kernel); valid when has_mapBh
+  bool has_mapBh = false;
   bool maps = false;
   int sub = 0;                      // SNPs per pipelined sub-block (multiple of BN)
   int S_run = 0;                    // slices the GEMM uses: the first S_run of the S built
@@ -1470,6 +1874,8 @@ cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_
   if (r == cudaSuccess) chk(cudaMemset(p->err, 0, 3 * sizeof(int)));
   if (r == cudaSuccess) chk(make_map(&p->mapA, p->A, p->Kpad, (long long)p->S * p->Mpad, BM));
   if (r == cudaSuccess) chk(make_map(&p->mapB, p->G, p->Kpad, p->Ncap, BN));
+  if (r == cudaSuccess) chk(make_map(&p->mapBh, p->G, p->Kpad, p->Ncap, BN / 2));
+  if (r == cudaSuccess) p->has_mapBh = true;
   if (r == cudaSuccess) chk(cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                  SMEM_BYTES));
   p->sub = p->Ncap;  // one GEMM launch per block
@@ -1557,8 +1963,16 @@ cudaError_t run_gemm(OzakiPlan* p, cudaStream_t s, int col0, int x, int tri_rows
   g.ldc = p->Mpad;
   g.err = p->err;
   g.wait_ns = p->wait_ns;
-  ozaki_gemm_kernel<<<persistent_grid(g.tiles_m * g.tiles_n), THREADS, SMEM_BYTES, s>>>(p->mapA, p->mapB, g,
-                                                                                        p->err + 1);
+  // uniform tiles: the 2-SM kernel (pairs of row tiles share each genotype
+  // tile across two SMs); the triangular L^-1 operand: one CTA per tile,
+  // longest tiles first from the counter
+  const int pairs = ((g.tiles_m + 1) / 2) * g.tiles_n;
+  const int clusters = (tri_rows == 0 && p->has_mapBh) ? pair_clusters() : 0;
+  if (clusters > 0)
+    ozaki_gemm2_kernel<<<2 * std::min(pairs, clusters), THREADS, p2::SMEM, s>>>(p->mapA, p->mapBh, g);
+  else
+    ozaki_gemm_kernel<<<persistent_grid(g.tiles_m * g.tiles_n), THREADS, SMEM_BYTES, s>>>(p->mapA, p->mapB, g,
+                                                                                          p->err + 1);
   note_launch();
   return cudaGetLastError();
 }
@@ -1933,6 +2347,8 @@ extern "C" int fglsgpu_selftest_split_gemm(int M, int K, int N, int S, const dou
   if (r == cudaSuccess) chk(cudaMemcpy(dX, X, sizeof(double) * (size_t)K * N, cudaMemcpyHostToDevice));
   if (r == cudaSuccess) chk(make_map(&p.mapA, p.A, p.Kpad, (long long)S * p.Mpad, BM));
   if (r == cudaSuccess) chk(make_map(&p.mapB, p.G, p.Kpad, p.Ncap, BN));
+  if (r == cudaSuccess) chk(make_map(&p.mapBh, p.G, p.Kpad, p.Ncap, BN / 2));
+  if (r == cudaSuccess) p.has_mapBh = true;
   if (r == cudaSuccess)
     chk(cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
   if (r == cudaSuccess) {
