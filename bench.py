@@ -182,6 +182,11 @@ def aggregate_throughput(world, blocks_per_rank, snps_per_block, traits, seconds
     return world * blocks_per_rank * snps_per_block * traits / seconds
 
 
+# GB300's nominal dense FP8 tensor rate, for context beside the measured-peak
+# fraction (the measured denominator is twice a cuBLAS BF16 GEMM's rate).
+NOMINAL_FP8_TFLOPS = 4500.0
+
+
 def gemm_traffic(n, t, xb):
     """DRAM bytes (read + write) of one split-GEMM launch of this workload, from
     the committed ncu summary profiles/ozaki_gemm_n{n}_t{t}_xb{xb}.txt (its
@@ -1121,9 +1126,11 @@ def run_eigen(args, rank, world, local, dist):
         },
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes": algo_bytes,
-                     "kernel": "ozaki_gemm_kernel",
+                     "kernel": "ozaki_gemm2_kernel (2-SM CTA pairs, tcgen05.mma.cta_group::2)",
                      "peak_source": f"2 x {pk_kind} {pk_key} (FP8 dense rate = 2 x BF16; "
                                     f"timed region {timed_s:.2f} s)",
+                     "nominal_fp8_tflops": NOMINAL_FP8_TFLOPS,
+                     "frac_of_nominal": achieved / NOMINAL_FP8_TFLOPS,
                      "fp64_equivalent_tflops": 2.0 * M_A * n * xb * args.steps / gemm_s / 1e12,
                      "work": f"2*{S_used} slices*{M_A} rows*{n} K per SNP; {gemm_n} launches, "
                              f"{gemm_ms / max(gemm_n, 1):.3f} ms each"},
