@@ -6,10 +6,10 @@
 // (src/fgls_chol.c:251-262), L = chol(M), the null model of
 // [y~ | XL~] = L^-1 [y | XL] (src/fgls_chol.c:273-325), L^-1 by trailing
 // panel TRSMs, and the split operand [L^-1 ; (L^-T [y~ | XL~])^T] cut into
-// BF16 digit slices, resident in HBM for the whole job.
+// FP8 (E4M3) five-bit digit slices, resident in HBM for the whole job.
 //
 // Per step (one launch each, whatever the number of cohorts):
-//   1. grouped_genotypes: every cohort's block -> its BF16 operand
+//   1. grouped_genotypes: every cohort's block -> its E4M3 operand
 //   2. ozaki_grouped_gemm_kernel: one persistent launch (a CTA per SM) over
 //      the tiles of all problems, listed longest first and taken from a
 //      launch-wide counter -> X~ = L^-1 X (R^2 as float pairs) and the Gram
@@ -22,7 +22,7 @@
 // (two graphs alternate between two pinned tables).
 //
 // Autotuning at creation (fglsgpu_batch_config x_b = 0 and/or slices = 0):
-//   slices: the smallest S in 3..6 whose beta on a probe block (hashed
+//   slices: the smallest S in 5..9 whose beta on a probe block (hashed
 //           genotypes) is within tol/8 of the FP64 path (TRSM, skinny Gram,
 //           solve) for every problem;
 //   x_b:    the candidate SNP block (1024 .. 8192) with the highest measured
@@ -49,22 +49,23 @@ using namespace fgls;
 
 namespace {
 
-constexpr int S_BUILT = 6;     // BF16 eight-bit digit slices cut at setup; fewer may be used
+constexpr int S_BUILT = 9;     // FP8 five-bit digit slices cut at setup; fewer may be used
+constexpr int S_MIN_TUNE = 5;  // smallest slice count the autotuner tries
 constexpr int PROBE = 256;     // SNPs of the autotuning probe block
 constexpr int XB_MAX = 8192;   // largest autotuned SNP block
 
 struct Cohort {
   int n = 0, wXL = 0, p = 0, t = 0;
   int Kpad = 0, Ncap = 0;
-  __nv_bfloat16* G = nullptr;     // BF16 genotype operand (Ncap x Kpad)
+  uint8_t* G = nullptr;           // E4M3 genotype operand (Ncap x Kpad)
   unsigned char* probe = nullptr; // PROBE x n hashed genotypes
 };
 
 struct Problem {
   int c = 0, j = 0;
   int M = 0, Mpad = 0;
-  __nv_bfloat16* A = nullptr;  // S_BUILT x Mpad x Kpad BF16 digit slices
-  double* scale6 = nullptr;    // row scales of the S_BUILT-slice cut
+  uint8_t* A = nullptr;        // S_BUILT x Mpad x Kpad E4M3 digit slices
+  double* scale_built = nullptr;  // row scales of the S_BUILT-slice cut
   double* scale = nullptr;     // row scales for the slices in use
   double* top = nullptr;       // null model (wXL + wXL^2 + 1)
   double* C = nullptr;         // Mpad x Ncap split GEMM output
@@ -177,7 +178,7 @@ void free_batch(fglsgpu_batch* b) {
     if (c.probe) cudaFree(c.probe);
   }
   for (auto& q : b->pr) {
-    void* ptrs[] = {q.A, q.scale6, q.scale, q.top, q.C, q.GR, q.ref};
+    void* ptrs[] = {q.A, q.scale_built, q.scale, q.top, q.C, q.GR, q.ref};
     for (void* v : ptrs)
       if (v) cudaFree(v);
   }
@@ -202,7 +203,7 @@ int configure(fglsgpu_batch* b, int S, int x_b) {
   for (size_t k = 0; k < b->pr.size(); k++) {
     Problem& q = b->pr[k];
     const Cohort& c = b->co[q.c];
-    B_TRY(b, split_rescale_rows(b->s, q.Mpad, q.scale6, S_BUILT, S, q.scale), "row scales");
+    B_TRY(b, split_rescale_rows(b->s, q.Mpad, q.scale_built, S_BUILT, S, q.scale), "row scales");
     d[k] = GroupedGemmDesc{q.A, S, S_BUILT, q.M, q.Mpad, c.Kpad, c.n, c.n, q.scale, c.G, c.Ncap, q.C, q.c};
   }
   B_TRY(b, cudaStreamSynchronize(b->s), "row scales");
@@ -457,7 +458,7 @@ cudaError_t setup_problem(fglsgpu_batch* b, Scratch& w, const CohortInputs& ci, 
   FGLS_CUDA_TRY(cudaMemcpyAsync(w.WY + n, ci.XL, sizeof(double) * n * wXL, cudaMemcpyDeviceToDevice, s));
   FGLS_CUDA_TRY(dtrsm_llnn(s, n, 1 + wXL, w.L, n, w.WY, n));
   FGLS_CUDA_TRY(null_model_chol(s, n, wXL, w.WY, q.top, w.st, 0));
-  FGLS_CUDA_TRY(split_chol_operand(s, n, wXL, w.L, w.WY, S_BUILT, q.Mpad, c.Kpad, q.A, q.scale6, w.Linv, w.LinvT,
+  FGLS_CUDA_TRY(split_chol_operand(s, n, wXL, w.L, w.WY, S_BUILT, q.Mpad, c.Kpad, q.A, q.scale_built, w.Linv, w.LinvT,
                                    w.U));
   // FP64 path on the probe block (the reference's chol per-block loop)
   FGLS_CUDA_TRY(dtrsm_llnn(s, n, PROBE, w.L, n, w.X64, n));
@@ -480,9 +481,9 @@ int fglsgpu_batch_create(const fglsgpu_cohort* cohorts, int count, const fglsgpu
     return bfail(nullptr, FGLSGPU_EINVAL, "invalid batch config x_b=%d slices=%d", cfg->x_b, cfg->slices);
   for (int c = 0; c < count; c++) {
     const fglsgpu_cohort& k = cohorts[c];
-    if (k.n < 2 || k.n > 16383 || k.wXL < 1 || k.wXL + 1 > FGLS_MAX_P || k.t < 1 || !k.Phi || !k.XL || !k.Y || !k.h ||
+    if (k.n < 2 || k.n > 16368 || k.wXL < 1 || k.wXL + 1 > FGLS_MAX_P || k.t < 1 || !k.Phi || !k.XL || !k.Y || !k.h ||
         !k.sigma)
-      return bfail(nullptr, FGLSGPU_EINVAL, "cohort %d: invalid (n=%d wXL=%d t=%d; n <= 16383, wXL+1 <= %d)", c, k.n,
+      return bfail(nullptr, FGLSGPU_EINVAL, "cohort %d: invalid (n=%d wXL=%d t=%d; n <= 16368, wXL+1 <= %d)", c, k.n,
                    k.wXL, k.t, FGLS_MAX_P);
   }
   int ndev = 0;
@@ -533,7 +534,7 @@ int fglsgpu_batch_create(const fglsgpu_cohort* cohorts, int count, const fglsgpu
     nmax = std::max(nmax, k.n);
     wmax = std::max(wmax, k.wXL);
     B_CHECK(dalloc(&k.G, (size_t)k.Ncap * k.Kpad), "genotype operand");
-    B_CHECK(cudaMemset(k.G, 0, sizeof(__nv_bfloat16) * (size_t)k.Ncap * k.Kpad), "genotype operand");
+    B_CHECK(cudaMemset(k.G, 0, (size_t)k.Ncap * k.Kpad), "genotype operand");
     B_CHECK(dalloc(&k.probe, (size_t)PROBE * k.n), "probe block");
     for (int j = 0; j < k.t; j++) {
       Problem q;
@@ -547,9 +548,9 @@ int fglsgpu_batch_create(const fglsgpu_cohort* cohorts, int count, const fglsgpu
   for (auto& q : b->pr) {
     const Cohort& k = b->co[q.c];
     B_CHECK(dalloc(&q.A, (size_t)S_BUILT * q.Mpad * k.Kpad), "split operand");
-    B_CHECK(cudaMemset(q.A, 0, sizeof(__nv_bfloat16) * (size_t)S_BUILT * q.Mpad * k.Kpad), "split operand");
-    B_CHECK(dalloc(&q.scale6, q.Mpad), "row scales");
-    B_CHECK(cudaMemset(q.scale6, 0, sizeof(double) * q.Mpad), "row scales");
+    B_CHECK(cudaMemset(q.A, 0, (size_t)S_BUILT * q.Mpad * k.Kpad), "split operand");
+    B_CHECK(dalloc(&q.scale_built, q.Mpad), "row scales");
+    B_CHECK(cudaMemset(q.scale_built, 0, sizeof(double) * q.Mpad), "row scales");
     B_CHECK(dalloc(&q.scale, q.Mpad), "row scales");
     B_CHECK(dalloc(&q.top, k.wXL + k.wXL * k.wXL + 1), "null model");
     B_CHECK(dalloc(&q.C, (size_t)q.Mpad * b->ncap), "split GEMM output");
@@ -668,7 +669,7 @@ int fglsgpu_batch_create(const fglsgpu_cohort* cohorts, int count, const fglsgpu
   int S = cfg->slices;
   if (S == 0) {
     S = S_BUILT;
-    for (int cand = 3; cand <= S_BUILT; cand++) {
+    for (int cand = S_MIN_TUNE; cand <= S_BUILT; cand++) {
       double e = 0.0;
       rc = probe_error(b, cand, &e);
       if (rc) {

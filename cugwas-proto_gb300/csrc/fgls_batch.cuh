@@ -16,9 +16,9 @@ struct StepCohort {
   int pad;
 };
 
-// Per cohort, fixed: BF16 genotype operand of the split GEMM.
+// Per cohort, fixed: E4M3 genotype operand of the split GEMM.
 struct GenoCohort {
-  __nv_bfloat16* G;  // Ncap x Kpad, column c at G + c*Kpad
+  uint8_t* G;  // E4M3 genotypes, Ncap x Kpad, column c at G + c*Kpad
   int n, Kpad;
 };
 

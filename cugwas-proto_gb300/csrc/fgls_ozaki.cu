@@ -17,14 +17,14 @@
 // partial sum are multiples of 2^-5 below 2^19, representable in FP32, and
 // the accumulation is exact and bit-reproducible.  The kind::f8f6f4 MMA runs
 // at twice the BF16 rate: 9 five-bit slices (45 bits) cost 4.5 BF16
-// slice-equivalents where 6 eight-bit BF16 slices (48 bits) cost 6.
+// slice-equivalents where 6 eight-bit BF16 slices (48 bits) would cost 6
+// (and eight-bit digits would need 29 bits for a fused pair).
 //
 // Kernel ozaki_gemm_kernel (persistent: one CTA per SM takes 128 x 256
 // output tiles from a launch-wide counter, 10 warps):
 //   warp 0      TMA producer: per K-step of 128 bytes (128 digits), two
 //               A-slice tiles (128 x 128) and one genotype tile (256 x 128),
-//               128B-swizzled, three 64 KB stages (the grouped launch: 64 BF16
-//               digits, the same bytes).
+//               128B-swizzled, three 64 KB stages.
 //   warp 1      allocates 512 TMEM columns and issues tcgen05.mma
 //               (kind::f8f6f4, E4M3 x E4M3 -> F32, M=128 N=256 K=32): both
 //               slices of pass p into accumulator p % 2 (columns
@@ -35,9 +35,6 @@
 //               Horner-accumulate the passes in int64 in the output buffer
 //               (V = V * 2^10 + q), and on the last pass write
 //               V * 2^(e_r - 9 - 10 (passes-1)) as FP64.  |V| < 2^62 for S <= 9.
-// (The grouped launch's BF16 eight-bit digits would need 29 bits for a fused
-// pair: it accumulates slice 2p into columns [0,256) and 2p+1 into
-// [256,512) and combines them in the epilogue.)
 // Every mbarrier wait is bounded; on expiry the kernel raises an error flag,
 // drains its own in-flight copies and MMAs (bounded), frees TMEM and exits.
 //
@@ -73,43 +70,26 @@ namespace fgls {
 
 namespace oz {
 
-constexpr int BM = 128, BN = 256, BK = 64;
-constexpr int STAGES = 3;
-constexpr int A_TILE = BM * BK * 2;               // 16 KB
-// Split GEMM ring.  FP8 digits: a K-step of 128 digits, 128-byte rows with
-// 128B swizzle, three 64 KB stages; BF16 digits (grouped launches): 64
-// digits, again 128-byte rows, three 64 KB stages.  64-byte rows (64B
-// swizzle) allow six 32 KB stages in the same shared memory, and so more
-// bytes in flight, but the MMAs read 64B-swizzled operands more slowly: with
-// one accumulator per slice pair and double-buffered TMEM the split GEMM took
-// 8.99 ms per launch with 128-byte rows and 9.17 ms with 64-byte rows (n =
-// 10000, x_b = 16384; five 32 KB stages: 9.61 ms, seven: 9.13 ms).
-#ifndef FGLS_GEMM_BK
-#define FGLS_GEMM_BK 128
-#endif
-#ifndef FGLS_GROUPED_BK
-#define FGLS_GROUPED_BK 64
-#endif
-#ifndef FGLS_GEMM_STAGES64
-#define FGLS_GEMM_STAGES64 6
-#endif
-// Operand formats: FP8 E4M3 five-bit digits (single-problem launches) or
-// BF16 eight-bit digits (grouped launches, whose short-K tiles favour three
-// slice-pair passes over five).  KB counts digits per K-step, ESZ their bytes.
-template <int KB, int ESZ>
+constexpr int BM = 128, BN = 256;
+constexpr int A_TILE = BM * 128;  // 16 KB: 128 rows of 128 bytes
+// Split GEMM ring (one-SM kernel): a K-step of 128 FP8 digits, 128-byte
+// rows with 128B swizzle, three 64 KB stages of two A-slice tiles and one
+// genotype tile.  64-byte rows (64B swizzle) allow six 32 KB stages in the
+// same shared memory, and so more bytes in flight, but the MMAs read
+// 64B-swizzled operands more slowly: with one accumulator per slice pair and
+// double-buffered TMEM the split GEMM took 8.99 ms per launch with 128-byte
+// rows and 9.17 ms with 64-byte rows (n = 10000, x_b = 16384; five 32 KB
+// stages: 9.61 ms, seven: 9.13 ms).
 struct GemmRing {
-  static constexpr int ROW = KB * ESZ;  // bytes of one K-step row
-  static_assert(ROW == 128 || ROW == 64, "K-step of the split GEMM");
-  static constexpr int STAGES = ROW == 128 ? 3 : FGLS_GEMM_STAGES64;
+  static constexpr int ROW = 128;  // bytes (FP8 digits) of one K-step row
+  static constexpr int STAGES = 3;
   static constexpr int A = BM * ROW;
   static constexpr int B = BN * ROW;
   static constexpr int STAGE = 2 * A + B;
   static constexpr int SMEM = STAGES * STAGE + 1024 + 256;
 };
-constexpr int GBK = FGLS_GEMM_BK;         // single-problem launch
-constexpr int GRBK = FGLS_GROUPED_BK;     // grouped launch
-constexpr int SMEM_BYTES = GemmRing<GBK, 1>::SMEM;          // FP8 digits
-constexpr int GROUPED_SMEM_BYTES = GemmRing<GRBK, 2>::SMEM;  // BF16 digits
+constexpr int GBK = GemmRing::ROW;  // digits per K-step (the tensor maps' box)
+constexpr int SMEM_BYTES = GemmRing::SMEM;
 constexpr int THREADS = 320;  // producer, MMA, 8 epilogue warps
 constexpr int MAX_SLICES = 9;   // FP8 digit slices; |V| < 2^62 in the epilogue
 constexpr int FUSED_KMAX = 16368;  // K of the FP8 split GEMM: (32 + 1/32) K < 2^19
@@ -120,9 +100,6 @@ constexpr int GROUP_M = 8;
 // tcgen05.mma instruction descriptor, kind::f8f6f4: D=F32, A=B=E4M3
 // (format 0), both K-major, N=256, M=128.
 constexpr uint32_t IDESC = (1u << 4) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
-// kind::f16: D=F32, A=B=BF16 (format 1), K-major, N=256, M=128 (grouped launches)
-constexpr uint32_t IDESC_BF16 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                                ((uint32_t)(BM >> 4) << 24);
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -244,28 +221,6 @@ __device__ __forceinline__ uint64_t desc_sw128(const void* p) {
   return d;
 }
 
-// K-major operand rows of 64 bytes with 64-byte swizzle (8-row atoms of 512 B)
-__device__ __forceinline__ uint64_t desc_sw64(const void* p) {
-  const uint32_t a = smem_u32(p);
-  uint64_t d = 0;
-  d |= (uint64_t)((a & 0x3FFFFu) >> 4);  // start address
-  d |= (uint64_t)1 << 16;                // leading byte offset (unused for swizzled K-major)
-  d |= (uint64_t)(512 >> 4) << 32;       // stride byte offset: 8 rows x 64 B
-  d |= (uint64_t)1 << 46;                // descriptor version (sm_100 family)
-  d |= (uint64_t)4 << 61;                // 64B swizzle
-  return d;
-}
-template <int ROW>
-__device__ __forceinline__ uint64_t desc_gemm(const void* p) { return ROW == 128 ? desc_sw128(p) : desc_sw64(p); }
-
-__device__ __forceinline__ void mma_bf16(uint32_t dt, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dt),
-      "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
-      : "memory");
-}
 __device__ __forceinline__ void mma_f8(uint32_t dt, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
@@ -339,19 +294,12 @@ struct GroupedTile {
   int prob, m_tile, n_tile, pad;
 };
 
-// An integer-valued float |f| < 2^22 as int without a conversion instruction:
-// f + 1.5 * 2^23 lies in [2^23, 2^24), where the float's mantissa bits are
-// the integer f + 2^22.  (Every slice product sum of the split GEMM is such an
-// integer: |P| <= 128 * 2 * K < 2^22 for K <= 16383.)
-__device__ __forceinline__ int exact_f2i(float f) {
-  return __float_as_int(__fadd_rn(f, 12582912.0f)) - 0x4B400000;
-}
-
 // q = 32 v for a float v that is a multiple of 2^-5 with |v| < 2^19 (a fused
 // FP8 slice pair, P_2p + P_2p+1 / 32), exactly and without a conversion
-// instruction: h = rint(v) through the 1.5 * 2^23 addend (|v| < 2^22), the
-// remainder l = v - h in [-1/2, 1/2] is exact, and 32 l is an integer in
-// [-16, 16]; q = 32 h + 32 l, |q| < 2^24.
+// instruction: h = rint(v) through the 1.5 * 2^23 addend (|v| < 2^22: v +
+// 1.5 * 2^23 lies in [2^23, 2^24), where the float's mantissa bits are the
+// integer h + 2^22), the remainder l = v - h in [-1/2, 1/2] is exact, and
+// 32 l is an integer in [-16, 16]; q = 32 h + 32 l, |q| < 2^24.
 __device__ __forceinline__ int fused_pair_f2i(float v) {
   const float t = __fadd_rn(v, 12582912.0f);
   const float l = __fsub_rn(v, __fsub_rn(t, 12582912.0f));
@@ -360,7 +308,7 @@ __device__ __forceinline__ int fused_pair_f2i(float v) {
 }
 
 // An integer |x| < 2^22 as a float, exactly, without a conversion
-// instruction (the inverse of exact_f2i).
+// instruction (the 1.5 * 2^23 addend read backwards).
 __device__ __forceinline__ float exact_i2f(int x) { return __fsub_rn(__int_as_float(x + 0x4B400000), 12582912.0f); }
 
 __device__ __forceinline__ void two_sum_g(float a, float b, float& s, float& e) {
@@ -465,14 +413,12 @@ struct GroupedTiles {
 
 // One pass of the split GEMM's epilogue for one thread (one output row,
 // `cend` columns of its half tile from `crow`, stride ldc): read the pass's
-// sums from TMEM 32 columns at a time (FUSED: one accumulator holding
-// P_2p + P_2p+1 / 32 at `tacc`; else P_2p at `tacc` and P_2p+1 at `tacc2`),
-// form the exact int32 q = P_2p * BASE + P_2p+1, and fold it into the int64
-// partial sums in C (V = V * BASE^2 + q), or on the last pass write V times
-// the row scale (FP64, or squared as a float pair for rows `sq`).
-template <bool FUSED, int BASE>
-__device__ __forceinline__ void epilogue_pass(uint32_t tacc, uint32_t tacc2, bool two, int p, bool last, bool sq,
-                                              double scale, float fscale, long long* crow, long long ldc, int cend) {
+// accumulator (P_2p + P_2p+1 / 32) from TMEM at `tacc` 32 columns at a time,
+// form the exact int32 q = 32 v = P_2p * 32 + P_2p+1, and fold it into the
+// int64 partial sums in C (V = V * 2^10 + q), or on the last pass write V
+// times the row scale (FP64, or squared as a float pair for rows `sq`).
+__device__ __forceinline__ void epilogue_pass(uint32_t tacc, int p, bool last, bool sq, double scale, float fscale,
+                                              long long* crow, long long ldc, int cend) {
 #pragma unroll 1
   for (int ch = 0; ch < BN / 64; ch++) {
     const int c0 = ch * 32;
@@ -482,22 +428,15 @@ __device__ __forceinline__ void epilogue_pass(uint32_t tacc, uint32_t tacc2, boo
 #pragma unroll
       for (int j = 0; j < 32; j++) prev[j] = (c0 + j < cend) ? __ldcg(crow + (long long)(c0 + j) * ldc) : 0;
     }
-    uint32_t v0[32], v1[32];
-    tmem_ld32(tacc + c0, v0);
-    if (!FUSED && two) tmem_ld32(tacc2 + c0, v1);
+    uint32_t v[32];
+    tmem_ld32(tacc + c0, v);
     tmem_ld_wait();
 #pragma unroll
     for (int j = 0; j < 32; j++) {
       if (c0 + j >= cend) break;
-      int qv;
-      if constexpr (FUSED) {
-        qv = fused_pair_f2i(__uint_as_float(v0[j]));
-      } else {
-        qv = exact_f2i(__uint_as_float(v0[j])) * BASE;
-        if (two) qv += exact_f2i(__uint_as_float(v1[j]));
-      }
+      const int qv = fused_pair_f2i(__uint_as_float(v[j]));
       long long* cp = crow + (long long)(c0 + j) * ldc;
-      const long long V = (p == 0) ? (long long)qv : prev[j] * (long long)(BASE * BASE) + (long long)qv;
+      const long long V = (p == 0) ? (long long)qv : prev[j] * 1024ll + (long long)qv;
       if (!last)
         *cp = V;
       else if (sq)
@@ -522,26 +461,21 @@ __device__ __forceinline__ void epilogue_pass(uint32_t tacc, uint32_t tacc2, boo
 constexpr int TQ = 4;                // tile-queue slots
 constexpr int TQ_CONSUMERS = 1 + 8;  // the MMA thread and lane 0 of each epilogue warp
 
-// Persistent split GEMM: each CTA takes tiles from the launch-wide counter
-// until none are left; per tile, (S + 1) / 2 passes of two slices each.  Per
-// pass the epilogue reads the pass's accumulation from TMEM 32 columns at a
-// time, forms the exact int32 q = P_2p * BASE + P_2p+1, folds q into the
-// int64 partial sums in C (V = V * BASE^2 + q; on the last pass the FP64 /
-// squared float-pair output) and then hands the columns back to the MMA
-// warp.  FP8 digits (FUSED): both slices of a pass go into one 256-column
-// accumulator and passes alternate between the two halves of TMEM, so the
-// epilogue of one pass runs under the MMAs of the next.  BF16 digits: slice
-// 2p in columns [0,256), 2p+1 in [256,512), one pass at a time.
+// Persistent one-SM split GEMM: each CTA takes tiles from the launch-wide
+// counter (or a static deal) until none are left; per tile, (S + 1) / 2
+// passes of two slices each, both into one 256-column accumulator, passes
+// alternating between the two halves of TMEM so that the epilogue of one
+// pass (epilogue_pass) runs under the MMAs of the next.
 // Between tiles the producer keeps loading the next tile's operands, so a
 // CTA never drains its ring, and TMEM is allocated and the barriers
 // initialised once per CTA.  (Releasing TMEM before the C round trip, with
 // q held in registers, measured slower: within 168 registers a thread keeps
 // too few partial-sum loads in flight for the round trip to finish within
 // one pass of MMAs.)
-template <int KB, int ESZ, class Src>
+template <class Src>
 __device__ __forceinline__ void gemm_persistent(const Src& src, int* tile_counter) {
-  using R = GemmRing<KB, ESZ>;
-  constexpr int BASE = ESZ == 1 ? 32 : 256;  // digit base: FP8 five-bit, BF16 eight-bit digits
+  using R = GemmRing;
+  constexpr int KB = R::ROW;  // FP8 digits per K-step
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* full = (uint64_t*)(smem + R::STAGES * R::STAGE);
@@ -555,9 +489,6 @@ __device__ __forceinline__ void gemm_persistent(const Src& src, int* tile_counte
   uint32_t* tbase_slot = (uint32_t*)(tq_id + TQ);
   volatile int* abort_flag = (volatile int*)(tbase_slot + 1);
   static_assert((R::STAGES * 2 + 5 + 2 * TQ) * 8 + TQ * 4 + 8 <= 256, "barriers fit the 256-byte tail");
-  // FP8 five-bit digits: a slice pair accumulates exactly in one FP32
-  // accumulator (K <= FUSED_KMAX), so TMEM holds two passes
-  constexpr bool FUSED = ESZ == 1;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ntiles = src.count();
@@ -685,30 +616,21 @@ __device__ __forceinline__ void gemm_persistent(const Src& src, int* tile_counte
 #pragma unroll 1
         for (int p = 0; p < passes && ok; p++, q++) {
           const bool two = 2 * p + 1 < g.S;
-          const uint32_t buf = FUSED ? (q & 1) : 0;
-          const uint32_t par = FUSED ? ((q >> 1) & 1) : (q & 1);
+          const uint32_t buf = q & 1, par = (q >> 1) & 1;  // accumulator half and its phase
           if (!mbar_wait(&tempty[buf], par ^ 1, abort_flag, g.err, 2, g.wait_ns)) { ok = false; break; }
           tc_fence_after();
-          const uint32_t acc0 = tbase + 256 * buf;              // slice 2p
-          const uint32_t acc1 = FUSED ? acc0 : tbase + 256;     // slice 2p + 1
+          const uint32_t acc = tbase + 256 * buf;
 #pragma unroll 1
           for (int kb = 0; kb < nk; kb++) {
             if (!mbar_wait(&full[stage], phase, abort_flag, g.err, 3, g.wait_ns)) { ok = false; break; }
             tc_fence_after();
             uint8_t* sb = smem + stage * R::STAGE;
-            const uint64_t a0 = desc_gemm<R::ROW>(sb), a1 = desc_gemm<R::ROW>(sb + R::A),
-                           b = desc_gemm<R::ROW>(sb + 2 * R::A);
+            const uint64_t a0 = desc_sw128(sb), a1 = desc_sw128(sb + R::A), b = desc_sw128(sb + 2 * R::A);
 #pragma unroll
-            for (int kk = 0; kk < R::ROW / 32; kk++) {  // 32 bytes of K per MMA (32 FP8 or 16 BF16 digits)
+            for (int kk = 0; kk < R::ROW / 32; kk++) {  // 32 FP8 digits per MMA
               const uint64_t koff = (uint64_t)((kk * 32) >> 4);
-              const uint32_t acc = (kb > 0 || kk > 0) ? 1u : 0u;
-              if constexpr (ESZ == 1) {
-                mma_f8(acc0, a0 + koff, b + koff, IDESC, acc);
-                if (two) mma_f8(acc1, a1 + koff, b + koff, IDESC, 1u);  // adds to slice 2p's sum
-              } else {
-                mma_bf16(acc0, a0 + koff, b + koff, IDESC_BF16, acc);
-                if (two) mma_bf16(acc1, a1 + koff, b + koff, IDESC_BF16, acc);
-              }
+              mma_f8(acc, a0 + koff, b + koff, IDESC, (kb > 0 || kk > 0) ? 1u : 0u);
+              if (two) mma_f8(acc, a1 + koff, b + koff, IDESC, 1u);  // adds to slice 2p's sum
             }
             any = true;
             mma_commit(&empty[stage]);
@@ -769,8 +691,7 @@ __device__ __forceinline__ void gemm_persistent(const Src& src, int* tile_counte
       for (int p = 0; p < passes; p++, q++) {
         const bool two = 2 * p + 1 < g.S;
         const bool last = p == passes - 1;
-        const uint32_t buf = FUSED ? (q & 1) : 0;
-        const uint32_t par = FUSED ? ((q >> 1) & 1) : (q & 1);
+        const uint32_t buf = q & 1, par = (q >> 1) & 1;
         // pull this row's partial sums (written a pass ago, since evicted by
         // the operand stream) back into L2 while the pass's MMAs run
         if (p > 0)
@@ -781,7 +702,7 @@ __device__ __forceinline__ void gemm_persistent(const Src& src, int* tile_counte
         okw = __shfl_sync(0xffffffffu, okw, 0);  // warp-uniform: tcgen05.ld is .sync.aligned
         if (!okw) { ok = false; break; }
         tc_fence_after();
-        epilogue_pass<FUSED, BASE>(ta + 256 * buf, ta + 256, two, p, last, sq, scale, fscale, crow, g.ldc, cend);
+        epilogue_pass(ta + 256 * buf, p, last, sq, scale, fscale, crow, g.ldc, cend);
         tc_fence_before();
         mbar_arrive(&tempty[buf]);
       }
@@ -808,7 +729,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                       const __grid_constant__ GemmArgs g, int* tile_counter) {
   const SingleTiles src{&tmA, &tmB, &g, -1};
-  gemm_persistent<GBK, 1>(src, tile_counter);
+  gemm_persistent(src, tile_counter);
 }
 
 // ---------------------------------------------------------------------------
@@ -847,7 +768,6 @@ __device__ __forceinline__ void gemm_pair(const SingleTiles& src) {
   constexpr int ROW = p2::ROW, A = p2::A, B = p2::B, STAGE = p2::STAGE, STAGES = p2::STAGES;
   constexpr int EPI_WARPS = p2::EPI_WARPS;
   constexpr uint32_t IDESC = p2::IDESC;
-  constexpr int BASE = 32;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* full = (uint64_t*)(smem + STAGES * STAGE);  // [STAGES], used in the leader
@@ -1075,7 +995,7 @@ __device__ __forceinline__ void gemm_pair(const SingleTiles& src) {
         okw = __shfl_sync(0xffffffffu, okw, 0);
         if (!okw) { ok = false; break; }
         tc_fence_after();
-        epilogue_pass<true, BASE>(ta + 256 * buf, 0, two, p, last, sq, scale, fscale, crow, g.ldc, cend);
+        epilogue_pass(ta + 256 * buf, p, last, sq, scale, fscale, crow, g.ldc, cend);
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive_cluster(lead_tempty + 8u * buf);
@@ -1119,7 +1039,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                               const CUtensorMap* __restrict__ maps, const int* __restrict__ cols, int ntiles,
                               int* tile_counter) {
   const GroupedTiles src{tiles, probs, maps, cols, ntiles};
-  gemm_persistent<GRBK, 2>(src, tile_counter);
+  gemm_persistent(src, tile_counter);
 }
 
 // ---------------------------------------------------------------------------
@@ -1146,11 +1066,12 @@ __global__ void __launch_bounds__(THREADS, 1)
 // bounded waits as ozaki_gemm_kernel.  Threads keep the running (hi, lo) sums
 // of 56 traits.
 // ---------------------------------------------------------------------------
+constexpr int QT_STAGES = 3;                      // ring stages
 constexpr int QT_TP = 112;                          // trait rows of the digit operand
 constexpr int QT_KB = 128;                          // K-block: 128 one-byte digits (one 128B-swizzled row)
 constexpr int QT_BT = QT_TP * QT_KB;                // 14 KB trait tile
 constexpr int QT_STAGE = A_TILE + 4 * QT_BT;        // 72 KB
-constexpr int QT_SMEM = STAGES * QT_STAGE + 1024 + 256;
+constexpr int QT_SMEM = QT_STAGES * QT_STAGE + 1024 + 256;
 constexpr int QT_MAXPASS = 40;
 // kind::f8f6f4 instruction descriptor: F32 accumulator, A and B E4M3 (format
 // 0), K-major, N = 224, M = 128
@@ -1226,9 +1147,9 @@ __global__ void __launch_bounds__(THREADS, 1)
                   const __grid_constant__ QuadPasses qp, const QuadArgs g) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint64_t* full = (uint64_t*)(smem + STAGES * QT_STAGE);
-  uint64_t* empty = full + STAGES;
-  uint64_t* tfull = empty + STAGES;
+  uint64_t* full = (uint64_t*)(smem + QT_STAGES * QT_STAGE);
+  uint64_t* empty = full + QT_STAGES;
+  uint64_t* tfull = empty + QT_STAGES;
   uint64_t* tempty = tfull + 1;
   uint64_t* drain = tempty + 1;
   uint32_t* tbase_slot = (uint32_t*)(drain + 1);
@@ -1241,7 +1162,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   const int u1 = qt_range_begin(blockIdx.x + 1, g.units, gridDim.x);
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < STAGES; s++) {
+    for (int s = 0; s < QT_STAGES; s++) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
@@ -1266,9 +1187,9 @@ __global__ void __launch_bounds__(THREADS, 1)
     if (lane == 0) {
       int stage = 0;
       uint32_t phase = 0;
-      int issued[STAGES];
-      uint32_t issued_phase[STAGES];
-      for (int s = 0; s < STAGES; s++) issued[s] = 0;
+      int issued[QT_STAGES];
+      uint32_t issued_phase[QT_STAGES];
+      for (int s = 0; s < QT_STAGES; s++) issued[s] = 0;
       bool ok = true;
       for (int u = u0; u < u1 && ok; u++) {
         const int tile = u / np, p = u - tile * np;
@@ -1287,11 +1208,11 @@ __global__ void __launch_bounds__(THREADS, 1)
                           &full[stage]);
           issued[stage] = 1;
           issued_phase[stage] = phase;
-          if (++stage == STAGES) { stage = 0; phase ^= 1; }
+          if (++stage == QT_STAGES) { stage = 0; phase ^= 1; }
         }
       }
       if (!ok)
-        for (int s = 0; s < STAGES; s++)
+        for (int s = 0; s < QT_STAGES; s++)
           if (issued[s]) mbar_drain(&full[s], issued_phase[s]);
     }
   } else if (warp == 1) {
@@ -1322,7 +1243,7 @@ __global__ void __launch_bounds__(THREADS, 1)
           }
           any = true;
           mma_commit(&empty[stage]);
-          if (++stage == STAGES) { stage = 0; phase ^= 1; }
+          if (++stage == QT_STAGES) { stage = 0; phase ^= 1; }
         }
         if (!ok) break;
         mma_commit(tfull);
@@ -1525,15 +1446,14 @@ __global__ void __launch_bounds__(256) trait_digits_kernel(int n, const double* 
 
 // ---------------------------------------------------------------------------
 // Slicing: row r of A (K-contiguous source, element k at src[k + r*lds]) ->
-// S digit slices (E4M3 bytes, or BF16 when BF16D) at A[(s*Mpad + r)*Kpad + k],
-// scale per row.
+// S five-bit digit slices (E4M3 bytes; odd slices hold d / 32, the weight
+// of a fused pair's second slice) at A[(s*Mpad + r)*Kpad + k], scale per row.
 // ---------------------------------------------------------------------------
-template <bool BF16D>
 __global__ void __launch_bounds__(256) slice_rows_kernel(int K, int rows, const double* __restrict__ src,
                                                          long long lds, int row_off, int S, int Mpad, int Kpad,
-                                                         void* __restrict__ Aout, double* __restrict__ row_scale) {
-  // FP8: five-bit digits |d| <= 16 (E4M3 bytes); BF16: eight-bit digits |d| <= 128
-  constexpr int LOG_BASE = BF16D ? 8 : 5;
+                                                         uint8_t* __restrict__ Aout, double* __restrict__ row_scale) {
+  // five-bit digits |d| <= 16, exact in E4M3 (and so is d / 32)
+  constexpr int LOG_BASE = 5;
   const int r = blockIdx.x;
   if (r >= rows) return;
   const double* a = src + (long long)r * lds;
@@ -1563,19 +1483,13 @@ __global__ void __launch_bounds__(256) slice_rows_kernel(int K, int rows, const 
     for (int s = 0; s < S; s++) {
       const double d = rint(v);
       const long long at = ((long long)s * Mpad + R) * Kpad + k;
-      if constexpr (BF16D)
-        ((__nv_bfloat16*)Aout)[at] = __double2bfloat16(d);  // |d| <= 128: exact
-      else  // |d| <= 16: exact; odd slices hold d / 32, the weight of a fused pair's second slice
-        ((uint8_t*)Aout)[at] = (uint8_t)e4m3_digit((s & 1) ? (float)d * 0.03125f : (float)d);
+      Aout[at] = (uint8_t)e4m3_digit((s & 1) ? (float)d * 0.03125f : (float)d);
       v = (v - d) * (double)(1 << LOG_BASE);
     }
   }
 }
 
-// Genotype value (FP64 or byte) as BF16 (grouped launches) or as an E4M3 byte
-// (single-problem launches); hard calls 0/1/2 are exact in both.
-__device__ __forceinline__ __nv_bfloat16 geno_bf16(unsigned char v) { return __float2bfloat16((float)v); }
-__device__ __forceinline__ __nv_bfloat16 geno_bf16(double v) { return __float2bfloat16((float)v); }
+// Genotype value (FP64 or byte) as an E4M3 byte; hard calls 0/1/2 are exact.
 __device__ __forceinline__ uint8_t geno_f8(unsigned char v) {
   return (uint8_t)__nv_cvt_float_to_fp8((float)v, __NV_SATFINITE, __NV_E4M3);
 }
@@ -1712,26 +1626,19 @@ EncodeTiledFn get_encoder() {
   return fn;
 }
 
-// 2D tensor map of esz-byte digits (1: E4M3, 2: BF16), K innermost, box
-// {box_k, box_rows}; 128B swizzle for 128-byte rows, 64B swizzle for 64-byte
-// rows.  make_map is the single-problem split GEMM's E4M3 layout (K-step GBK).
-cudaError_t make_map_box(CUtensorMap* m, const void* base, long long K, long long rows, int box_rows, int box_k,
-                         int esz) {
+// 2D tensor map of the split GEMM's E4M3 operands (A slices or genotypes):
+// K innermost in rows of K bytes, box {GBK, box_rows}, 128B swizzle.
+cudaError_t make_map(CUtensorMap* m, const void* base, long long K, long long rows, int box_rows) {
   EncodeTiledFn enc = get_encoder();
   if (!enc) return cudaErrorNotSupported;
   cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)K * esz};
-  cuuint32_t box[2] = {(cuuint32_t)box_k, (cuuint32_t)box_rows};
+  cuuint64_t strides[1] = {(cuuint64_t)K};
+  cuuint32_t box[2] = {(cuuint32_t)GBK, (cuuint32_t)box_rows};
   cuuint32_t es[2] = {1, 1};
-  const int row = box_k * esz;
-  CUresult r = enc(m, esz == 2 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_UINT8, 2,
-                   const_cast<void*>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                   row == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
-                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<void*>(base), dims, strides, box, es,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
-}
-cudaError_t make_map(CUtensorMap* m, const void* base, long long K, long long rows, int box_rows) {
-  return make_map_box(m, base, K, rows, box_rows, GBK, 1);
 }
 // 2D byte tensor map (FP8 digits), K innermost in rows of K bytes, box
 // {QT_KB, box_rows}, 128B swizzle.
@@ -1934,10 +1841,10 @@ namespace {
 cudaError_t slice_operands(OzakiPlan* p, cudaStream_t s, const double* top, long long ldtop, int toprows) {
   // rows [0, toprows) from `top` (row r contiguous at top + r*ldtop), rows
   // [n, n + nU) from the columns of U.
-  slice_rows_kernel<false><<<toprows, 256, 0, s>>>(p->n, toprows, top, ldtop, 0, p->S, p->Mpad, p->Kpad, p->A,
+  slice_rows_kernel<<<toprows, 256, 0, s>>>(p->n, toprows, top, ldtop, 0, p->S, p->Mpad, p->Kpad, p->A,
                                                     p->scale);
   note_launch();
-  slice_rows_kernel<false><<<p->nU, 256, 0, s>>>(p->n, p->nU, p->U, p->n, p->n, p->S, p->Mpad, p->Kpad, p->A,
+  slice_rows_kernel<<<p->nU, 256, 0, s>>>(p->n, p->nU, p->U, p->n, p->n, p->S, p->Mpad, p->Kpad, p->A,
                                                   p->scale);
   note_launch();
   return cudaGetLastError();
@@ -2124,23 +2031,23 @@ int split_k_padded(int n) { return (n + KALIGN - 1) / KALIGN * KALIGN; }
 int split_cols_padded(int x) { return (x + BN - 1) / BN * BN; }
 
 cudaError_t split_chol_operand(cudaStream_t s, int n, int wXL, const double* L, const double* WY, int S, int Mpad,
-                               int Kpad, __nv_bfloat16* A, double* scale, double* Linv, double* LinvT, double* U) {
+                               int Kpad, uint8_t* A, double* scale, double* Linv, double* LinvT, double* U) {
   const int nU = 1 + wXL;
   FGLS_CUDA_TRY(lower_inverse(s, n, L, Linv));
   FGLS_CUDA_TRY(dgemm(s, true, false, n, nU, n, 1.0, Linv, n, WY, n, 0.0, U, n));
   dim3 tg((n + 31) / 32, (n + 31) / 32);
   transpose_kernel<<<tg, dim3(32, 8), 0, s>>>(n, Linv, LinvT);
   note_launch();
-  slice_rows_kernel<true><<<n, 256, 0, s>>>(n, n, LinvT, n, 0, S, Mpad, Kpad, A, scale);
+  slice_rows_kernel<<<n, 256, 0, s>>>(n, n, LinvT, n, 0, S, Mpad, Kpad, A, scale);
   note_launch();
-  slice_rows_kernel<true><<<nU, 256, 0, s>>>(n, nU, U, n, n, S, Mpad, Kpad, A, scale);
+  slice_rows_kernel<<<nU, 256, 0, s>>>(n, nU, U, n, n, S, Mpad, Kpad, A, scale);
   note_launch();
   return cudaGetLastError();
 }
 
 namespace {
 // per-row scale of an S-slice operand from that of the same digits cut at
-// S_built slices: 2^(e - 15 - 16 (passes - 1)) depends on the pass count only
+// S_built slices: 2^(e + 1 - 10 passes) depends on the pass count only
 __global__ void rescale_rows_kernel(int rows, const double* __restrict__ built, int bits, double* __restrict__ out) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r < rows) out[r] = ldexp(built[r], bits);
@@ -2151,25 +2058,26 @@ __global__ void grouped_genotypes_kernel(const GenoCohort* __restrict__ gc, cons
   const int c = blockIdx.y;
   const int x = sc[c].x, n = gc[c].n, Kpad = gc[c].Kpad;
   const T* __restrict__ src = (const T*)sc[c].X;
-  __nv_bfloat16* __restrict__ G = gc[c].G;
+  uint8_t* __restrict__ G = gc[c].G;
   // columns strided over the CTAs of this cohort, rows over the threads; u8
-  // columns that start on a 4-byte boundary move 4 calls per load
+  // columns that start on a 4-byte boundary move 4 calls per load (Kpad is a
+  // multiple of 128, so the E4M3 column is 4-byte aligned)
   for (int col = blockIdx.x; col < x; col += gridDim.x) {
     const T* s = src + (long long)col * n;
-    __nv_bfloat16* g = G + (long long)col * Kpad;
+    uint8_t* g = G + (long long)col * Kpad;
     if constexpr (sizeof(T) == 1) {
       if (((uintptr_t)s & 3) == 0) {
         const int n4 = n >> 2;
         for (int q = threadIdx.x; q < n4; q += blockDim.x) {
           const uchar4 v = ((const uchar4*)s)[q];
-          ((__nv_bfloat162*)g)[2 * q] = __halves2bfloat162(geno_bf16(v.x), geno_bf16(v.y));
-          ((__nv_bfloat162*)g)[2 * q + 1] = __halves2bfloat162(geno_bf16(v.z), geno_bf16(v.w));
+          ((uint32_t*)g)[q] = (uint32_t)geno_f8(v.x) | ((uint32_t)geno_f8(v.y) << 8) |
+                              ((uint32_t)geno_f8(v.z) << 16) | ((uint32_t)geno_f8(v.w) << 24);
         }
-        for (int k = 4 * n4 + threadIdx.x; k < n; k += blockDim.x) g[k] = geno_bf16(s[k]);
+        for (int k = 4 * n4 + threadIdx.x; k < n; k += blockDim.x) g[k] = geno_f8(s[k]);
         continue;
       }
     }
-    for (int k = threadIdx.x; k < n; k += blockDim.x) g[k] = geno_bf16(s[k]);
+    for (int k = threadIdx.x; k < n; k += blockDim.x) g[k] = geno_f8(s[k]);
   }
 }
 }  // namespace
@@ -2177,7 +2085,7 @@ __global__ void grouped_genotypes_kernel(const GenoCohort* __restrict__ gc, cons
 cudaError_t split_rescale_rows(cudaStream_t s, int rows, const double* built_scale, int S_built, int S,
                                double* scale) {
   const int dpass = (S_built + 1) / 2 - (S + 1) / 2;
-  rescale_rows_kernel<<<(rows + 255) / 256, 256, 0, s>>>(rows, built_scale, 16 * dpass, scale);  // 16 bits a BF16 pair
+  rescale_rows_kernel<<<(rows + 255) / 256, 256, 0, s>>>(rows, built_scale, 10 * dpass, scale);  // 10 bits a slice pair
   note_launch();
   return cudaGetLastError();
 }
@@ -2242,8 +2150,8 @@ cudaError_t grouped_gemm_create(GroupedGemm** out, const GroupedGemmDesc* d, int
     g.wait_ns = WAIT_NS;
     probs[i].cohort = d[i].cohort;
     probs[i].pad = 0;
-    FGLS_CUDA_TRY(make_map_box(&maps[2 * i], d[i].A, d[i].Kpad, (long long)d[i].S_alloc * d[i].Mpad, BM, GRBK, 2));
-    FGLS_CUDA_TRY(make_map_box(&maps[2 * i + 1], d[i].G, d[i].Kpad, d[i].Ncap, BN, GRBK, 2));
+    FGLS_CUDA_TRY(make_map(&maps[2 * i], d[i].A, d[i].Kpad, (long long)d[i].S_alloc * d[i].Mpad, BM));
+    FGLS_CUDA_TRY(make_map(&maps[2 * i + 1], d[i].G, d[i].Kpad, d[i].Ncap, BN));
     order[i] = i;
     work[i] = (long long)g.tiles_m * g.Kpad;
   }
@@ -2279,7 +2187,7 @@ cudaError_t grouped_gemm_create(GroupedGemm** out, const GroupedGemmDesc* d, int
     chk(cudaMemcpy(gg->maps, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice));
   if (r == cudaSuccess)
     chk(cudaFuncSetAttribute(ozaki_grouped_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             GROUPED_SMEM_BYTES));
+                             SMEM_BYTES));
   if (r != cudaSuccess) {
     grouped_gemm_destroy(gg);
     return r;
@@ -2290,7 +2198,7 @@ cudaError_t grouped_gemm_create(GroupedGemm** out, const GroupedGemmDesc* d, int
 
 cudaError_t grouped_gemm_run(GroupedGemm* gg, cudaStream_t s, const int* dcols) {
   if (gg->ntiles == 0) return cudaSuccess;
-  ozaki_grouped_gemm_kernel<<<persistent_grid(gg->ntiles), THREADS, GROUPED_SMEM_BYTES, s>>>(
+  ozaki_grouped_gemm_kernel<<<persistent_grid(gg->ntiles), THREADS, SMEM_BYTES, s>>>(
       gg->tiles, gg->probs, gg->maps, dcols, gg->ntiles, gg->counter);
   note_launch();
   return cudaGetLastError();
@@ -2352,7 +2260,7 @@ extern "C" int fglsgpu_selftest_split_gemm(int M, int K, int N, int S, const dou
   if (r == cudaSuccess)
     chk(cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
   if (r == cudaSuccess) {
-    slice_rows_kernel<false><<<M, 256, 0, s>>>(K, M, dA, K, 0, S, p.Mpad, p.Kpad, p.A, p.scale);
+    slice_rows_kernel<<<M, 256, 0, s>>>(K, M, dA, K, 0, S, p.Mpad, p.Kpad, p.A, p.scale);
     chk(cudaGetLastError());
   }
   if (r == cudaSuccess) chk(load_genotypes<double>(&p, s, dX, N));
@@ -2458,7 +2366,7 @@ extern "C" int fglsgpu_split_gemm_noalloc(int M, int K, int N, int slices, const
   if (r == cudaSuccess) chk(make_map(&p.mapA, p.A, p.Kpad, (long long)slices * p.Mpad, BM));
   if (r == cudaSuccess) chk(make_map(&p.mapB, p.G, p.Kpad, p.Ncap, BN));
   if (r == cudaSuccess) {
-    slice_rows_kernel<false><<<M, 256, 0, s>>>(K, M, dA, K, 0, slices, p.Mpad, p.Kpad, p.A, p.scale);
+    slice_rows_kernel<<<M, 256, 0, s>>>(K, M, dA, K, 0, slices, p.Mpad, p.Kpad, p.A, p.scale);
     note_launch();
     chk(cudaGetLastError());
   }

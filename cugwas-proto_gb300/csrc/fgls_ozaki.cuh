@@ -1,13 +1,12 @@
 // Split-precision ("Ozaki") tensor-core path: the FP64 operand of each bulk
 // GEMM (Z^T, U = M^-1 [y XL] or L^-1) is cut into integer digit slices with a
-// per-row power-of-two scale: five-bit digits stored as FP8 E4M3 for
-// single-problem launches, eight-bit digits in BF16 for the grouped (batched
-// cohort) launch; the genotype operand (0/1/2) is exact in either format.  tcgen05.mma (kind::f8f6f4 or kind::f16) multiplies slice x
-// genotype tiles with FP32 accumulation in TMEM (every partial sum is an
-// integer below 2^24, hence exact), and the epilogue recombines the slices.
+// per-row power-of-two scale: five-bit digits stored as FP8 E4M3 (odd
+// slices as d / 32); the genotype operand (0/1/2) is exact in E4M3 too.
+// tcgen05.mma (kind::f8f6f4) accumulates each slice pair x genotype tile in
+// one FP32 accumulator in TMEM (every partial sum is a multiple of 2^-5
+// below 2^19, hence exact), and the epilogue recombines the pairs.
 #pragma once
 
-#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -66,22 +65,22 @@ struct GenoCohort;
 int split_rows_padded(int rows);
 int split_k_padded(int n);
 int split_cols_padded(int x);
-// [L^-1 ; (L^-T WY)^T] of one chol problem cut into S BF16 eight-bit digit slices at A
+// [L^-1 ; (L^-T WY)^T] of one chol problem cut into S E4M3 five-bit digit slices at A
 // (S x Mpad x Kpad) with row scales; Linv, LinvT (n x n) and U (n x (1+wXL))
 // are caller scratch.
 cudaError_t split_chol_operand(cudaStream_t s, int n, int wXL, const double* L, const double* WY, int S, int Mpad,
-                               int Kpad, __nv_bfloat16* A, double* scale, double* Linv, double* LinvT, double* U);
+                               int Kpad, uint8_t* A, double* scale, double* Linv, double* LinvT, double* U);
 // row scales of the first S slices of an operand cut into S_built slices
 cudaError_t split_rescale_rows(cudaStream_t s, int rows, const double* built_scale, int S_built, int S,
                                double* scale);
-// genotype blocks of all cohorts (per-step table) -> their BF16 operands
+// genotype blocks of all cohorts (per-step table) -> their E4M3 operands
 cudaError_t grouped_genotypes(cudaStream_t s, const GenoCohort* dgc, const StepCohort* dsc, int cohorts, bool u8);
 
 struct GroupedGemmDesc {
-  const __nv_bfloat16* A;  // BF16 digit slices, S_alloc x Mpad x Kpad
+  const uint8_t* A;        // E4M3 five-bit digit slices (odd slices / 32), S_alloc x Mpad x Kpad
   int S, S_alloc, M, Mpad, Kpad, tri_rows, sq_rows;
   const double* scale;     // Mpad row scales for S slices
-  const __nv_bfloat16* G;  // cohort BF16 genotype operand, Ncap x Kpad
+  const uint8_t* G;        // cohort E4M3 genotype operand, Ncap x Kpad
   int Ncap;
   double* C;               // Mpad x x_b output (ld Mpad)
   int cohort;

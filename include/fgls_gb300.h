@@ -331,7 +331,8 @@ typedef struct {
 
 typedef struct {
   int x_b;          /* SNPs per cohort per step (0: autotune)             */
-  int slices;       /* BF16 eight-bit digit slices 3..6 (0: autotune)     */
+  int slices;       /* FP8 five-bit digit slices 1..9 (0: autotune over   */
+                    /* 5..9); cohorts need n <= 16368                     */
   int device;       /* CUDA device ordinal                                */
   int use_graph;    /* 1: replay each step from a captured CUDA graph     */
   int genotypes_u8; /* 1: genotype blocks are bytes, 0: FP64              */

@@ -75,8 +75,8 @@ def check(pbs, out):
 def test_batch_matches_oracle_per_cohort_with_graph():
     from fgls_gb300 import Batch
     pbs, desc = cohorts()
-    with Batch(desc, x_b=256, slices=6, use_graph=True) as b:
-        assert b.params()[:2] == (256, 6)
+    with Batch(desc, x_b=256, slices=9, use_graph=True) as b:
+        assert b.params()[:2] == (256, 9)
         out = run_batch(b, pbs, 256)
     check(pbs, out)
 
@@ -84,9 +84,9 @@ def test_batch_matches_oracle_per_cohort_with_graph():
 def test_batch_graph_replay_is_bit_identical_and_idle_cohorts():
     from fgls_gb300 import Batch
     pbs, desc = cohorts(COHORTS[:3], seed=40)
-    with Batch(desc, x_b=128, slices=6, use_graph=False) as b:
+    with Batch(desc, x_b=128, slices=9, use_graph=False) as b:
         ref = run_batch(b, pbs, 128)
-    with Batch(desc, x_b=128, slices=6, use_graph=True) as b:
+    with Batch(desc, x_b=128, slices=9, use_graph=True) as b:
         got = run_batch(b, pbs, 128, idle=1)
     for (B1, V1), (B2, V2) in zip(ref, got):
         assert np.array_equal(B1, B2) and np.array_equal(V1, V2)
@@ -95,7 +95,7 @@ def test_batch_graph_replay_is_bit_identical_and_idle_cohorts():
 def test_batch_fp64_genotype_input():
     from fgls_gb300 import Batch
     pbs, desc = cohorts(COHORTS[1:3], seed=60)
-    with Batch(desc, x_b=256, slices=6, use_graph=True, genotypes_u8=False) as b:
+    with Batch(desc, x_b=256, slices=9, use_graph=True, genotypes_u8=False) as b:
         out = run_batch(b, pbs, 256, u8=False)
     check(pbs, out)
 
@@ -105,7 +105,7 @@ def test_batch_autotuner_meets_tolerance():
     pbs, desc = cohorts(COHORTS[:4], seed=80)
     with Batch(desc, x_b=0, slices=0, use_graph=True, tol=1e-10) as b:
         x_b, S, perr = b.params()
-        assert x_b in (1024, 2048, 4096, 8192) and 3 <= S <= 6
+        assert x_b in (1024, 2048, 4096, 8192) and 5 <= S <= 9
         assert 0.0 <= perr <= 1e-10 / 8
         out = run_batch(b, pbs, x_b)
     check(pbs, out)
