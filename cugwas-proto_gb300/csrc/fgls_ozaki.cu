@@ -380,22 +380,25 @@ struct SingleTiles {
     const int per_group = gm * g->tiles_n;
     const int first_m = (t / per_group) * gm;
     const int gsz = min(units_m() - first_m, gm);
-    int m_tile = first_m + (t % per_group) % gsz;
-    if (pair_rank >= 0) m_tile = 2 * m_tile + pair_rank;
-    if (g->tri_rows > 0) m_tile = g->tiles_m - 1 - m_tile;
+    int mu = first_m + (t % per_group) % gsz;
+    if (g->tri_rows > 0) mu = units_m() - 1 - mu;  // longest (lowest) rows of L^-1 first
+    const int m_tile = pair_rank >= 0 ? 2 * mu + pair_rank : mu;
     return TileRef{0, m_tile, (t % per_group) / gsz, g->N, false};
   }
 };
 
 // Many independent problems: a host-built table of tiles (longest problems
 // first); the valid columns of each cohort this launch are cols[cohort];
-// tensor maps in global memory, written by the host before the launch.
+// tensor maps in global memory, written by the host before the launch.  In
+// the 2-SM kernel an entry names a pair of row tiles (m_tile = pair index):
+// rank r computes row tile 2 m_tile + r.
 struct GroupedTiles {
   const GroupedTile* tiles;
   const GroupedProblem* probs;
   const CUtensorMap* maps;
   const int* cols;
   int ntiles;
+  int pair_rank;  // CTA rank in the 2-SM kernel's pair, -1: one CTA per tile
   static constexpr bool global_maps = true;
   __device__ __forceinline__ int count() const { return ntiles; }
   __device__ __forceinline__ bool dynamic() const { return true; }
@@ -407,7 +410,8 @@ struct GroupedTiles {
   __device__ __forceinline__ TileRef tile(int i) const {
     const GroupedTile tl = tiles[i];
     const int N = cols[probs[tl.prob].cohort];
-    return TileRef{tl.prob, tl.m_tile, tl.n_tile, N, tl.n_tile * BN >= N};
+    const int m_tile = pair_rank >= 0 ? 2 * tl.m_tile + pair_rank : tl.m_tile;
+    return TileRef{tl.prob, m_tile, tl.n_tile, N, tl.n_tile * BN >= N};
   }
 };
 
@@ -733,7 +737,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 }
 
 // ---------------------------------------------------------------------------
-// 2-SM split GEMM (FP8 digits, uniform tiles): a cluster of two CTAs on two
+// 2-SM split GEMM (FP8 digits): a cluster of two CTAs on two
 // SMs computes 256 x 256 output tiles with tcgen05.mma.cta_group::2 (M =
 // 256, N = 256, K = 32).  CTA rank r holds rows 128 r .. 128 r + 127 of the
 // tile (its A-slice tiles in shared memory, its accumulators in TMEM) and
@@ -749,9 +753,13 @@ __global__ void __launch_bounds__(THREADS, 1)
 // it; the leader arms it with both CTAs' bytes); empty[s] and tfull[b] live
 // in both CTAs and are released by the leader's multicast commits;
 // tempty[b] lives in the leader and counts one arrival per epilogue warp of
-// both CTAs.  Tiles are dealt statically per pair, so both CTAs know the
-// sequence without exchanging it; each CTA's producer still publishes it to
-// its own MMA thread (leader only) and epilogue warps.  Every wait is bounded.
+// both CTAs.  The leader's producer picks each tile (a static deal per
+// cluster for uniform tiles, the launch-wide counter for the triangular L^-1
+// operand and for grouped problems) and writes its index into both CTAs'
+// tile queues (the peer's slot through distributed shared memory, then a
+// remote arrive on the peer's tq_full); tq_empty lives in the leader and
+// counts the slot's eighteen readers (the leader's MMA thread, the peer's
+// producer, both CTAs' epilogue warps).  Every wait is bounded.
 namespace p2 {
 constexpr int ROW = 128;            // bytes (FP8 digits) per K-step row
 constexpr int A = BM * ROW;         // 16 KB: one A-slice tile of this CTA
@@ -764,7 +772,8 @@ constexpr uint32_t IDESC = (1u << 4) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)
 constexpr int EPI_WARPS = 8;
 }  // namespace p2
 
-__device__ __forceinline__ void gemm_pair(const SingleTiles& src) {
+template <class Src>
+__device__ __forceinline__ void gemm_pair(const Src& src, int* tile_counter) {
   constexpr int ROW = p2::ROW, A = p2::A, B = p2::B, STAGE = p2::STAGE, STAGES = p2::STAGES;
   constexpr int EPI_WARPS = p2::EPI_WARPS;
   constexpr uint32_t IDESC = p2::IDESC;
@@ -775,14 +784,13 @@ __device__ __forceinline__ void gemm_pair(const SingleTiles& src) {
   uint64_t* tfull = empty + STAGES;                      // [2]
   uint64_t* tempty = tfull + 2;                          // [2], used in the leader
   uint64_t* drain = tempty + 2;
-  uint64_t* tq_full = drain + 1;
-  uint64_t* tq_empty = tq_full + TQ;
+  uint64_t* tq_full = drain + 1;                         // [TQ], both CTAs
+  uint64_t* tq_empty = tq_full + TQ;                     // [TQ], used in the leader
   volatile int* tq_id = (volatile int*)(tq_empty + TQ);
   uint32_t* tbase_slot = (uint32_t*)(tq_id + TQ);
   volatile int* abort_flag = (volatile int*)(tbase_slot + 1);
   static_assert((STAGES * 2 + 5 + 2 * TQ) * 8 + TQ * 4 + 8 <= 256, "barriers fit the 256-byte tail");
 
-  const GemmArgs& g = *src.g;
   const uint32_t rank = (uint32_t)src.pair_rank;
   const bool lead = rank == 0;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -801,7 +809,9 @@ __device__ __forceinline__ void gemm_pair(const SingleTiles& src) {
     mbar_init(drain, 1);
     for (int s = 0; s < TQ; s++) {
       mbar_init(&tq_full[s], 1);
-      mbar_init(&tq_empty[s], lead ? 1 + EPI_WARPS : EPI_WARPS);  // the peer has no MMA thread
+      // consumers of a queue slot: the leader's MMA thread and both CTAs'
+      // epilogue warps and the peer's producer
+      mbar_init(&tq_empty[s], 2 * (1 + EPI_WARPS));
     }
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -816,8 +826,30 @@ __device__ __forceinline__ void gemm_pair(const SingleTiles& src) {
   cluster_sync();  // both CTAs' barriers are initialised before either signals the other's
   tc_fence_after();
   const uint32_t tbase = *tbase_slot;
-  const int deal_id = (int)(blockIdx.x >> 1), deal_n = (int)(gridDim.x >> 1);
-  const uint32_t lead_full = cluster_addr(full, 0);  // leader's full[0]; full[s] is 8 s bytes further
+  const uint32_t lead_full = cluster_addr(full, 0);          // full[s] is 8 s bytes further
+  const uint32_t lead_tq_empty = cluster_addr(tq_empty, 0);  // tq_empty[s] likewise
+  int* err = src.err();
+  const uint64_t wait_ns = src.wait_ns();
+
+  // Bounded wait with cluster-scope acquire, for the tile-queue barriers:
+  // their arrivals (and the queued index) may come from the other CTA.
+  auto cwait = [&](uint64_t* bar, uint32_t par, int site) -> bool {
+    const uint64_t t0 = globaltimer_ns();
+    for (uint32_t it = 0;; ++it) {
+      if (mbar_try_wait_cluster(bar, par)) return true;
+      if ((it & 63) == 63) {
+        if (*abort_flag || *(volatile int*)err) {
+          *abort_flag = 1;
+          return false;
+        }
+        if (globaltimer_ns() - t0 > wait_ns) {
+          *abort_flag = 1;
+          atomicCAS(err, 0, site);
+          return false;
+        }
+      }
+    }
+  };
 
   if (warp == 0) {
     if (lane == 0) {
@@ -829,22 +861,53 @@ __device__ __forceinline__ void gemm_pair(const SingleTiles& src) {
       bool ok = true;
       int tq = 0;
       uint32_t tqph = 0;
+      int last_prob = -1;
+      const bool dyn = src.dynamic();
+      const int deal_id = (int)(blockIdx.x >> 1), deal_n = (int)(gridDim.x >> 1);
       int kdeal = 0;
+      const uint32_t peer_tq_id = cluster_addr((const void*)tq_id, 1);
+      const uint32_t peer_tq_full = cluster_addr(tq_full, 1);
 #pragma unroll 1
       while (ok) {
-        const int base = kdeal * deal_n;
-        int it = base >= ntiles ? ntiles : base + ((kdeal & 1) ? deal_n - 1 - deal_id : deal_id);
-        kdeal++;
-        if (it >= ntiles) it = -1;
-        if (!mbar_wait(&tq_empty[tq], tqph ^ 1, abort_flag, g.err, 5, g.wait_ns)) { ok = false; break; }
-        tq_id[tq] = it;
-        mbar_arrive(&tq_full[tq]);
+        int it;
+        if (lead) {
+          // the leader picks the pair's next tile and publishes it to both CTAs
+          if (dyn) {
+            it = atomicAdd(tile_counter, 1);
+          } else {
+            const int base = kdeal * deal_n;
+            it = base >= ntiles ? ntiles : base + ((kdeal & 1) ? deal_n - 1 - deal_id : deal_id);
+            kdeal++;
+          }
+          if (it >= ntiles) it = -1;
+          if (!cwait(&tq_empty[tq], tqph ^ 1, 5)) { ok = false; break; }
+          tq_id[tq] = it;
+          asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(peer_tq_id + 4u * (uint32_t)tq), "r"(it) : "memory");
+          mbar_arrive(&tq_full[tq]);
+          mbar_arrive_cluster(peer_tq_full + 8u * (uint32_t)tq);  // release: the index is visible first
+        } else {
+          if (!cwait(&tq_full[tq], tqph, 9)) { ok = false; break; }
+          it = tq_id[tq];
+          mbar_arrive_cluster(lead_tq_empty + 8u * (uint32_t)tq);
+        }
         if (++tq == TQ) { tq = 0; tqph ^= 1; }
         if (it < 0) break;
         const TileRef T = src.tile(it);
+        if (T.skip) continue;
+        const GemmArgs& g = src.args(T.prob);
+        const CUtensorMap* tmA = src.mapA(T.prob);
+        const CUtensorMap* tmB = src.mapB(T.prob);
+        if (Src::global_maps && T.prob != last_prob) {
+          asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;" ::"l"((uint64_t)tmA) : "memory");
+          asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;" ::"l"((uint64_t)tmB) : "memory");
+          last_prob = T.prob;
+        }
         const int m0 = T.m_tile * BM, n0 = T.n_tile * BN;
         const int passes = (g.S + 1) / 2;
-        const int nk = g.Kpad / ROW;
+        int nk = g.Kpad / ROW;
+        // the pair's larger row tile decides the K extent of the zero-topped L^-1
+        const int top = ((T.m_tile | 1) + 1) * BM;
+        if (top <= g.tri_rows) nk = min(nk, (top + ROW - 1) / ROW);
 #pragma unroll 1
         for (int p = 0; p < passes && ok; p++) {
           const int s0 = 2 * p, s1 = 2 * p + 1;
@@ -856,9 +919,9 @@ __device__ __forceinline__ void gemm_pair(const SingleTiles& src) {
             uint8_t* sb = smem + stage * STAGE;
             const uint32_t fb = lead_full + 8u * (uint32_t)stage;
             if (lead) mbar_expect_tx(&full[stage], 2 * ((two ? 2 * A : A) + B));  // both CTAs' bytes
-            tma_load_2d_cg2(sb, src.tmA, kb * ROW, s0 * g.Mpad + m0, fb);
-            if (two) tma_load_2d_cg2(sb + A, src.tmA, kb * ROW, s1 * g.Mpad + m0, fb);
-            tma_load_2d_cg2(sb + 2 * A, src.tmB, kb * ROW, g.col0 + n0 + (int)rank * (BN / 2), fb);
+            tma_load_2d_cg2(sb, tmA, kb * ROW, s0 * g.Mpad + m0, fb);
+            if (two) tma_load_2d_cg2(sb + A, tmA, kb * ROW, s1 * g.Mpad + m0, fb);
+            tma_load_2d_cg2(sb + 2 * A, tmB, kb * ROW, g.col0 + n0 + (int)rank * (BN / 2), fb);
             issued[stage] = 1;
             issued_phase[stage] = phase;
             if (++stage == STAGES) { stage = 0; phase ^= 1; }
@@ -870,7 +933,7 @@ __device__ __forceinline__ void gemm_pair(const SingleTiles& src) {
         // no multicast commit is still on its way to this CTA
 #pragma unroll 1
         for (int i = 0; i < STAGES; i++) {
-          if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, g.err, 8, g.wait_ns)) break;
+          if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, err, 8, wait_ns)) break;
           if (++stage == STAGES) { stage = 0; phase ^= 1; }
         }
       } else if (lead) {
@@ -889,13 +952,18 @@ __device__ __forceinline__ void gemm_pair(const SingleTiles& src) {
       uint32_t tqph = 0;
 #pragma unroll 1
       while (ok) {
-        if (!mbar_wait(&tq_full[tq], tqph, abort_flag, g.err, 6, g.wait_ns)) { ok = false; break; }
+        if (!cwait(&tq_full[tq], tqph, 6)) { ok = false; break; }
         const int it = tq_id[tq];
         mbar_arrive(&tq_empty[tq]);
         if (++tq == TQ) { tq = 0; tqph ^= 1; }
         if (it < 0) break;
+        const TileRef T = src.tile(it);
+        if (T.skip) continue;
+        const GemmArgs& g = src.args(T.prob);
         const int passes = (g.S + 1) / 2;
-        const int nk = g.Kpad / ROW;
+        int nk = g.Kpad / ROW;
+        const int top = ((T.m_tile | 1) + 1) * BM;
+        if (top <= g.tri_rows) nk = min(nk, (top + ROW - 1) / ROW);
 #pragma unroll 1
         for (int p = 0; p < passes && ok; p++, q++) {
           const bool two = 2 * p + 1 < g.S;
@@ -960,10 +1028,10 @@ __device__ __forceinline__ void gemm_pair(const SingleTiles& src) {
     while (ok) {
       int it = 0, okq = 1;
       if (lane == 0) {
-        okq = mbar_wait(&tq_full[tq], tqph, abort_flag, g.err, 7, g.wait_ns) ? 1 : 0;
+        okq = cwait(&tq_full[tq], tqph, 7) ? 1 : 0;
         if (okq) {
           it = tq_id[tq];
-          mbar_arrive(&tq_empty[tq]);
+          mbar_arrive_cluster(lead_tq_empty + 8u * (uint32_t)tq);
         }
       }
       okq = __shfl_sync(0xffffffffu, okq, 0);
@@ -972,6 +1040,8 @@ __device__ __forceinline__ void gemm_pair(const SingleTiles& src) {
       if (++tq == TQ) { tq = 0; tqph ^= 1; }
       if (it < 0) break;
       const TileRef T = src.tile(it);
+      if (T.skip) continue;
+      const GemmArgs& g = src.args(T.prob);
       const int m0 = T.m_tile * BM, n0 = T.n_tile * BN;
       const int r = m0 + row;
       const bool rvalid = r < g.M;
@@ -984,7 +1054,6 @@ __device__ __forceinline__ void gemm_pair(const SingleTiles& src) {
       const int passes = (g.S + 1) / 2;
 #pragma unroll 1
       for (int p = 0; p < passes; p++, q++) {
-        const bool two = 2 * p + 1 < g.S;
         const bool last = p == passes - 1;
         const uint32_t buf = q & 1, par = (q >> 1) & 1;
         if (p > 0)
@@ -1021,15 +1090,36 @@ __device__ __forceinline__ void gemm_pair(const SingleTiles& src) {
     while (globaltimer_ns() - t0 < 100000ull) {
     }
   }
+  // the last CTA out zeroes the tile counters for the next launch (every CTA
+  // has then stopped fetching tiles)
+  if (threadIdx.x == 0 && tile_counter) {
+    __threadfence();
+    if (atomicAdd(tile_counter + 1, 1) == (int)gridDim.x - 1) {
+      atomicExch(tile_counter, 0);
+      atomicExch(tile_counter + 1, 0);
+    }
+  }
 }
 
-// 2-SM launch: clusters of two CTAs, one pair of SMs per cluster, at most as
-// many clusters as fit at once (tiles are dealt statically per cluster).
+// 2-SM launches: clusters of two CTAs, one pair of SMs per cluster, at most
+// as many clusters as fit at once.  Uniform tiles are dealt statically per
+// cluster, those of the triangular L^-1 operand (and of grouped problems)
+// taken from the launch-wide counter (two ints, zero before the first launch).
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
     ozaki_gemm2_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmBh,
-                       const __grid_constant__ GemmArgs g) {
+                       const __grid_constant__ GemmArgs g, int* tile_counter) {
   const SingleTiles src{&tmA, &tmBh, &g, (int)cluster_rank()};
-  gemm_pair(src);
+  gemm_pair(src, tile_counter);
+}
+
+// Many independent problems over a table of row-tile pairs; genotype maps in
+// 128-row boxes.
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
+    ozaki_grouped_gemm2_kernel(const GroupedTile* __restrict__ tiles, const GroupedProblem* __restrict__ probs,
+                               const CUtensorMap* __restrict__ maps, const int* __restrict__ cols, int ntiles,
+                               int* tile_counter) {
+  const GroupedTiles src{tiles, probs, maps, cols, ntiles, (int)cluster_rank()};
+  gemm_pair(src, tile_counter);
 }
 
 // Many independent problems in one persistent launch over a tile table;
@@ -1038,7 +1128,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     ozaki_grouped_gemm_kernel(const GroupedTile* __restrict__ tiles, const GroupedProblem* __restrict__ probs,
                               const CUtensorMap* __restrict__ maps, const int* __restrict__ cols, int ntiles,
                               int* tile_counter) {
-  const GroupedTiles src{tiles, probs, maps, cols, ntiles};
+  const GroupedTiles src{tiles, probs, maps, cols, ntiles, -1};
   gemm_persistent(src, tile_counter);
 }
 
@@ -1870,13 +1960,13 @@ cudaError_t run_gemm(OzakiPlan* p, cudaStream_t s, int col0, int x, int tri_rows
   g.ldc = p->Mpad;
   g.err = p->err;
   g.wait_ns = p->wait_ns;
-  // uniform tiles: the 2-SM kernel (pairs of row tiles share each genotype
-  // tile across two SMs); the triangular L^-1 operand: one CTA per tile,
-  // longest tiles first from the counter
+  // the 2-SM kernel (pairs of row tiles share each genotype tile across two
+  // SMs; the triangular L^-1 operand's pairs longest first from the counter),
+  // else one CTA per tile
   const int pairs = ((g.tiles_m + 1) / 2) * g.tiles_n;
-  const int clusters = (tri_rows == 0 && p->has_mapBh) ? pair_clusters() : 0;
+  const int clusters = p->has_mapBh ? pair_clusters() : 0;
   if (clusters > 0)
-    ozaki_gemm2_kernel<<<2 * std::min(pairs, clusters), THREADS, p2::SMEM, s>>>(p->mapA, p->mapBh, g);
+    ozaki_gemm2_kernel<<<2 * std::min(pairs, clusters), THREADS, p2::SMEM, s>>>(p->mapA, p->mapBh, g, p->err + 1);
   else
     ozaki_gemm_kernel<<<persistent_grid(g.tiles_m * g.tiles_n), THREADS, SMEM_BYTES, s>>>(p->mapA, p->mapB, g,
                                                                                           p->err + 1);
@@ -2119,6 +2209,7 @@ cudaError_t grouped_genotypes(cudaStream_t s, const GenoCohort* dgc, const StepC
 
 struct GroupedGemm {
   int ntiles = 0, nprob = 0;
+  bool pair = false;  // 2-SM kernel over row-tile pairs
   GroupedTile* tiles = nullptr;
   GroupedProblem* probs = nullptr;
   CUtensorMap* maps = nullptr;
@@ -2127,6 +2218,7 @@ struct GroupedGemm {
 
 cudaError_t grouped_gemm_create(GroupedGemm** out, const GroupedGemmDesc* d, int count, int x_b, int* err) {
   *out = nullptr;
+  const bool pair = pair_clusters() > 0;
   std::vector<GroupedProblem> probs(count);
   std::vector<CUtensorMap> maps(2 * (size_t)count);
   std::vector<int> order(count);
@@ -2151,7 +2243,7 @@ cudaError_t grouped_gemm_create(GroupedGemm** out, const GroupedGemmDesc* d, int
     probs[i].cohort = d[i].cohort;
     probs[i].pad = 0;
     FGLS_CUDA_TRY(make_map(&maps[2 * i], d[i].A, d[i].Kpad, (long long)d[i].S_alloc * d[i].Mpad, BM));
-    FGLS_CUDA_TRY(make_map(&maps[2 * i + 1], d[i].G, d[i].Kpad, d[i].Ncap, BN));
+    FGLS_CUDA_TRY(make_map(&maps[2 * i + 1], d[i].G, d[i].Kpad, d[i].Ncap, pair ? BN / 2 : BN));
     order[i] = i;
     work[i] = (long long)g.tiles_m * g.Kpad;
   }
@@ -2160,13 +2252,18 @@ cudaError_t grouped_gemm_create(GroupedGemm** out, const GroupedGemmDesc* d, int
   std::vector<GroupedTile> tiles;
   for (int i : order) {
     const GemmArgs& g = probs[i].g;
-    for (int first = 0; first < g.tiles_m; first += GROUP_M) {
-      const int gsz = std::min(GROUP_M, g.tiles_m - first);
+    // rows in units of tiles, or of tile pairs for the 2-SM kernel (an odd
+    // last pair's second tile lies past the operand and is never written)
+    const int units = pair ? (g.tiles_m + 1) / 2 : g.tiles_m;
+    const int gm = pair ? GROUP_M / 2 : GROUP_M;
+    for (int first = 0; first < units; first += gm) {
+      const int gsz = std::min(gm, units - first);
       for (int nt = 0; nt < g.tiles_n; nt++)
         for (int m = 0; m < gsz; m++) tiles.push_back(GroupedTile{i, first + m, nt, 0});
     }
   }
   GroupedGemm* gg = new GroupedGemm();
+  gg->pair = pair;
   gg->ntiles = (int)tiles.size();
   gg->nprob = count;
   cudaError_t r = cudaSuccess;
@@ -2188,6 +2285,8 @@ cudaError_t grouped_gemm_create(GroupedGemm** out, const GroupedGemmDesc* d, int
   if (r == cudaSuccess)
     chk(cudaFuncSetAttribute(ozaki_grouped_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              SMEM_BYTES));
+  if (r == cudaSuccess && pair)
+    chk(cudaFuncSetAttribute(ozaki_grouped_gemm2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, p2::SMEM));
   if (r != cudaSuccess) {
     grouped_gemm_destroy(gg);
     return r;
@@ -2198,8 +2297,12 @@ cudaError_t grouped_gemm_create(GroupedGemm** out, const GroupedGemmDesc* d, int
 
 cudaError_t grouped_gemm_run(GroupedGemm* gg, cudaStream_t s, const int* dcols) {
   if (gg->ntiles == 0) return cudaSuccess;
-  ozaki_grouped_gemm_kernel<<<persistent_grid(gg->ntiles), THREADS, SMEM_BYTES, s>>>(
-      gg->tiles, gg->probs, gg->maps, dcols, gg->ntiles, gg->counter);
+  if (gg->pair)
+    ozaki_grouped_gemm2_kernel<<<2 * std::min(gg->ntiles, pair_clusters()), THREADS, p2::SMEM, s>>>(
+        gg->tiles, gg->probs, gg->maps, dcols, gg->ntiles, gg->counter);
+  else
+    ozaki_grouped_gemm_kernel<<<persistent_grid(gg->ntiles), THREADS, SMEM_BYTES, s>>>(
+        gg->tiles, gg->probs, gg->maps, dcols, gg->ntiles, gg->counter);
   note_launch();
   return cudaGetLastError();
 }
