@@ -935,8 +935,9 @@ def run_eigen(args, rank, world, local, dist):
     eng.set_problem(Phi, XL, Y, h, s)
     setup_s = time.perf_counter() - t0
     S_used, S_err = eng.split_params()
+    QD_used = eng.quad_digits()
     log(f"[bench] rank {rank}: data {gen_s:.1f}s, setup (eigendecomposition + operands) {setup_s:.1f}s, "
-        f"slices {S_used} (probe err {S_err:.2e})")
+        f"slices {S_used}, quadratic-Gram digits {QD_used} (probe err {S_err:.2e})")
 
     pool = [genotype_block(xb, n, sd, dev) for sd in rank_block_seeds(rank, args.pool)]
     torch.cuda.synchronize()  # the engine's streams do not wait for torch's
@@ -1117,9 +1118,10 @@ def run_eigen(args, rank, world, local, dist):
         "config": {
             "workload": f"fgls_eigen split-precision, n={n} p=4 t={t}, job m={M_JOB} SNPs, "
                         f"steps of x_b={xb} SNPs x {t} traits",
-            "n": n, "t": t, "p": 4, "m_job": M_JOB, "x_b": xb, "slices": S_used,
-            "slices_choice": ("autotuned: smallest of 6..9 within 1e-10/8 of the FP64 path on a 256-SNP probe "
-                              f"block (probe beta error {S_err:.2e})" if args.slices == 0 else "given"),
+            "n": n, "t": t, "p": 4, "m_job": M_JOB, "x_b": xb, "slices": S_used, "quad_digits": QD_used,
+            "slices_choice": ("autotuned: smallest of 6..9 slices, then of 8..11 quadratic-Gram digits, within "
+                              f"1e-10/8 of the FP64 path on a 256-SNP probe block (probe beta error {S_err:.2e})"
+                              if args.slices == 0 else "given"),
             "genotype_input": "FP64 reference layout, resident in HBM",
             "l2": f"inputs larger than L2: {len(pool)} distinct {xb * n * 8 / 1e9:.2f} GB blocks cycled",
             "setup_s": setup_s, "job_s_estimate": M_JOB * t / value + setup_s,

@@ -324,10 +324,12 @@ __global__ void probe_genotypes_kernel(int n, int x, double* __restrict__ out) {
 // digit slices; a probe block of 256 SNPs runs through the all-FP64 path and
 // through the split path with the first 6, 7, 8 and 9 slices, and the
 // smallest count whose beta (normwise per trait and SNP) is within
-// TUNE_TOL / 8 of the FP64 result is kept.  Called after every build of the
-// split operands (they depend on the trait's weights or factor).
+// TUNE_TOL / 8 of the FP64 result is kept.  Then, with that slice count, the
+// tensor-core quadratic Gram's base-32 digits a side (eigen, t >= 33) are
+// chosen the same way from 8..11.  Called after every build of the split
+// operands (they depend on the trait's weights or factor).
 constexpr double TUNE_TOL = 1e-10;
-constexpr int TUNE_SNPS = 256, TUNE_MIN_SLICES = 6;
+constexpr int TUNE_SNPS = 256, TUNE_MIN_SLICES = 6, TUNE_MIN_QDIGITS = 8;
 
 int tune_slices(fglsgpu_engine* e) {
   fglsgpu_config& c = e->cfg;
@@ -376,16 +378,14 @@ int tune_slices(fglsgpu_engine* e) {
   std::vector<double> Br((size_t)nt * xp * p), Bs(Br.size());
   if (!rc && cudaMemcpyAsync(Br.data(), dBr, sizeof(double) * Br.size(), cudaMemcpyDeviceToHost, s) != cudaSuccess)
     rc = fail(e, FGLSGPU_ECUDA, "slice probe copy");
-  int chosen = built;
-  double err = -1.0;
-  for (int S = std::min(TUNE_MIN_SLICES, built); S <= built && !rc; S++) {
-    ENG_TRY(e, ozaki_set_run_slices(e->oz, s, S), "slice probe");
-    rc = compute_block(e, dX, GENO_F64, xp, dBs, dVs, (long long)xp * p, (long long)xp * p * p, 0);
-    if (rc) break;
-    ENG_TRY(e, cudaMemcpyAsync(Bs.data(), dBs, sizeof(double) * Bs.size(), cudaMemcpyDeviceToHost, s),
-            "slice probe copy");
-    ENG_TRY(e, cudaStreamSynchronize(s), "slice probe");
-    double worst = 0.0;
+  // the probe block through the split path as configured: worst beta error
+  auto probe = [&](double* worst) -> int {
+    int q_rc = compute_block(e, dX, GENO_F64, xp, dBs, dVs, (long long)xp * p, (long long)xp * p * p, 0);
+    if (q_rc) return q_rc;
+    if (cudaMemcpyAsync(Bs.data(), dBs, sizeof(double) * Bs.size(), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+      return fail(e, FGLSGPU_ECUDA, "slice probe copy");
+    double w = 0.0;
     for (size_t q = 0; q < Br.size(); q += p) {
       double d2 = 0.0, r2 = 0.0;
       for (int k = 0; k < p; k++) {
@@ -394,13 +394,40 @@ int tune_slices(fglsgpu_engine* e) {
         r2 += Br[q + k] * Br[q + k];
       }
       const double rel = r2 > 0.0 ? std::sqrt(d2 / r2) : std::sqrt(d2);
-      worst = (rel > worst || rel != rel) ? rel : worst;
+      w = (rel > w || rel != rel) ? rel : w;
     }
+    *worst = w;
+    return FGLSGPU_OK;
+  };
+  const int qbuilt = ozaki_quad_digits(e->oz);  // 0: no tensor-core quadratic Gram
+  int chosen = built;
+  double err = -1.0;
+  for (int S = std::min(TUNE_MIN_SLICES, built); S <= built && !rc; S++) {
+    ENG_TRY(e, ozaki_set_run_slices(e->oz, s, S), "slice probe");
+    double worst = 0.0;
+    rc = probe(&worst);
+    if (rc) break;
     err = worst;
     if (worst <= TUNE_TOL / 8) {
       chosen = S;
       break;
     }
+  }
+  int qchosen = qbuilt;
+  if (!rc && qbuilt > 0) {
+    ENG_TRY(e, ozaki_set_run_slices(e->oz, s, chosen), "slice choice");
+    for (int k = std::min(TUNE_MIN_QDIGITS, qbuilt); k < qbuilt && !rc; k++) {
+      ozaki_set_quad_digits(e->oz, k);
+      double worst = 0.0;
+      rc = probe(&worst);
+      if (rc) break;
+      if (worst <= TUNE_TOL / 8) {
+        qchosen = k;
+        err = worst;
+        break;
+      }
+    }
+    ozaki_set_quad_digits(e->oz, qchosen);
   }
   release();
   if (!rc) rc = check_status(e, "slice probe");
@@ -821,6 +848,12 @@ int fglsgpu_set_precision(fglsgpu_engine* e, int precision) {
     if (rc) return rc;
   }
   if (c.variant == FGLSGPU_VARIANT_CHOL) e->trait_sel = -1;  // re-select: the operands differ per path
+  return FGLSGPU_OK;
+}
+
+int fglsgpu_quad_digits(fglsgpu_engine* e, int* digits) {
+  if (!e || !digits) return fail(e, FGLSGPU_EINVAL, "null argument");
+  *digits = e->oz ? ozaki_quad_digits(e->oz) : 0;
   return FGLSGPU_OK;
 }
 

@@ -693,7 +693,6 @@ __device__ __forceinline__ void gemm_persistent(const Src& src, int* tile_counte
       const int passes = (g.S + 1) / 2;
 #pragma unroll 1
       for (int p = 0; p < passes; p++, q++) {
-        const bool two = 2 * p + 1 < g.S;
         const bool last = p == passes - 1;
         const uint32_t buf = q & 1, par = (q >> 1) & 1;
         // pull this row's partial sums (written a pass ago, since evicted by
@@ -1803,7 +1802,8 @@ struct OzakiPlan {
   int sms = 0;                  // SM count of the device
   // tensor-core quadratic Gram (eigen, 33 <= t <= 112): digit operands
   bool tq = false;
-  int SQ = 11;                    // digits per side; pairs with s + t <= SQ + 1
+  int SQ = 11;                    // digits per side built (trait digits); pairs with s + t <= SQ_run + 1
+  int SQ_run = 11;                // digits per side in use (1..SQ)
   int Kq = 0;                     // digit row length (bytes): n rounded up to QT_KB
   int tgp = 0;                    // trait rows per digit plane (multiple of QT_TP)
   double* qpart = nullptr;        // QT_SLOTS x Ncap x tgp partial planes of the tensor-core Gram
@@ -1824,6 +1824,20 @@ struct OzakiPlan {
   double* scale_run = nullptr;      // Mpad row scales for S_run slices (when S_run < S)
   unsigned long long wait_ns = WAIT_NS;  // limit of one wait in the tcgen05 kernels
 };
+
+// Passes of the tensor-core quadratic Gram for k digits a side: one SNP
+// digit s with up to four trait digits t, s + t <= k + 1.  Round-to-nearest
+// base-32 digits, so the first k of the SQ digits built are the k-digit cut.
+static void quad_passes(OzakiPlan* p, int k) {
+  p->SQ_run = k;
+  memset(&p->qp, 0, sizeof(p->qp));
+  for (int sd = 1; sd <= k; sd++)
+    for (int t0 = 1; t0 <= k + 1 - sd; t0 += 4) {
+      const int q0 = p->qp.n++;
+      p->qp.s[q0] = (signed char)sd;
+      for (int q = 0; q < 4; q++) p->qp.t[q0][q] = (signed char)(t0 + q <= k + 1 - sd ? t0 + q : 0);
+    }
+}
 
 cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_b, int slices, int eigen) {
   *out = nullptr;
@@ -1896,14 +1910,7 @@ cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_
     if (r == cudaSuccess) chk(make_map_u8(&p->mapDd, p->Ddig, p->Kq, (long long)p->SQ * p->tgp, QT_TP));
     if (r == cudaSuccess)
       chk(cudaFuncSetAttribute(quadtc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, QT_SMEM));
-    // passes: one SNP digit s with up to four trait digits t, s + t <= SQ + 1
-    memset(&p->qp, 0, sizeof(p->qp));
-    for (int sd = 1; sd <= p->SQ; sd++)
-      for (int t0 = 1; t0 <= p->SQ + 1 - sd; t0 += 4) {
-        const int k = p->qp.n++;
-        p->qp.s[k] = (signed char)sd;
-        for (int q = 0; q < 4; q++) p->qp.t[k][q] = (signed char)(t0 + q <= p->SQ + 1 - sd ? t0 + q : 0);
-      }
+    quad_passes(p, p->SQ);
   }
   // the memsets above ran on the legacy default stream, which does not order
   // against the caller's non-blocking streams: finish them before any launch
@@ -1995,7 +2002,7 @@ cudaError_t selfgram(OzakiPlan* p, cudaStream_t s, int col0, int xq, int t, doub
   if (!p->tq || col0 != 0)
     return quad_gram(s, p->n, xq, t, A, p->Mpad, p->amax + col0, p->D, p->n, p->dmax, p->part, GR + col0, ldg,
                      p->sms);
-  snp_digits_kernel<<<xq, QD_THREADS, 0, s>>>(p->n, A, p->Mpad, p->SQ, p->Ncap, p->Kq, p->Adig, p->aexp);
+  snp_digits_kernel<<<xq, QD_THREADS, 0, s>>>(p->n, A, p->Mpad, p->SQ_run, p->Ncap, p->Kq, p->Adig, p->aexp);
   note_launch();
   QuadArgs g;
   g.x = xq;
@@ -2190,6 +2197,13 @@ cudaError_t ozaki_set_run_slices(OzakiPlan* p, cudaStream_t s, int S) {
   rescale_rows_kernel<<<(p->Mpad + 255) / 256, 256, 0, s>>>(p->Mpad, p->scale, 10 * dpass, p->scale_run);
   note_launch();
   return cudaGetLastError();
+}
+
+int ozaki_quad_digits(const OzakiPlan* p) { return p && p->tq ? p->SQ_run : 0; }
+
+void ozaki_set_quad_digits(OzakiPlan* p, int k) {
+  if (!p || !p->tq) return;
+  quad_passes(p, std::max(1, std::min(k, p->SQ)));
 }
 
 int ozaki_slices(const OzakiPlan* p, int* built) {

@@ -55,6 +55,10 @@ int* ozaki_error_word(OzakiPlan* p);
 cudaError_t ozaki_set_run_slices(OzakiPlan* p, cudaStream_t s, int S);
 // Slices in use; *built (may be null) receives the slices the operand holds.
 int ozaki_slices(const OzakiPlan* p, int* built);
+// base-32 digits a side of the tensor-core quadratic Gram in use (0 when the
+// plan does not use it), and setting them (1..11; fewer digits, fewer passes)
+int ozaki_quad_digits(const OzakiPlan* p);
+void ozaki_set_quad_digits(OzakiPlan* p, int k);
 // Limit of one pipeline wait in the plan's tcgen05 kernels (0: 2 s).
 void ozaki_set_wait_limit(OzakiPlan* p, unsigned long long ns);
 

@@ -43,7 +43,7 @@ EXPORTS = (
     "fglsgpu_batch_sync", "fglsgpu_batch_stream", "fglsgpu_batch_last_error", "fglsgpu_batch_profile",
     "fglsgpu_batch_profile_read", "fglsgpu_run_block_device_packed", "fglsgpu_run_snps_compact",
     "fglsgpu_reml_fit", "fglsgpu_set_hsigma", "fglsgpu_set_wait_limit", "fglsgpu_run_snps_u8",
-    "fglsgpu_run_snps_packed", "fglsgpu_split_params",
+    "fglsgpu_run_snps_packed", "fglsgpu_split_params", "fglsgpu_quad_digits",
 )
 PROF_CLASSES = ("genotypes", "split_gemm", "selfgram", "solve", "fp64_gemm", "trsm", "gram", "spare")
 
@@ -116,6 +116,7 @@ def lib():
     L.fglsgpu_set_hsigma.argtypes = [P, P, P]
     L.fglsgpu_set_wait_limit.argtypes = [P, LL]
     L.fglsgpu_split_params.argtypes = [P, C.POINTER(I), C.POINTER(C.c_double)]
+    L.fglsgpu_quad_digits.argtypes = [P, C.POINTER(I)]
     L.fglsgpu_pvalues_device.argtypes = [P, P, P, I, LL, LL, P, LL]
     L.fglsgpu_batch_create.argtypes = [C.POINTER(CohortDesc), I, C.POINTER(BatchConfig), C.POINTER(P)]
     L.fglsgpu_batch_destroy.argtypes = [P]
@@ -237,6 +238,12 @@ class Engine:
         sl, err = C.c_int(), C.c_double()
         self._check(self.L.fglsgpu_split_params(self._h, C.byref(sl), C.byref(err)))
         return sl.value, err.value
+
+    def quad_digits(self):
+        """Base-32 digits a side of the tensor-core quadratic Gram in use (0: off)."""
+        d = C.c_int()
+        self._check(self.L.fglsgpu_quad_digits(self._h, C.byref(d)))
+        return d.value
 
     def set_wait_limit(self, ns=0):
         """Limit of one tcgen05 pipeline wait in ns (0: the 2 s default)."""

@@ -243,6 +243,13 @@ int fglsgpu_set_precision(fglsgpu_engine *e, int precision);
  * otherwise).  No counterpart in the reference. */
 int fglsgpu_split_params(fglsgpu_engine *e, int *slices, double *probe_err);
 
+/* Base-32 digits a side that the split eigen path's tensor-core quadratic
+ * Gram uses (t >= 33; 0 when that path is off).  With cfg.slices == 0 the
+ * probe block also chooses them, the smallest count in 8..11 whose beta stays
+ * within 1e-10 / 8 of the FP64 path (after the slice choice); else 11.  No
+ * reference counterpart (the reference has no split path). */
+int fglsgpu_quad_digits(fglsgpu_engine *e, int *digits);
+
 /* Limit of one pipeline wait (on an mbarrier: a TMA copy landing, an MMA
  * finishing, an epilogue draining TMEM) inside the split path's tcgen05
  * kernels, in nanoseconds; 0 restores the default of 2 s.  A wait that
