@@ -140,17 +140,26 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volati
   const uint64_t t0 = globaltimer_ns();
   for (uint32_t it = 0;; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
-    if ((it & 63) == 63) {
-      if (*abort_flag || *(volatile int*)err) {
-        *abort_flag = 1;
-        return false;
-      }
-      if (globaltimer_ns() - t0 > limit_ns) {
-        *abort_flag = 1;
-        atomicCAS(err, 0, site);
-        return false;
-      }
+    // the clock after the first miss (a short limit takes effect at once)
+    // and every 64; the error words, which cost a memory load, every 64
+    const bool every = (it & 63) == 63;
+    if (every && (*abort_flag || *(volatile int*)err)) {
+      *abort_flag = 1;
+      return false;
     }
+    if ((every || it == 0) && globaltimer_ns() - t0 > limit_ns) {
+      *abort_flag = 1;
+      atomicCAS(err, 0, site);
+      return false;
+    }
+  }
+}
+
+// Drain wait of a CTA pair's leader on the abort path: one deadline for all
+// its stages (a stage may never complete when the peer gave up before its
+// copies; the leader's own copies land within microseconds).
+__device__ __forceinline__ void mbar_drain_until(uint64_t* bar, uint32_t parity, uint64_t deadline) {
+  while (!mbar_try_wait(bar, parity) && globaltimer_ns() < deadline) {
   }
 }
 
@@ -836,16 +845,15 @@ __device__ __forceinline__ void gemm_pair(const Src& src, int* tile_counter) {
     const uint64_t t0 = globaltimer_ns();
     for (uint32_t it = 0;; ++it) {
       if (mbar_try_wait_cluster(bar, par)) return true;
-      if ((it & 63) == 63) {
-        if (*abort_flag || *(volatile int*)err) {
-          *abort_flag = 1;
-          return false;
-        }
-        if (globaltimer_ns() - t0 > wait_ns) {
-          *abort_flag = 1;
-          atomicCAS(err, 0, site);
-          return false;
-        }
+      const bool every = (it & 63) == 63;  // as in mbar_wait
+      if (every && (*abort_flag || *(volatile int*)err)) {
+        *abort_flag = 1;
+        return false;
+      }
+      if ((every || it == 0) && globaltimer_ns() - t0 > wait_ns) {
+        *abort_flag = 1;
+        atomicCAS(err, 0, site);
+        return false;
       }
     }
   };
@@ -937,8 +945,9 @@ __device__ __forceinline__ void gemm_pair(const Src& src, int* tile_counter) {
         }
       } else if (lead) {
         // the leader's barrier tracks both CTAs' copies of every stage it armed
+        const uint64_t deadline = globaltimer_ns() + WAIT_NS;
         for (int s = 0; s < STAGES; s++)
-          if (issued[s]) mbar_drain(&full[s], issued_phase[s]);
+          if (issued[s]) mbar_drain_until(&full[s], issued_phase[s], deadline);
       }
     }
   } else if (warp == 1) {
@@ -972,8 +981,10 @@ __device__ __forceinline__ void gemm_pair(const Src& src, int* tile_counter) {
             const uint64_t t0 = globaltimer_ns();
             uint32_t spin = 0;
             while (!mbar_try_wait_cluster(&tempty[buf], par ^ 1)) {
-              if ((++spin & 63) == 0 &&
-                  (*abort_flag || *(volatile int*)g.err || globaltimer_ns() - t0 > g.wait_ns)) {
+              const bool every = (spin & 63) == 63, first = spin == 0;  // as in mbar_wait
+              spin++;
+              if ((every && (*abort_flag || *(volatile int*)g.err)) ||
+                  ((every || first) && globaltimer_ns() - t0 > g.wait_ns)) {
                 *abort_flag = 1;
                 atomicCAS(g.err, 0, 2);
                 ok = false;
@@ -1397,15 +1408,267 @@ __global__ void __launch_bounds__(THREADS, 1)
   if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(512) : "memory");
 }
 
-// GR[i + j ldg] = sum over the CTAs that covered tile (i / 128, j / 112) of
-// their partial planes, in slot order (deterministic).
+// ---------------------------------------------------------------------------
+// 2-SM tensor-core quadratic Gram: a cluster of two CTAs computes 256 SNP
+// rows (rank r: rows 128 r .. 128 r + 127 of the pair tile) of one 112-trait
+// group per unit, with tcgen05.mma.cta_group::2 (M = 256) issued by the
+// leader.  An MMA over the slot pair (2q, 2q + 1) (N = 224) takes trait
+// digit slot 2q + r from CTA r (112 rows); with the pair's second slot empty
+// (N = 112) each CTA holds 56 rows of slot 2q.  Per CTA a stage is the SNP
+// digit tile (16 KB) and two trait tiles (2 x 14 KB): 44 KB, five stages;
+// the accumulator layout in each CTA's TMEM and the epilogue are those of
+// quadtc_kernel.  Units are dealt to clusters in contiguous ranges; full[s]
+// and tempty live in the leader, empty[s] and tfull in both CTAs.
+// ---------------------------------------------------------------------------
+constexpr int QT2_STAGES = 5;
+constexpr int QT2_STAGE = A_TILE + 2 * QT_BT;  // 44 KB
+constexpr int QT2_SMEM = QT2_STAGES * QT2_STAGE + 1024 + 256;
+constexpr uint32_t QT2_IDESC = (1u << 4) | ((uint32_t)(224 >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
+constexpr uint32_t QT2_IDESC1 = (1u << 4) | ((uint32_t)(QT_TP >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
+
+// Partial plane of pair tile `tl` from this cluster (slot = this cluster -
+// the tile's first owner): the thread's SNP row and 56 traits, scaled to FP64.
+__device__ __forceinline__ void quadtc2_flush(const QuadArgs& g, int tl, int np, int rank, int q, int lane, int jl,
+                                              const float (&H)[56], const float (&L)[56]) {
+  const int i = (tl / g.groups) * (2 * BM) + rank * BM + q * 32 + lane;
+  const int jh = (tl % g.groups) * QT_TP + jl;
+  const int slot = (int)(blockIdx.x >> 1) - qt_owner(tl * np, g.units, gridDim.x >> 1);
+  if (i >= g.x) return;
+  const double si = ldexp(1.0, g.aexp[i]);
+  double* P = g.part + (size_t)slot * g.Ncap * g.tgp;
+#pragma unroll
+  for (int c = 0; c < 56; c++) {
+    const int j = jh + c;
+    if (j < g.t) P[i + (size_t)j * g.Ncap] = ((double)H[c] + (double)L[c]) * si * ldexp(1.0, g.dexp[j]);
+  }
+}
+
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
+    quadtc2_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmD,
+                   const __grid_constant__ CUtensorMap tmD56, const __grid_constant__ QuadPasses qp,
+                   const QuadArgs g) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + QT2_STAGES * QT2_STAGE);  // [QT2_STAGES], used in the leader
+  uint64_t* empty = full + QT2_STAGES;                           // [QT2_STAGES]
+  uint64_t* tfull = empty + QT2_STAGES;
+  uint64_t* tempty = tfull + 1;  // used in the leader
+  uint64_t* drain = tempty + 1;
+  uint32_t* tbase_slot = (uint32_t*)(drain + 1);
+  volatile int* abort_flag = (volatile int*)(tbase_slot + 1);
+  static_assert((QT2_STAGES * 2 + 3) * 8 + 8 <= 256, "barriers fit the 256-byte tail");
+
+  const uint32_t rank = cluster_rank();
+  const bool lead = rank == 0;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nk = g.Kq / QT_KB;
+  const int np = qp.n;
+  const int cid = (int)(blockIdx.x >> 1), ncl = (int)(gridDim.x >> 1);
+  const int u0 = qt_range_begin(cid, g.units, ncl);
+  const int u1 = qt_range_begin(cid + 1, g.units, ncl);
+  const uint16_t BOTH = 0x3;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < QT2_STAGES; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(tfull, 1);
+    mbar_init(tempty, 2 * 8);  // one arrival per epilogue warp of both CTAs
+    mbar_init(drain, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {  // one warp of each CTA allocates the same columns in both
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tbase_slot)),
+                 "r"(512)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  cluster_sync();
+  tc_fence_after();
+  const uint32_t tbase = *tbase_slot;
+  const uint32_t lead_full = cluster_addr(full, 0);
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      int issued[QT2_STAGES];
+      uint32_t issued_phase[QT2_STAGES];
+      for (int s = 0; s < QT2_STAGES; s++) issued[s] = 0;
+      bool ok = true;
+      for (int u = u0; u < u1 && ok; u++) {
+        const int tile = u / np, p = u - tile * np;
+        const int m0 = (tile / g.groups) * (2 * BM) + (int)rank * BM, grp = tile % g.groups;
+        // this CTA's bytes of a K-step: the SNP digit tile, then per slot
+        // pair its slot 2q + rank (both slots present) or its 56-row half
+        // of slot 2q (second slot empty)
+        int bytes = A_TILE;
+        for (int pq = 0; pq < 2; pq++)
+          if (qp.t[p][2 * pq] > 0) bytes += qp.t[p][2 * pq + 1] > 0 ? QT_BT : QT_BT / 2;
+        for (int kb = 0; kb < nk; kb++) {
+          if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, g.err, 11, g.wait_ns)) { ok = false; break; }
+          issued[stage] = 0;
+          uint8_t* sb = smem + stage * QT2_STAGE;
+          const uint32_t fb = lead_full + 8u * (uint32_t)stage;
+          if (lead) mbar_expect_tx(&full[stage], 2 * bytes);  // both CTAs' copies
+          tma_load_2d_cg2(sb, &tmA, kb * QT_KB, (qp.s[p] - 1) * g.Ncap + m0, fb);
+          for (int pq = 0; pq < 2; pq++) {
+            const int t0 = qp.t[p][2 * pq], t1 = qp.t[p][2 * pq + 1];
+            if (t0 <= 0) continue;
+            uint8_t* db = sb + A_TILE + pq * QT_BT;
+            if (t1 > 0)
+              tma_load_2d_cg2(db, &tmD, kb * QT_KB, ((rank ? t1 : t0) - 1) * g.tgp + grp * QT_TP, fb);
+            else
+              tma_load_2d_cg2(db, &tmD56, kb * QT_KB, (t0 - 1) * g.tgp + grp * QT_TP + (int)rank * (QT_TP / 2),
+                              fb);
+          }
+          issued[stage] = 1;
+          issued_phase[stage] = phase;
+          if (++stage == QT2_STAGES) { stage = 0; phase ^= 1; }
+        }
+      }
+      if (ok) {
+        // every stage filled so far has been released by the leader's MMAs:
+        // no multicast commit is still on its way to this CTA
+#pragma unroll 1
+        for (int i = 0; i < QT2_STAGES; i++) {
+          if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, g.err, 15, g.wait_ns)) break;
+          if (++stage == QT2_STAGES) { stage = 0; phase ^= 1; }
+        }
+      } else if (lead) {
+        const uint64_t deadline = globaltimer_ns() + WAIT_NS;
+        for (int s = 0; s < QT2_STAGES; s++)
+          if (issued[s]) mbar_drain_until(&full[s], issued_phase[s], deadline);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0 && lead) {
+      int stage = 0;
+      uint32_t phase = 0;
+      bool ok = true, any = false;
+      for (int u = u0; u < u1 && ok; u++) {
+        const int lu = u - u0;
+        const int p = u % np;
+        const bool second = qp.t[p][2] > 0;
+        const uint32_t id01 = qp.t[p][1] > 0 ? QT2_IDESC : QT2_IDESC1;
+        const uint32_t id23 = qp.t[p][3] > 0 ? QT2_IDESC : QT2_IDESC1;
+        {  // both CTAs' epilogues have drained the accumulators
+          const uint64_t t0 = globaltimer_ns();
+          uint32_t spin = 0;
+          while (!mbar_try_wait_cluster(tempty, (lu & 1) ^ 1)) {
+            const bool every = (spin & 63) == 63, first = spin == 0;  // as in mbar_wait
+            spin++;
+            if ((every && (*abort_flag || *(volatile int*)g.err)) ||
+                ((every || first) && globaltimer_ns() - t0 > g.wait_ns)) {
+              *abort_flag = 1;
+              atomicCAS(g.err, 0, 12);
+              ok = false;
+              break;
+            }
+          }
+          if (!ok) break;
+        }
+        tc_fence_after();
+        for (int kb = 0; kb < nk; kb++) {
+          if (!mbar_wait(&full[stage], phase, abort_flag, g.err, 13, g.wait_ns)) { ok = false; break; }
+          tc_fence_after();
+          uint8_t* sb = smem + stage * QT2_STAGE;
+          const uint64_t a = desc_sw128(sb), b01 = desc_sw128(sb + A_TILE), b23 = desc_sw128(sb + A_TILE + QT_BT);
+#pragma unroll
+          for (int k = 0; k < QT_KB / 32; k++) {  // K = 32 one-byte digits per MMA
+            const uint64_t koff = (uint64_t)((k * 32) >> 4);
+            const uint32_t acc = (kb > 0 || k > 0) ? 1u : 0u;
+            mma_f8_cg2(tbase, a + koff, b01 + koff, id01, acc);
+            if (second) mma_f8_cg2(tbase + 224, a + koff, b23 + koff, id23, acc);
+          }
+          any = true;
+          mma_commit_cg2(&empty[stage], BOTH);
+          if (++stage == QT2_STAGES) { stage = 0; phase ^= 1; }
+        }
+        if (!ok) break;
+        mma_commit_cg2(tfull, BOTH);
+      }
+      if (!ok && any) {
+        mma_commit_cg2(drain, 0x1);
+        mbar_drain(drain, 0);
+      }
+    }
+    __syncwarp();
+  } else {
+    // epilogue: as in quadtc_kernel, over this CTA's 128 SNP rows
+    const int q = warp & 3;
+    const int jl = ((warp - 2) >> 2) * 56;
+    const uint32_t lead_tempty = cluster_addr(tempty, 0);
+    float H[56], L[56];
+    bool done = true;
+    for (int u = u0; u < u1 && done;) {
+      const int tile = u / np;
+      const int uend = min(u1, (tile + 1) * np);
+#pragma unroll
+      for (int c = 0; c < 56; c++) H[c] = L[c] = 0.0f;
+      for (; u < uend; u++) {
+        const int lu = u - u0;
+        const int p = u - tile * np;
+        int ok = 1;
+        if (lane == 0) ok = mbar_wait(tfull, lu & 1, abort_flag, g.err, 14, g.wait_ns) ? 1 : 0;
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (!ok) { done = false; break; }
+        tc_fence_after();
+#pragma unroll 1
+        for (int slot = 0; slot < 4; slot++) {
+          const int tt = qp.t[p][slot];
+          if (tt <= 0) continue;
+          const float w = __int_as_float((127 - 5 * (qp.s[p] + tt)) << 23);  // 32^-(s+t)
+          const uint32_t col = (uint32_t)((slot >> 1) * 224 + (slot & 1) * QT_TP + jl);
+          const uint32_t ta = tbase + ((uint32_t)(q * 32) << 16) + col;
+#pragma unroll
+          for (int c8 = 0; c8 < 7; c8++) {
+            uint32_t v[8];
+            tmem_ld8(ta + c8 * 8, v);
+            tmem_ld_wait();
+#pragma unroll
+            for (int e8 = 0; e8 < 8; e8++) {
+              const float x = __fmul_rn(__uint_as_float(v[e8]), w);
+              float s2, e;
+              two_sum_f(H[c8 * 8 + e8], x, s2, e);
+              H[c8 * 8 + e8] = s2;
+              L[c8 * 8 + e8] = __fadd_rn(L[c8 * 8 + e8], e);
+            }
+          }
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive_cluster(lead_tempty);
+      }
+      if (done) quadtc2_flush(g, tile, np, (int)rank, q, lane, jl, H, L);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  cluster_sync();  // the leader's MMAs into both CTAs' TMEM are complete
+  tc_fence_after();
+  if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(512) : "memory");
+  cluster_sync();
+  if (*abort_flag) {
+    const uint64_t t0 = globaltimer_ns();
+    while (globaltimer_ns() - t0 < 100000ull) {
+    }
+  }
+}
+
+// GR[i + j ldg] = sum over the CTAs (or CTA pairs) that covered tile
+// (i / rows, j / 112) of their partial planes, in slot order (deterministic).
 __global__ void __launch_bounds__(256) quadtc_combine_kernel(int x, int t, int Ncap, int tgp, int groups, int np,
-                                                             int units, int ctas, const double* __restrict__ part,
+                                                             int units, int ctas, int rows,
+                                                             const double* __restrict__ part,
                                                              double* __restrict__ GR, long long ldg) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (long long)x * t) return;
   const int i = (int)(idx % x), j = (int)(idx / x);
-  const int tile = (i / BM) * groups + j / QT_TP;
+  const int tile = (i / rows) * groups + j / QT_TP;
   const int first = qt_owner(tile * np, units, ctas), last = qt_owner(tile * np + np - 1, units, ctas);
   double v = 0.0;
   for (int c = first; c <= last; c++) v += part[(size_t)(c - first) * Ncap * tgp + i + (size_t)j * Ncap];
@@ -1811,6 +2074,7 @@ struct OzakiPlan {
   uint8_t* Ddig = nullptr;        // SQ x tgp x Kq trait digits (E4M3)
   int *aexp = nullptr, *dexp = nullptr;
   CUtensorMap mapAd, mapDd;
+  CUtensorMap mapDd56;  // trait digits in 56-row boxes (2-SM quadratic Gram, one-digit slot pairs)
   QuadPasses qp;
   double* Linv = nullptr;       // chol: n x n, L^-1
   double* LinvT = nullptr;      // chol: n x n, (L^-1)^T (rows of L^-1 contiguous)
@@ -1908,6 +2172,9 @@ cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_
     if (r == cudaSuccess) chk(cudaMemset(p->dexp, 0, sizeof(int) * p->tgp));
     if (r == cudaSuccess) chk(make_map_u8(&p->mapAd, p->Adig, p->Kq, (long long)p->SQ * p->Ncap, BM));
     if (r == cudaSuccess) chk(make_map_u8(&p->mapDd, p->Ddig, p->Kq, (long long)p->SQ * p->tgp, QT_TP));
+    if (r == cudaSuccess) chk(make_map_u8(&p->mapDd56, p->Ddig, p->Kq, (long long)p->SQ * p->tgp, QT_TP / 2));
+    if (r == cudaSuccess)
+      chk(cudaFuncSetAttribute(quadtc2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, QT2_SMEM));
     if (r == cudaSuccess)
       chk(cudaFuncSetAttribute(quadtc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, QT_SMEM));
     quad_passes(p, p->SQ);
@@ -2011,21 +2278,27 @@ cudaError_t selfgram(OzakiPlan* p, cudaStream_t s, int col0, int xq, int t, doub
   g.Ncap = p->Ncap;
   g.Kq = p->Kq;
   g.groups = p->tgp / QT_TP;
-  const int tiles = (xq + BM - 1) / BM * g.groups;
-  g.units = tiles * p->qp.n;
   g.aexp = p->aexp;
   g.dexp = p->dexp;
   g.part = p->qpart;
   g.err = p->err;
   g.wait_ns = p->wait_ns;
-  // persistent CTAs, at most one per SM, each with >= half a tile's passes
-  // (so a tile spans at most QT_SLOTS CTAs)
-  const int ctas = std::max(1, std::min(p->sms, g.units / ((p->qp.n + 1) / 2)));
-  quadtc_kernel<<<ctas, THREADS, QT_SMEM, s>>>(p->mapAd, p->mapDd, p->qp, g);
+  // 2-SM: tiles of 256 SNP rows over CTA pairs; else 128 rows per CTA.
+  // Persistent CTAs (pairs), at most one per SM, each with >= half a tile's
+  // passes (so a tile spans at most QT_SLOTS of them)
+  const int clusters = pair_clusters();
+  const int rows = clusters > 0 ? 2 * BM : BM;
+  g.units = (xq + rows - 1) / rows * g.groups * p->qp.n;
+  const int cap = clusters > 0 ? clusters : p->sms;
+  const int ctas = std::max(1, std::min(cap, g.units / ((p->qp.n + 1) / 2)));
+  if (clusters > 0)
+    quadtc2_kernel<<<2 * ctas, THREADS, QT2_SMEM, s>>>(p->mapAd, p->mapDd, p->mapDd56, p->qp, g);
+  else
+    quadtc_kernel<<<ctas, THREADS, QT_SMEM, s>>>(p->mapAd, p->mapDd, p->qp, g);
   note_launch();
   const long long cells = (long long)xq * t;
   quadtc_combine_kernel<<<(int)((cells + 255) / 256), 256, 0, s>>>(xq, t, p->Ncap, p->tgp, g.groups, p->qp.n,
-                                                                    g.units, ctas, p->qpart, GR, ldg);
+                                                                    g.units, ctas, rows, p->qpart, GR, ldg);
   note_launch();
   return cudaGetLastError();
 }
