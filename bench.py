@@ -696,6 +696,7 @@ def run_cohorts(args):
               use_graph=True, genotypes_u8=True, tol=1e-10)
     setup_s = time.perf_counter() - t0
     xb, S, perr = b.params()
+    tile = b.tile()
     log(f"[bench] cohorts: data {gen_s:.1f}s, setup {setup_s:.1f}s, x_b={xb}, slices={S}, probe err {perr:.2e}")
     pool = 2
     X = [[genotype_block(xb, c["n"], c["seed"] + i, dev).to(torch.uint8) for i in range(pool)] for c in co]
@@ -813,6 +814,8 @@ def run_cohorts(args):
                                f"steps of x_b={xb} SNPs of every cohort",
                    "cohorts": C, "n": [c["n"] for c in co], "p": [c["p"] for c in co], "t": T, "m": M,
                    "x_b": xb, "slices": S, "probe_beta_err": perr, "setup_s": setup_s,
+                   "gemm_tile": f"{tile[0]}x{tile[1]}" + (" (autotuned: 256x256 on CTA pairs vs 128x256 on one SM)"
+                                                          if not args.xb_set else ""),
                    "job_s_estimate": C * M * T / value + setup_s, "buckets": buckets,
                    "stage_ms_per_step": {k: v / max(nprof, 1) for k, v in prof.items()},
                    "l2": f"inputs larger than L2: {pool} blocks per cohort, "

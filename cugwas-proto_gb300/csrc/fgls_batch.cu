@@ -26,7 +26,9 @@
 //           genotypes) is within tol/8 of the FP64 path (TRSM, skinny Gram,
 //           solve) for every problem;
 //   x_b:    the candidate SNP block (1024 .. 8192) with the highest measured
-//           tests/s on one step.
+//           tests/s on one step;
+//   tile:   at that block, the faster of the grouped GEMM's two tile shapes
+//           (256 x 256 over CTA pairs with 2-SM MMAs, 128 x 256 on one SM).
 #include <cuda_runtime.h>
 #include <stdarg.h>
 #include <stdio.h>
@@ -80,6 +82,7 @@ struct fglsgpu_batch {
   std::vector<Cohort> co;
   std::vector<Problem> pr;
   int x_b = 0, S = 0, ncap = 0;
+  bool pair_tiles = true;  // grouped GEMM tile shape: 256 x 256 over CTA pairs, else 128 x 256
   cudaStream_t s = nullptr;
   DevStatus* dst = nullptr;
   DevStatus* hst = nullptr;
@@ -214,7 +217,7 @@ int configure(fglsgpu_batch* b, int S, int x_b) {
       cudaGraphExecDestroy(b->gexec[k]);
       b->gexec[k] = nullptr;
     }
-  B_TRY(b, grouped_gemm_create(&b->gg, d.data(), (int)d.size(), x_b, b->derr), "grouped GEMM plan");
+  B_TRY(b, grouped_gemm_create(&b->gg, d.data(), (int)d.size(), x_b, b->derr, b->pair_tiles), "grouped GEMM plan");
   b->S = S;
   b->x_b = x_b;
   return FGLSGPU_OK;
@@ -702,6 +705,16 @@ int fglsgpu_batch_create(const fglsgpu_cohort* cohorts, int count, const fglsgpu
         xb = cand;
       }
     }
+    // the other tile shape at the chosen block
+    b->pair_tiles = false;
+    double r1 = 0.0;
+    rc = time_step(b, xb, &r1);
+    if (rc) {
+      tl_err = b->err;
+      return bail(rc);
+    }
+    b->tune_rates.push_back(r1);
+    b->pair_tiles = r1 <= best;
   }
   rc = configure(b, S, xb);
   if (rc) {
@@ -725,6 +738,13 @@ int fglsgpu_batch_destroy(fglsgpu_batch* b) {
   if (b->s) cudaStreamSynchronize(b->s);
   free_batch(b);
   delete b;
+  return FGLSGPU_OK;
+}
+
+int fglsgpu_batch_tile(const fglsgpu_batch* b, int* rows, int* cols) {
+  if (!b) return bfail(nullptr, FGLSGPU_EINVAL, "null batch");
+  if (rows) *rows = grouped_gemm_tile_rows(b->gg);
+  if (cols) *cols = 256;
   return FGLSGPU_OK;
 }
 

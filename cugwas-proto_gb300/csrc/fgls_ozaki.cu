@@ -2503,9 +2503,10 @@ struct GroupedGemm {
   int* counter = nullptr;  // tile counter and finished CTAs of the persistent launch
 };
 
-cudaError_t grouped_gemm_create(GroupedGemm** out, const GroupedGemmDesc* d, int count, int x_b, int* err) {
+cudaError_t grouped_gemm_create(GroupedGemm** out, const GroupedGemmDesc* d, int count, int x_b, int* err,
+                                bool want_pair) {
   *out = nullptr;
-  const bool pair = pair_clusters() > 0;
+  const bool pair = want_pair && pair_clusters() > 0;
   std::vector<GroupedProblem> probs(count);
   std::vector<CUtensorMap> maps(2 * (size_t)count);
   std::vector<int> order(count);
@@ -2595,6 +2596,8 @@ cudaError_t grouped_gemm_run(GroupedGemm* gg, cudaStream_t s, const int* dcols) 
 }
 
 int grouped_gemm_tiles(const GroupedGemm* gg) { return gg ? gg->ntiles : 0; }
+
+int grouped_gemm_tile_rows(const GroupedGemm* gg) { return gg && gg->pair ? 2 * BM : BM; }
 
 void grouped_gemm_destroy(GroupedGemm* gg) {
   if (!gg) return;

@@ -92,7 +92,12 @@ struct GroupedGemmDesc {
 struct GroupedGemm;
 // One launch over all problems' tiles (x_b columns each at most); the
 // columns of a launch come from dcols[cohort] (device ints).
-cudaError_t grouped_gemm_create(GroupedGemm** out, const GroupedGemmDesc* d, int count, int x_b, int* err);
+// pair: 256 x 256 tiles over CTA pairs (2-SM MMAs, when the device launches
+// clusters of two), else 128 x 256 tiles on one SM each
+cudaError_t grouped_gemm_create(GroupedGemm** out, const GroupedGemmDesc* d, int count, int x_b, int* err,
+                                bool pair);
+// output tile rows of a grouped plan (256: CTA pairs, 128: one SM)
+int grouped_gemm_tile_rows(const GroupedGemm* gg);
 cudaError_t grouped_gemm_run(GroupedGemm* gg, cudaStream_t s, const int* dcols);
 int grouped_gemm_tiles(const GroupedGemm* gg);
 void grouped_gemm_destroy(GroupedGemm* gg);

@@ -43,7 +43,7 @@ EXPORTS = (
     "fglsgpu_batch_sync", "fglsgpu_batch_stream", "fglsgpu_batch_last_error", "fglsgpu_batch_profile",
     "fglsgpu_batch_profile_read", "fglsgpu_run_block_device_packed", "fglsgpu_run_snps_compact",
     "fglsgpu_reml_fit", "fglsgpu_set_hsigma", "fglsgpu_set_wait_limit", "fglsgpu_run_snps_u8",
-    "fglsgpu_run_snps_packed", "fglsgpu_split_params", "fglsgpu_quad_digits",
+    "fglsgpu_run_snps_packed", "fglsgpu_split_params", "fglsgpu_quad_digits", "fglsgpu_batch_tile",
 )
 PROF_CLASSES = ("genotypes", "split_gemm", "selfgram", "solve", "fp64_gemm", "trsm", "gram", "spare")
 
@@ -121,6 +121,7 @@ def lib():
     L.fglsgpu_batch_create.argtypes = [C.POINTER(CohortDesc), I, C.POINTER(BatchConfig), C.POINTER(P)]
     L.fglsgpu_batch_destroy.argtypes = [P]
     L.fglsgpu_batch_params.argtypes = [P, C.POINTER(I), C.POINTER(I), C.POINTER(C.c_double)]
+    L.fglsgpu_batch_tile.argtypes = [P, C.POINTER(I), C.POINTER(I)]
     L.fglsgpu_batch_step.argtypes = [P, P, P, P, P, P]
     L.fglsgpu_batch_sync.argtypes = [P]
     L.fglsgpu_batch_stream.argtypes = [P]
@@ -372,6 +373,12 @@ class Batch:
         xb, S, e = C.c_int(), C.c_int(), C.c_double()
         self._check(self.L.fglsgpu_batch_params(self._h, C.byref(xb), C.byref(S), C.byref(e)))
         return xb.value, S.value, e.value
+
+    def tile(self):
+        """(rows, cols) of the grouped split GEMM's output tile."""
+        r, c = C.c_int(), C.c_int()
+        self._check(self.L.fglsgpu_batch_tile(self._h, C.byref(r), C.byref(c)))
+        return r.value, c.value
 
     def step(self, x_ptrs, xs, b_ptrs, v_ptrs, snp_base=None):
         k = len(self.dims)

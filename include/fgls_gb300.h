@@ -353,6 +353,11 @@ int fglsgpu_batch_destroy(fglsgpu_batch *b);
 /* The tuned (or given) SNP block and slice count, and the probe error of
  * the slice choice (-1 when slices were given). */
 int fglsgpu_batch_params(const fglsgpu_batch *b, int *x_b, int *slices, double *probe_err);
+
+/* The grouped split GEMM's output tile: 256 x 256 (two SMs per tile,
+ * tcgen05.mma.cta_group::2) or 128 x 256 (one SM).  With x_b = 0 the
+ * autotuner times both at its chosen block and keeps the faster; else 256. */
+int fglsgpu_batch_tile(const fglsgpu_batch *b, int *rows, int *cols);
 /* One step (asynchronous; fglsgpu_batch_sync reports device failures).  Per
  * cohort c: dX[c] = device genotype block of x[c] <= x_b SNPs (SNP i at
  * dX[c] + i*n_c, bytes or doubles per the config; x[c] = 0 skips the

@@ -107,5 +107,6 @@ def test_batch_autotuner_meets_tolerance():
         x_b, S, perr = b.params()
         assert x_b in (1024, 2048, 4096, 8192) and 5 <= S <= 9
         assert 0.0 <= perr <= 1e-10 / 8
+        assert b.tile() in ((256, 256), (128, 256))  # the faster grouped GEMM tile at x_b
         out = run_batch(b, pbs, x_b)
     check(pbs, out)
