@@ -480,8 +480,10 @@ int fglsgpu_batch_create(const fglsgpu_cohort* cohorts, int count, const fglsgpu
                          fglsgpu_batch** out) {
   if (!cohorts || !cfg || !out || count <= 0) return bfail(nullptr, FGLSGPU_EINVAL, "invalid batch arguments");
   *out = nullptr;
-  if (cfg->x_b < 0 || cfg->x_b > 65536 || cfg->slices < 0 || cfg->slices > S_BUILT)
-    return bfail(nullptr, FGLSGPU_EINVAL, "invalid batch config x_b=%d slices=%d", cfg->x_b, cfg->slices);
+  if (cfg->x_b < 0 || cfg->x_b > 65536 || cfg->slices < 0 || cfg->slices > S_BUILT ||
+      (cfg->tile_rows != 0 && cfg->tile_rows != 128 && cfg->tile_rows != 256))
+    return bfail(nullptr, FGLSGPU_EINVAL, "invalid batch config x_b=%d slices=%d tile_rows=%d", cfg->x_b,
+                 cfg->slices, cfg->tile_rows);
   for (int c = 0; c < count; c++) {
     const fglsgpu_cohort& k = cohorts[c];
     if (k.n < 2 || k.n > 16368 || k.wXL < 1 || k.wXL + 1 > FGLS_MAX_P || k.t < 1 || !k.Phi || !k.XL || !k.Y || !k.h ||
@@ -494,6 +496,7 @@ int fglsgpu_batch_create(const fglsgpu_cohort* cohorts, int count, const fglsgpu
   if (cudaSetDevice(cfg->device) != cudaSuccess) return bfail(nullptr, FGLSGPU_ENODEV, "cudaSetDevice failed");
   fglsgpu_batch* b = new fglsgpu_batch();
   b->cfg = *cfg;
+  b->pair_tiles = cfg->tile_rows != 128;  // given, or the default before autotuning
   if (b->cfg.tol <= 0.0) b->cfg.tol = 1e-10;
   const int xb_alloc = cfg->x_b > 0 ? cfg->x_b : XB_MAX;
   auto bail = [&](int rc) {
@@ -705,16 +708,18 @@ int fglsgpu_batch_create(const fglsgpu_cohort* cohorts, int count, const fglsgpu
         xb = cand;
       }
     }
-    // the other tile shape at the chosen block
-    b->pair_tiles = false;
-    double r1 = 0.0;
-    rc = time_step(b, xb, &r1);
-    if (rc) {
-      tl_err = b->err;
-      return bail(rc);
+    if (cfg->tile_rows == 0) {
+      // the other tile shape at the chosen block
+      b->pair_tiles = false;
+      double r1 = 0.0;
+      rc = time_step(b, xb, &r1);
+      if (rc) {
+        tl_err = b->err;
+        return bail(rc);
+      }
+      b->tune_rates.push_back(r1);
+      b->pair_tiles = r1 <= best;
     }
-    b->tune_rates.push_back(r1);
-    b->pair_tiles = r1 <= best;
   }
   rc = configure(b, S, xb);
   if (rc) {

@@ -65,7 +65,7 @@ class CohortDesc(C.Structure):
 
 
 class BatchConfig(C.Structure):
-    _fields_ = [(f, C.c_int) for f in ("x_b", "slices", "device", "use_graph", "genotypes_u8", "reserved")] + \
+    _fields_ = [(f, C.c_int) for f in ("x_b", "slices", "device", "use_graph", "genotypes_u8", "tile_rows")] + \
                [("tol", C.c_double)]
 
 
@@ -340,7 +340,7 @@ class Batch:
     ``cohorts``: list of dicts with Phi (n x n), XL (n x wXL), Y (n x t), h, sigma
     (numpy, natural orientation).  ``step`` takes per-cohort device pointers."""
 
-    def __init__(self, cohorts, x_b=0, slices=0, device=0, use_graph=True, genotypes_u8=True, tol=0.0):
+    def __init__(self, cohorts, x_b=0, slices=0, device=0, use_graph=True, genotypes_u8=True, tol=0.0, tile_rows=0):
         self.L = lib()
         self._keep = []
         descs = (CohortDesc * len(cohorts))()
@@ -357,7 +357,7 @@ class Batch:
                                   s.ctypes.data)
             self.dims.append((n, wXL + 1, t))
         self.cfg = BatchConfig(int(x_b), int(slices), int(device), int(bool(use_graph)), int(bool(genotypes_u8)),
-                               0, float(tol))
+                               int(tile_rows), float(tol))
         h = C.c_void_p()
         rc = self.L.fglsgpu_batch_create(descs, len(cohorts), C.byref(self.cfg), C.byref(h))
         self._keep = None

@@ -343,7 +343,8 @@ typedef struct {
   int device;       /* CUDA device ordinal                                */
   int use_graph;    /* 1: replay each step from a captured CUDA graph     */
   int genotypes_u8; /* 1: genotype blocks are bytes, 0: FP64              */
-  int reserved;
+  int tile_rows;    /* grouped GEMM tile rows: 256 (CTA pairs), 128 (one  */
+                    /* SM); 0: autotuned with x_b = 0, else 256            */
   double tol;       /* autotune target for beta vs FP64 (0: 1e-10)        */
 } fglsgpu_batch_config;
 

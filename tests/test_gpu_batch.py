@@ -92,6 +92,24 @@ def test_batch_graph_replay_is_bit_identical_and_idle_cohorts():
         assert np.array_equal(B1, B2) and np.array_equal(V1, V2)
 
 
+def test_batch_tile_shapes_are_bit_identical():
+    """The grouped split GEMM on 256 x 256 tiles over CTA pairs (2-SM MMAs,
+    row-tile pairs from the launch-wide counter, odd row-tile counts leaving a
+    phantom second tile) and on 128 x 256 tiles on one SM: every partial sum
+    is an exact integer, so the results agree to the bit, and both match the
+    oracle."""
+    from fgls_gb300 import Batch
+    pbs, desc = cohorts(seed=70)
+    outs = []
+    for rows in (256, 128):
+        with Batch(desc, x_b=256, slices=9, use_graph=True, tile_rows=rows) as b:
+            assert b.tile() == (rows, 256)
+            outs.append(run_batch(b, pbs, 256))
+    for (B1, V1), (B2, V2) in zip(*outs):
+        assert np.array_equal(B1, B2) and np.array_equal(V1, V2)
+    check(pbs, outs[0])
+
+
 def test_batch_fp64_genotype_input():
     from fgls_gb300 import Batch
     pbs, desc = cohorts(COHORTS[1:3], seed=60)
