@@ -12,14 +12,16 @@
 //   1. grouped_genotypes: every cohort's block -> its E4M3 operand
 //   2. ozaki_grouped_gemm_kernel: one persistent launch (a CTA per SM) over
 //      the tiles of all problems, listed longest first and taken from a
-//      launch-wide counter -> X~ = L^-1 X (R^2 as float pairs) and the Gram
-//      rows x~'y~, x~'XL~
-//   3. unit_gram_grouped: x~'x~ per (problem, SNP) in double-FP32
+//      launch-wide counter -> X~ = L^-1 X, summed as R^2 over 32-row groups
+//      in the last pass (X~ itself is not written), and the Gram rows
+//      x~'y~, x~'XL~
+//   3. unit_gram_grouped: x~'x~ per (problem, SNP), the group sums added in
+//      double-FP32
 //   4. snp_solve_grouped<p>: per distinct p, the p x p solves of all problems
 // The per-step inputs (genotype pointer, SNP count, output pointers of each
 // cohort) are one small table copied from pinned host memory at the start of
 // the step, so the whole step is captured once as a CUDA graph and replayed
-// (two graphs alternate between two pinned tables).
+// (a ring of NSLOT graphs, one per pinned table).
 //
 // Autotuning at creation (fglsgpu_batch_config x_b = 0 and/or slices = 0):
 //   slices: the smallest S in 5..9 whose beta on a probe block (hashed
@@ -55,6 +57,11 @@ constexpr int S_BUILT = 9;     // FP8 five-bit digit slices cut at setup; fewer 
 constexpr int S_MIN_TUNE = 5;  // smallest slice count the autotuner tries
 constexpr int PROBE = 256;     // SNPs of the autotuning probe block
 constexpr int XB_MAX = 8192;   // largest autotuned SNP block
+// Pinned step tables (and step graphs) in the ring: the host fills table k
+// once the step that last used it has finished, so it may run NSLOT - 1
+// steps ahead of the device and a host-side stall of that length costs no
+// device time.
+constexpr int NSLOT = 8;
 
 struct Cohort {
   int n = 0, wXL = 0, p = 0, t = 0;
@@ -71,6 +78,7 @@ struct Problem {
   double* scale = nullptr;     // row scales for the slices in use
   double* top = nullptr;       // null model (wXL + wXL^2 + 1)
   double* C = nullptr;         // Mpad x Ncap split GEMM output
+  float2* Q = nullptr;         // Mpad/32 x Ncap sums of R^2 over 32-row groups (ld Ncap)
   double* GR = nullptr;        // Ncap
   double* ref = nullptr;       // PROBE x p FP64-path beta on the probe block
 };
@@ -94,12 +102,12 @@ struct fglsgpu_batch {
   int pcount[FGLS_MAX_P + 1] = {0}, poff[FGLS_MAX_P + 1] = {0};
   // per-step table: StepCohort[C] followed by int x[C]
   size_t step_bytes = 0;
-  void* hstep[2] = {nullptr, nullptr};
+  void* hstep[NSLOT] = {};
   void* dstep = nullptr;
-  cudaEvent_t slot_done[2] = {nullptr, nullptr};
+  cudaEvent_t slot_done[NSLOT] = {};
   int slot = 0;
   GroupedGemm* gg = nullptr;
-  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+  cudaGraphExec_t gexec[NSLOT] = {};
   long long graph_launches = 0;  // kernels per replayed step
   double tune_err = -1.0;
   std::vector<double> tune_rates;
@@ -181,14 +189,14 @@ void free_batch(fglsgpu_batch* b) {
     if (c.probe) cudaFree(c.probe);
   }
   for (auto& q : b->pr) {
-    void* ptrs[] = {q.A, q.scale_built, q.scale, q.top, q.C, q.GR, q.ref};
+    void* ptrs[] = {q.A, q.scale_built, q.scale, q.top, q.C, q.Q, q.GR, q.ref};
     for (void* v : ptrs)
       if (v) cudaFree(v);
   }
   void* ptrs[] = {b->dst, b->derr, b->dgeno, b->dunit, b->dsolve, b->dplist, b->dstep};
   for (void* v : ptrs)
     if (v) cudaFree(v);
-  for (int k = 0; k < 2; k++) {
+  for (int k = 0; k < NSLOT; k++) {
     if (b->hstep[k]) cudaFreeHost(b->hstep[k]);
     if (b->slot_done[k]) cudaEventDestroy(b->slot_done[k]);
     if (b->gexec[k]) cudaGraphExecDestroy(b->gexec[k]);
@@ -207,12 +215,13 @@ int configure(fglsgpu_batch* b, int S, int x_b) {
     Problem& q = b->pr[k];
     const Cohort& c = b->co[q.c];
     B_TRY(b, split_rescale_rows(b->s, q.Mpad, q.scale_built, S_BUILT, S, q.scale), "row scales");
-    d[k] = GroupedGemmDesc{q.A, S, S_BUILT, q.M, q.Mpad, c.Kpad, c.n, c.n, q.scale, c.G, c.Ncap, q.C, q.c};
+    d[k] = GroupedGemmDesc{q.A, S, S_BUILT, q.M, q.Mpad, c.Kpad, c.n, c.n, q.scale, c.G, c.Ncap, q.C, q.Q,
+                           b->ncap, q.c};
   }
   B_TRY(b, cudaStreamSynchronize(b->s), "row scales");
   if (b->gg) grouped_gemm_destroy(b->gg);
   b->gg = nullptr;
-  for (int k = 0; k < 2; k++)
+  for (int k = 0; k < NSLOT; k++)
     if (b->gexec[k]) {
       cudaGraphExecDestroy(b->gexec[k]);
       b->gexec[k] = nullptr;
@@ -243,7 +252,7 @@ cudaError_t enqueue_step(fglsgpu_batch* b, cudaStream_t s, const void* host_tabl
 }
 
 int capture_graphs(fglsgpu_batch* b) {
-  for (int k = 0; k < 2; k++) {
+  for (int k = 0; k < NSLOT; k++) {
     cudaGraph_t g = nullptr;
     const long long l0 = g_launches.load();
     B_TRY(b, cudaStreamBeginCapture(b->s, cudaStreamCaptureModeThreadLocal), "graph capture");
@@ -290,7 +299,7 @@ int launch_step(fglsgpu_batch* b, const void* const* dX, const int* x, double* c
     B_TRY(b, enqueue_step(b, b->s, b->hstep[k]), "step");
   }
   B_TRY(b, cudaEventRecord(b->slot_done[k], b->s), "step slot");
-  b->slot ^= 1;
+  b->slot = (b->slot + 1) % NSLOT;
   return FGLSGPU_OK;
 }
 
@@ -525,7 +534,8 @@ int fglsgpu_batch_create(const fglsgpu_cohort* cohorts, int count, const fglsgpu
   B_CHECK(cudaMemset(b->dst, 0, sizeof(DevStatus)), "status");
   B_CHECK(cudaMemset(b->derr, 0, sizeof(int)), "status");
   B_CHECK(cudaMallocHost(&b->hst, sizeof(DevStatus)), "status");
-  for (int k = 0; k < 2; k++) B_CHECK(cudaEventCreateWithFlags(&b->slot_done[k], cudaEventDisableTiming), "events");
+  for (int k = 0; k < NSLOT; k++)
+    B_CHECK(cudaEventCreateWithFlags(&b->slot_done[k], cudaEventDisableTiming), "events");
   b->ncap = split_cols_padded(std::max(xb_alloc, PROBE));
   int nmax = 0, wmax = 0;
   b->co.resize(count);
@@ -560,6 +570,7 @@ int fglsgpu_batch_create(const fglsgpu_cohort* cohorts, int count, const fglsgpu
     B_CHECK(dalloc(&q.scale, q.Mpad), "row scales");
     B_CHECK(dalloc(&q.top, k.wXL + k.wXL * k.wXL + 1), "null model");
     B_CHECK(dalloc(&q.C, (size_t)q.Mpad * b->ncap), "split GEMM output");
+    B_CHECK(dalloc(&q.Q, (size_t)(q.Mpad / 32) * b->ncap), "split GEMM group sums");
     B_CHECK(dalloc(&q.GR, b->ncap), "Gram");
     B_CHECK(dalloc(&q.ref, (size_t)PROBE * k.p), "probe reference");
   }
@@ -651,7 +662,7 @@ int fglsgpu_batch_create(const fglsgpu_cohort* cohorts, int count, const fglsgpu
     for (int k = 0; k < P; k++) {
       const Problem& q = b->pr[k];
       const Cohort& c = b->co[q.c];
-      unit[k] = UnitGramProblem{(const float2*)q.C, q.Mpad, q.GR, c.n, q.c};
+      unit[k] = UnitGramProblem{q.Q, b->ncap, q.GR, c.n, q.c};
       solve[k] = SolveProblem{q.top, q.C + c.n, q.Mpad, q.GR, q.c, q.j};
     }
     B_CHECK(dalloc(&b->dgeno, C), "tables");
@@ -664,7 +675,7 @@ int fglsgpu_batch_create(const fglsgpu_cohort* cohorts, int count, const fglsgpu
     B_CHECK(cudaMemcpy(b->dplist, plist.data(), sizeof(int) * plist.size(), cudaMemcpyHostToDevice), "tables");
     b->step_bytes = (sizeof(StepCohort) + sizeof(int)) * C;
     B_CHECK(cudaMalloc(&b->dstep, b->step_bytes), "step table");
-    for (int k = 0; k < 2; k++) {
+    for (int k = 0; k < NSLOT; k++) {
       B_CHECK(cudaMallocHost(&b->hstep[k], b->step_bytes), "step table");
       memset(b->hstep[k], 0, b->step_bytes);
       B_CHECK(cudaEventRecord(b->slot_done[k], b->s), "events");

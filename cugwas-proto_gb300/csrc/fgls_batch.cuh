@@ -24,8 +24,8 @@ struct GenoCohort {
 
 // Per (cohort, trait) problem, fixed.
 struct UnitGramProblem {
-  const float2* A;  // R^2 pairs, column i at A + i*lda, rows [0, n)
-  long long lda;
+  const float2* Q;  // sums of R^2 over 32-row groups: SNP i, group g at Q[i + g*ldq]
+  long long ldq;
   double* GR;       // x_b results
   int n, cohort;
 };

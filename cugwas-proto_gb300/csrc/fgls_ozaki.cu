@@ -47,7 +47,10 @@
 //          digits of R^2 and d_j (quadtc_kernel below, 33 <= t), else in
 //          double-FP32 (error-free products and sums) on the CUDA cores:
 //          quad_gram (fgls_selfgram.cu).
-//   chol:  A = [L^-1 ; U^T], U = L^-T [y~ | XL~].
+//   chol:  A = [L^-1 ; U^T], U = L^-T [y~ | XL~].  The quadratic term has
+//          unit weights, |x~|^2 = sum_l R_l^2: the GEMM's last pass sums the
+//          squares over each 32-row group in registers (no R^2 is written)
+//          and sqsum_combine (fgls_selfgram.cu) adds the groups.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_fp8.h>
@@ -291,6 +294,11 @@ struct GemmArgs {
   int sq_rows;      // rows [0, sq_rows): write (C^2) as an error-free float pair (hi, lo)
   int* err;         // first failing wait site (0 = ok)
   unsigned long long wait_ns;  // limit of one pipeline wait
+  // Unit weights (chol variant): when set, rows [0, sq_rows) write no
+  // squares; the last pass sums (C^2) over each 32-row group g instead, as a
+  // float pair at sqsum[c + g * ldq] for output column c.
+  float2* sqsum = nullptr;
+  long long ldq = 0;
 };
 
 // Grouped launches: one problem per (cohort, trait), tiles listed by the host.
@@ -424,14 +432,57 @@ struct GroupedTiles {
   }
 };
 
+// Sum of two float pairs of non-negative values: TwoSum of the high parts,
+// the rounding error and both low parts into the low part.  No
+// renormalisation: over the five rounds below the low part stays below
+// ~2^-20 of the high part, so its own rounding costs ~2^-44 relative, and
+// the combine kernel renormalises.
+__device__ __forceinline__ void pair_add(float ah, float al, float bh, float bl, float& h, float& l) {
+  float e;
+  two_sum_g(ah, bh, h, e);
+  l = __fadd_rn(e, __fadd_rn(al, bl));
+}
+
+// Column sums over a warp's 32 rows.  Five exchange-and-add rounds with
+// lane offsets 16, 8, 4, 2, 1, each lane keeping the half of its columns
+// named by its lane bit, leave the sum of column `lane` with that lane; the
+// order of the additions is fixed.  The caller runs the first round (offset
+// 16, 32 -> 16 columns) as it forms the values; this runs the other four on
+// lane k's 16 partial sums (h[c], l[c]), leaving column `lane` in (h[0], l[0]).
+__device__ __forceinline__ void warp_column_sums(float (&h)[16], float (&l)[16], int lane) {
+#pragma unroll
+  for (int o = 8; o >= 1; o >>= 1) {
+    const bool up = (lane & o) != 0;
+#pragma unroll
+    for (int k = 0; k < o; k++) {
+      const float sh = up ? h[k] : h[k + o], sl = up ? l[k] : l[k + o];
+      const float kh = up ? h[k + o] : h[k], kl = up ? l[k + o] : l[k];
+      const float rh = __shfl_xor_sync(0xffffffffu, sh, o), rl = __shfl_xor_sync(0xffffffffu, sl, o);
+      pair_add(kh, kl, rh, rl, h[k], l[k]);
+    }
+  }
+}
+
 // One pass of the split GEMM's epilogue for one thread (one output row,
 // `cend` columns of its half tile from `crow`, stride ldc): read the pass's
 // accumulator (P_2p + P_2p+1 / 32) from TMEM at `tacc` 32 columns at a time,
 // form the exact int32 q = 32 v = P_2p * 32 + P_2p+1, and fold it into the
 // int64 partial sums in C (V = V * 2^10 + q), or on the last pass write V
 // times the row scale (FP64, or squared as a float pair for rows `sq`).
+// With `qrow` set (warp-uniform: the warp's 32-row group holds rows `sq` of a
+// unit-weight problem) the last pass writes no squares: the warp sums them
+// over its rows and lane k writes column c0 + k's sum to qrow[c0 + k] for
+// the `qend` valid columns of the half tile; rows not `sq` still write FP64.
 __device__ __forceinline__ void epilogue_pass(uint32_t tacc, int p, bool last, bool sq, double scale, float fscale,
-                                              long long* crow, long long ldc, int cend) {
+                                              long long* crow, long long ldc, int cend, float2* qrow, int qend) {
+  const int lane = threadIdx.x & 31;
+  // The int64 partial sums live from one pass to the next (~50 us, while the
+  // other CTAs stream ~0.5 GB of operand tiles through L2): stored with
+  // evict-last priority and read back, their last use, with evict-first, so
+  // that they stay in L2 instead of making a DRAM round trip.
+  uint64_t pol_keep, pol_drop;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol_keep));
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol_drop));
 #pragma unroll 1
   for (int ch = 0; ch < BN / 64; ch++) {
     const int c0 = ch * 32;
@@ -439,11 +490,41 @@ __device__ __forceinline__ void epilogue_pass(uint32_t tacc, int p, bool last, b
     if (p > 0) {
       // all 32 partial sums in flight at once, before the TMEM reads
 #pragma unroll
-      for (int j = 0; j < 32; j++) prev[j] = (c0 + j < cend) ? __ldcg(crow + (long long)(c0 + j) * ldc) : 0;
+      for (int j = 0; j < 32; j++) {
+        long long t = 0;
+        if (c0 + j < cend)
+          asm volatile("ld.global.cg.L2::cache_hint.b64 %0, [%1], %2;"
+                       : "=l"(t)
+                       : "l"(crow + (long long)(c0 + j) * ldc), "l"(pol_drop));
+        prev[j] = t;
+      }
     }
     uint32_t v[32];
     tmem_ld32(tacc + c0, v);
     tmem_ld_wait();
+    if (last && qrow != nullptr) {
+      // column j's square as a float pair (0 past cend; rows not sq write FP64)
+      auto term = [&](int j) -> float2 {
+        if (c0 + j >= cend) return make_float2(0.0f, 0.0f);
+        const int qv = fused_pair_f2i(__uint_as_float(v[j]));
+        const long long V = (p == 0) ? (long long)qv : prev[j] * 1024ll + (long long)qv;
+        if (sq) return square_pair(V, fscale);
+        *(double*)(crow + (long long)(c0 + j) * ldc) = (double)V * scale;
+        return make_float2(0.0f, 0.0f);
+      };
+      float h[16], l[16];
+      const bool up = (lane & 16) != 0;
+#pragma unroll
+      for (int k = 0; k < 16; k++) {  // the offset-16 round: columns k and k + 16
+        const float2 a = term(k), b = term(k + 16);
+        const float2 send = up ? a : b, keep = up ? b : a;
+        const float rh = __shfl_xor_sync(0xffffffffu, send.x, 16), rl = __shfl_xor_sync(0xffffffffu, send.y, 16);
+        pair_add(keep.x, keep.y, rh, rl, h[k], l[k]);
+      }
+      warp_column_sums(h, l, lane);
+      if (c0 + lane < qend) qrow[c0 + lane] = make_float2(h[0], l[0]);
+      continue;
+    }
 #pragma unroll
     for (int j = 0; j < 32; j++) {
       if (c0 + j >= cend) break;
@@ -451,7 +532,7 @@ __device__ __forceinline__ void epilogue_pass(uint32_t tacc, int p, bool last, b
       long long* cp = crow + (long long)(c0 + j) * ldc;
       const long long V = (p == 0) ? (long long)qv : prev[j] * 1024ll + (long long)qv;
       if (!last)
-        *cp = V;
+        asm volatile("st.global.L2::cache_hint.b64 [%0], %1, %2;" ::"l"(cp), "l"(V), "l"(pol_keep) : "memory");
       else if (sq)
         *(float2*)cp = square_pair(V, fscale);
       else
@@ -699,14 +780,22 @@ __device__ __forceinline__ void gemm_persistent(const Src& src, int* tile_counte
       const int ncols = rvalid ? min(BN, T.N - n0) : 0;  // valid columns of this tile for this row
       const int cend = min(BN / 2, ncols - cbeg);        // of this thread's half (may be <= 0)
       long long* crow = (long long*)(g.C + (long long)r + (long long)(g.col0 + n0 + cbeg) * g.ldc);
+      // unit weights: this warp's 32-row group (rows r & ~31 ..) sums its squares
+      float2* qrow = (g.sqsum != nullptr && (r & ~31) < g.sq_rows)
+                         ? g.sqsum + (long long)(r >> 5) * g.ldq + (g.col0 + n0 + cbeg)
+                         : nullptr;
+      const int qend = min(BN / 2, min(BN, T.N - n0) - cbeg);
       const int passes = (g.S + 1) / 2;
 #pragma unroll 1
       for (int p = 0; p < passes; p++, q++) {
         const bool last = p == passes - 1;
         const uint32_t buf = q & 1, par = (q >> 1) & 1;
-        // pull this row's partial sums (written a pass ago, since evicted by
-        // the operand stream) back into L2 while the pass's MMAs run
-        if (p > 0)
+        // pull this row's partial sums (written a pass ago) back into L2
+        // while the pass's MMAs run, if the evict-last policy did not keep
+        // them.  Only for uniform long-K tiles: with the short passes of the
+        // triangular and grouped operands the instructions cost more than
+        // they save (grouped cohorts: 29.5 against 27.9 ms per launch).
+        if (p > 0 && !src.dynamic())
           for (int c = 0; c < cend; c++)
             asm volatile("prefetch.global.L2 [%0];" ::"l"(crow + (long long)c * g.ldc));
         int okw = 1;
@@ -714,7 +803,7 @@ __device__ __forceinline__ void gemm_persistent(const Src& src, int* tile_counte
         okw = __shfl_sync(0xffffffffu, okw, 0);  // warp-uniform: tcgen05.ld is .sync.aligned
         if (!okw) { ok = false; break; }
         tc_fence_after();
-        epilogue_pass(ta + 256 * buf, p, last, sq, scale, fscale, crow, g.ldc, cend);
+        epilogue_pass(ta + 256 * buf, p, last, sq, scale, fscale, crow, g.ldc, cend, qrow, qend);
         tc_fence_before();
         mbar_arrive(&tempty[buf]);
       }
@@ -1061,12 +1150,17 @@ __device__ __forceinline__ void gemm_pair(const Src& src, int* tile_counter) {
       const int ncols = rvalid ? min(BN, T.N - n0) : 0;
       const int cend = min(BN / 2, ncols - cbeg);
       long long* crow = (long long*)(g.C + (long long)r + (long long)(g.col0 + n0 + cbeg) * g.ldc);
+      // unit weights: this warp's 32-row group (rows r & ~31 ..) sums its squares
+      float2* qrow = (g.sqsum != nullptr && (r & ~31) < g.sq_rows)
+                         ? g.sqsum + (long long)(r >> 5) * g.ldq + (g.col0 + n0 + cbeg)
+                         : nullptr;
+      const int qend = min(BN / 2, min(BN, T.N - n0) - cbeg);
       const int passes = (g.S + 1) / 2;
 #pragma unroll 1
       for (int p = 0; p < passes; p++, q++) {
         const bool last = p == passes - 1;
         const uint32_t buf = q & 1, par = (q >> 1) & 1;
-        if (p > 0)
+        if (p > 0 && !src.dynamic())  // as in the one-SM kernel
           for (int c = 0; c < cend; c++)
             asm volatile("prefetch.global.L2 [%0];" ::"l"(crow + (long long)c * g.ldc));
         int okw = 1;
@@ -1074,7 +1168,7 @@ __device__ __forceinline__ void gemm_pair(const Src& src, int* tile_counter) {
         okw = __shfl_sync(0xffffffffu, okw, 0);
         if (!okw) { ok = false; break; }
         tc_fence_after();
-        epilogue_pass(ta + 256 * buf, p, last, sq, scale, fscale, crow, g.ldc, cend);
+        epilogue_pass(ta + 256 * buf, p, last, sq, scale, fscale, crow, g.ldc, cend, qrow, qend);
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive_cluster(lead_tempty + 8u * buf);
@@ -1933,11 +2027,6 @@ __global__ void transpose_kernel(int n, const double* __restrict__ A, double* __
 // Weights of the quadratic Gram terms (fgls_selfgram.cu) as float pairs.
 // ---------------------------------------------------------------------------
 // unit weights (chol: |x~|^2)
-__global__ void unit_pairs_kernel(int n, float2* D, float* dmax) {
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) D[e] = make_float2(1.f, 0.f);
-  if (blockIdx.x == 0 && threadIdx.x == 0) dmax[0] = 1.f;
-}
-
 // D (FP64 n x t) -> interleaved float pairs, and dmax[j] = max_l hi
 __global__ void split_pairs_kernel(int n, int t, const double* __restrict__ d, float2* __restrict__ D,
                                    float* __restrict__ dmax) {
@@ -2078,6 +2167,7 @@ struct OzakiPlan {
   QuadPasses qp;
   double* Linv = nullptr;       // chol: n x n, L^-1
   double* LinvT = nullptr;      // chol: n x n, (L^-1)^T (rows of L^-1 contiguous)
+  float2* sqsum = nullptr;      // chol: Mpad/32 x Ncap sums of R^2 over 32-row groups (ld Ncap)
   int* err = nullptr;
   CUtensorMap mapA, mapB;
   CUtensorMap mapBh;                // genotypes in 128-row boxes (2-SM kernel); valid when has_mapBh
@@ -2143,6 +2233,7 @@ cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_
   chk(cudaMalloc(&p->err, 3 * sizeof(int)));  // [wait error word, GEMM tile counter, finished CTAs]
   if (!eigen) chk(cudaMalloc(&p->Linv, sizeof(double) * (size_t)n * n));
   if (!eigen) chk(cudaMalloc(&p->LinvT, sizeof(double) * (size_t)n * n));
+  if (!eigen) chk(cudaMalloc(&p->sqsum, sizeof(float2) * (size_t)(p->Mpad / 32) * p->Ncap));
   if (r == cudaSuccess) chk(cudaMemset(p->A, 0, (size_t)p->S * p->Mpad * p->Kpad));
   if (r == cudaSuccess) chk(cudaMemset(p->G, 0, (size_t)p->Ncap * p->Kpad));
   if (r == cudaSuccess) chk(cudaMemset(p->scale, 0, sizeof(double) * p->Mpad));
@@ -2194,7 +2285,8 @@ cudaError_t ozaki_create(OzakiPlan** out, int n, int t, int wXL, int wXR, int x_
 void ozaki_destroy(OzakiPlan* p) {
   if (!p) return;
   void* ptrs[] = {p->A,    p->G,     p->scale, p->scale_run, p->C, p->U, p->D,    p->dmax, p->amax,
-                  p->part, p->Linv,  p->LinvT, p->err,   p->Adig, p->Ddig, p->aexp, p->dexp, p->qpart};
+                  p->part, p->Linv,  p->LinvT, p->err,   p->Adig, p->Ddig, p->aexp, p->dexp, p->qpart,
+                  p->sqsum};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   delete p;
@@ -2234,6 +2326,9 @@ cudaError_t run_gemm(OzakiPlan* p, cudaStream_t s, int col0, int x, int tri_rows
   g.ldc = p->Mpad;
   g.err = p->err;
   g.wait_ns = p->wait_ns;
+  // chol (unit weights): the GEMM sums the squares of rows [0, n) per 32-row group
+  g.sqsum = sq_rows > 0 ? p->sqsum : nullptr;
+  g.ldq = p->Ncap;
   // the 2-SM kernel (pairs of row tiles share each genotype tile across two
   // SMs; the triangular L^-1 operand's pairs longest first from the counter),
   // else one CTA per tile
@@ -2265,6 +2360,7 @@ cudaError_t load_genotypes_packed(OzakiPlan* p, cudaStream_t s, const uint8_t* X
 }
 
 cudaError_t selfgram(OzakiPlan* p, cudaStream_t s, int col0, int xq, int t, double* GR, long long ldg) {
+  if (p->sqsum) return sqsum_combine(s, p->n, xq, p->sqsum + col0, p->Ncap, GR + col0);
   const float2* A = (const float2*)(p->C + (long long)col0 * p->Mpad);
   if (!p->tq || col0 != 0)
     return quad_gram(s, p->n, xq, t, A, p->Mpad, p->amax + col0, p->D, p->n, p->dmax, p->part, GR + col0, ldg,
@@ -2344,9 +2440,6 @@ cudaError_t ozaki_set_chol(OzakiPlan* p, cudaStream_t s, const double* L, const 
   transpose_kernel<<<tg, dim3(32, 8), 0, s>>>(n, p->Linv, p->LinvT);
   note_launch();
   FGLS_CUDA_TRY(slice_operands(p, s, p->LinvT, n, n));
-  // unit weights for the quadratic term |x~|^2
-  unit_pairs_kernel<<<grid_for(n), 256, 0, s>>>(n, p->D, p->dmax);
-  note_launch();
   return cudaGetLastError();
 }
 
@@ -2526,6 +2619,8 @@ cudaError_t grouped_gemm_create(GroupedGemm** out, const GroupedGemmDesc* d, int
     g.ldc = d[i].Mpad;
     g.col0 = 0;
     g.sq_rows = d[i].sq_rows;
+    g.sqsum = d[i].Q;
+    g.ldq = d[i].ldq;
     g.err = err;
     g.wait_ns = WAIT_NS;
     probs[i].cohort = d[i].cohort;

@@ -87,6 +87,8 @@ struct GroupedGemmDesc {
   const uint8_t* G;        // cohort E4M3 genotype operand, Ncap x Kpad
   int Ncap;
   double* C;               // Mpad x x_b output (ld Mpad)
+  float2* Q;               // rows [0, sq_rows): sums of C^2 over 32-row groups, group g of column c
+  long long ldq;           //   at Q[c + g*ldq] (no squares are written to C)
   int cohort;
 };
 struct GroupedGemm;

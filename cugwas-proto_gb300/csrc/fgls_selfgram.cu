@@ -3,11 +3,12 @@
 //   GR[i + j*ldg] = sum_l A[l,i] * D[l,j]
 //
 // A = R^2 as float pairs (hi, lo) written by the split-GEMM epilogue (SNP i
-// at column i, row l = eigen/whitened coordinate), D = d_j(l) as float pairs
-// (eigen weights 1/(a_j w_l + b_j); chol: ones).  This is the reference's
-// per-trait rescale followed by the x~^T x~ dot product (src/fgls_eigen.c:
-// 505-507 and 530-535; chol src/fgls_chol.c:404-406), evaluated for all
-// traits at once.
+// at column i, row l = eigen coordinate), D = d_j(l) as float pairs (eigen
+// weights 1/(a_j w_l + b_j)).  This is the reference's per-trait rescale
+// followed by the x~^T x~ dot product (src/fgls_eigen.c:505-507 and
+// 530-535), evaluated for all traits at once.  The chol variant's unit-weight
+// term (src/fgls_chol.c:404-406) is summed by the split GEMM itself and
+// finished by sqsum_combine / unit_gram_grouped (end of this file).
 //
 // Arithmetic.  All terms are non-negative (no cancellation).  Each product is
 // error-free (p + pe = ah*dh exactly, by fma) and its cross terms ah*dl + al*dh
@@ -268,60 +269,55 @@ int pick_ks(int n, long long units, int slots) {
   return best;
 }
 
-// Unit weights (chol: x~'x~ = sum_l R_l^2), many problems in one launch: one
-// warp per (problem, SNP column).  Lane k sums rows k, k+32, ... from the
-// power-of-two offset B_i >= max_l R_l^2 (Fast2Sum exact), folding every 64
-// of its terms into (H, Lo) by TwoSum; the 32 lane pairs are then merged by
-// TwoSum.  Relative error ~1e-14.
-__global__ void __launch_bounds__(256) unit_gram_grouped_kernel(const UnitGramProblem* __restrict__ probs,
-                                                                const StepCohort* __restrict__ sc) {
+// Unit weights (chol: x~'x~ = sum_l R_l^2).  The split GEMM's last pass
+// leaves, per SNP column i, the sums of R_l^2 over the 32-row groups
+// g < ceil(n / 32) as float pairs at Q[i + g*ldq].  A CTA of 32 x 8 threads
+// takes 32 columns: thread (c, k) adds the groups g = k, k + 8, ... of
+// column c in double-FP32 (TwoSum of the high parts, Fast2Sum
+// renormalisation), then thread (c, 0) adds the eight partial sums in k
+// order and writes FP64: a fixed order, so the result is deterministic.  All
+// terms are non-negative: relative error ~(groups / 8 + 13) * 2^-47 at most.
+// A warp reads 32 consecutive columns of one group row (coalesced).
+constexpr int GS_COLS = 32, GS_SPLIT = 8;
+
+__device__ __forceinline__ void pair_acc(float& H, float& L, float vh, float vl) {
+  float s, e;
+  two_sum(H, vh, s, e);
+  e = __fadd_rn(e, __fadd_rn(L, vl));
+  H = __fadd_rn(s, e);
+  L = __fsub_rn(e, __fsub_rn(H, s));
+}
+
+__device__ __forceinline__ void group_sums(const float2* __restrict__ Q, long long ldq, int groups, int x, int i0,
+                                           double* __restrict__ GR) {
+  __shared__ float2 part[GS_SPLIT][GS_COLS];
+  const int c = threadIdx.x, k = threadIdx.y, i = i0 + c;
+  float H = 0.0f, L = 0.0f;
+  if (i < x)
+    for (int g = k; g < groups; g += GS_SPLIT) {
+      const float2 v = Q[i + (long long)g * ldq];
+      pair_acc(H, L, v.x, v.y);
+    }
+  part[k][c] = make_float2(H, L);
+  __syncthreads();
+  if (k == 0 && i < x) {
+    for (int q = 1; q < GS_SPLIT; q++) pair_acc(H, L, part[q][c].x, part[q][c].y);
+    GR[i] = (double)H + (double)L;
+  }
+}
+
+__global__ void __launch_bounds__(GS_COLS * GS_SPLIT) sqsum_combine_kernel(int n, int x, const float2* __restrict__ Q,
+                                                                          long long ldq, double* __restrict__ GR) {
+  group_sums(Q, ldq, (n + 31) >> 5, x, blockIdx.x * GS_COLS, GR);
+}
+
+// many problems in one launch: blockIdx.y = problem, SNPs of its cohort's step
+__global__ void __launch_bounds__(GS_COLS * GS_SPLIT) unit_gram_grouped_kernel(
+    const UnitGramProblem* __restrict__ probs, const StepCohort* __restrict__ sc) {
   const UnitGramProblem pr = probs[blockIdx.y];
   const int x = sc[pr.cohort].x;
-  const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (i >= x) return;
-  const float2* a = pr.A + (long long)i * pr.lda;
-  float m = 0.0f;
-  for (int l = lane; l < pr.n; l += 32) m = fmaxf(m, a[l].x);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  const float off = m > 0.0f ? pow2_ceil(m) : 0.0f;
-  float sh = off, sl = 0.0f, H = 0.0f, Lo = 0.0f;
-  int cnt = 0;
-  for (int l = lane; l < pr.n; l += 32) {
-    const float2 v = a[l];
-    const float s2 = __fadd_rn(sh, v.x);
-    const float err = __fsub_rn(v.x, __fsub_rn(s2, sh));
-    sh = s2;
-    sl = __fadd_rn(__fadd_rn(sl, v.y), err);
-    if (++cnt == FOLD) {
-      float hs, he, h2, e1;
-      two_sum(sh, -off, hs, he);
-      two_sum(H, hs, h2, e1);
-      H = h2;
-      Lo = __fadd_rn(Lo, __fadd_rn(__fadd_rn(e1, he), sl));
-      sh = off;
-      sl = 0.0f;
-      cnt = 0;
-    }
-  }
-  {
-    float hs, he, h2, e1;
-    two_sum(sh, -off, hs, he);
-    two_sum(H, hs, h2, e1);
-    H = h2;
-    Lo = __fadd_rn(Lo, __fadd_rn(__fadd_rn(e1, he), sl));
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const float Ho = __shfl_xor_sync(0xffffffffu, H, o);
-    const float Lother = __shfl_xor_sync(0xffffffffu, Lo, o);
-    float s2, e;
-    two_sum(H, Ho, s2, e);
-    H = s2;
-    Lo = __fadd_rn(__fadd_rn(Lo, Lother), e);
-  }
-  if (lane == 0) pr.GR[i] = (double)H + (double)Lo;
+  if ((int)blockIdx.x * GS_COLS >= x) return;  // whole CTA: no thread reaches the barrier
+  group_sums(pr.Q, pr.ldq, (pr.n + 31) >> 5, x, blockIdx.x * GS_COLS, pr.GR);
 }
 
 }  // namespace
@@ -329,8 +325,15 @@ __global__ void __launch_bounds__(256) unit_gram_grouped_kernel(const UnitGramPr
 cudaError_t unit_gram_grouped(cudaStream_t s, const UnitGramProblem* dprobs, int count, const StepCohort* dsc,
                               int x_b) {
   if (count <= 0) return cudaSuccess;
-  dim3 grid((x_b + 7) / 8, count);
-  unit_gram_grouped_kernel<<<grid, 256, 0, s>>>(dprobs, dsc);
+  dim3 grid((x_b + GS_COLS - 1) / GS_COLS, count);
+  unit_gram_grouped_kernel<<<grid, dim3(GS_COLS, GS_SPLIT), 0, s>>>(dprobs, dsc);
+  note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t sqsum_combine(cudaStream_t s, int n, int x, const float2* Q, long long ldq, double* GR) {
+  if (x <= 0) return cudaSuccess;
+  sqsum_combine_kernel<<<(x + GS_COLS - 1) / GS_COLS, dim3(GS_COLS, GS_SPLIT), 0, s>>>(n, x, Q, ldq, GR);
   note_launch();
   return cudaGetLastError();
 }

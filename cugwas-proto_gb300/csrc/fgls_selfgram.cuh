@@ -14,10 +14,14 @@ cudaError_t quad_gram(cudaStream_t s, int n, int x, int t, const float2* A, long
                       int sms);
 size_t quad_gram_part_elems(int x, int t);
 
+// Unit weights (chol): GR[i] = sum over the 32-row groups g < ceil(n/32) of
+// the split GEMM's group sums of R^2, Q[i + g*ldq] (float pairs), for i < x.
+cudaError_t sqsum_combine(cudaStream_t s, int n, int x, const float2* Q, long long ldq, double* GR);
+
 struct UnitGramProblem;
 struct StepCohort;
-// x~'x~ = sum_l R_l^2 for every (problem, SNP < x of its cohort this step),
-// unit weights, one launch (grid covers x_b SNPs per problem).
+// x~'x~ = sum_l R_l^2 for every (problem, SNP < x of its cohort this step)
+// from the problem's group sums, one launch (grid covers x_b SNPs per problem).
 cudaError_t unit_gram_grouped(cudaStream_t s, const UnitGramProblem* dprobs, int count, const StepCohort* dsc,
                               int x_b);
 
