@@ -187,11 +187,11 @@ def aggregate_throughput(world, blocks_per_rank, snps_per_block, traits, seconds
 NOMINAL_FP8_TFLOPS = 4500.0
 
 
-def gemm_traffic(n, t, xb):
-    """DRAM bytes (read + write) of one split-GEMM launch of this workload, from
-    the committed ncu summary profiles/ozaki_gemm_n{n}_t{t}_xb{xb}.txt (its
-    line 'dram_bytes_per_launch: <bytes>'); None when no capture exists."""
-    f = os.path.join(ROOT, "profiles", f"ozaki_gemm_n{n}_t{t}_xb{xb}.txt")
+def gemm_traffic(name):
+    """DRAM bytes (read + write) of one split-GEMM launch of a workload, from the
+    committed ncu summary profiles/<name>.txt (its line
+    'dram_bytes_per_launch: <bytes>'); None when no capture exists."""
+    f = os.path.join(ROOT, "profiles", f"{name}.txt")
     if not os.path.exists(f):
         return None
     for line in open(f):
@@ -762,6 +762,13 @@ def run_cohorts(args):
     timed_s = ms / 1e3
     pk_key = "bf16_tflops" if timed_s < 3.0 else "bf16_tflops_sustained"
     peak = 2.0 * float(pk.get(pk_key, FALLBACK_PEAKS[pk_key]))
+    # algorithmic bytes of one grouped launch: every problem's S digit slices
+    # (triangular L^-1 plus the U rows) and every cohort's E4M3 genotypes read
+    # once; per problem the U-row outputs (FP64) and the 32-row group sums of
+    # R^2 (float pairs) written once
+    algo_bytes = sum(c["t"] * (S * (c["n"] * (c["n"] + 1) / 2 + c["p"] * c["n"])
+                               + 8 * xb * (c["p"] + (c["n"] + 31) // 32)) + xb * c["n"] for c in co)
+    traffic = gemm_traffic(f"grouped_gemm_cohorts{C}_xb{xb}") if S == 9 else None
     # end to end: host pinned genotypes -> device, step, results -> host
     Xh = [X[i][0].cpu().pin_memory() for i in range(C)]
     Bh = [torch.empty_like(d, device="cpu").pin_memory() for d in dB]
@@ -821,8 +828,11 @@ def run_cohorts(args):
                    "l2": f"inputs larger than L2: {pool} blocks per cohort, "
                          f"{pool * xb * sum(c['n'] for c in co) / 1e9:.2f} GB of genotypes cycled"},
         "roofline": {"bound": "tensor", "achieved": flops / (gemm_ms / 1e3) / 1e12, "peak": peak,
-                     "unit": "TFLOP/s", "frac": flops / (gemm_ms / 1e3) / 1e12 / peak, "traffic": None,
-                     "kernel": "ozaki_grouped_gemm_kernel (FP8 five-bit digit slices, one accumulator per pair)",
+                     "unit": "TFLOP/s", "frac": flops / (gemm_ms / 1e3) / 1e12 / peak, "traffic": traffic,
+                     "algorithmic_bytes": algo_bytes,
+                     "kernel": ("ozaki_grouped_gemm2_kernel (2-SM CTA pairs, 256 x 256 tiles)" if tile[0] == 256 else
+                                "ozaki_grouped_gemm_kernel (one SM, 128 x 256 tiles)")
+                               + ", FP8 five-bit digit slices, one accumulator per slice pair",
                      "peak_source": f"2 x {pk_kind} {pk_key} (FP8 dense rate = 2 x BF16; timed region {timed_s:.2f} s)",
                      "nominal_fp8_tflops": NOMINAL_FP8_TFLOPS,
                      "frac_of_nominal": flops / (gemm_ms / 1e3) / 1e12 / NOMINAL_FP8_TFLOPS},
@@ -995,7 +1005,7 @@ def run_eigen(args, rank, world, local, dist):
     timed_s = ms / 1e3
     pk_key = "bf16_tflops" if timed_s < 3.0 else "bf16_tflops_sustained"
     peak = 2.0 * float(pk.get(pk_key, FALLBACK_PEAKS[pk_key]))
-    traffic = gemm_traffic(n, t, xb)
+    traffic = gemm_traffic(f"ozaki_gemm_n{n}_t{t}_xb{xb}")
     Mpad, Kpad = -(-M_A // 128) * 128, -(-n // 128) * 128
     algo_bytes = S_used * Mpad * Kpad + xb * Kpad + 8 * Mpad * xb  # A slices + genotypes read, C written once
 
