@@ -185,6 +185,8 @@ def aggregate_throughput(world, blocks_per_rank, snps_per_block, traits, seconds
 # GB300's nominal dense FP8 tensor rate, for context beside the measured-peak
 # fraction (the measured denominator is twice a cuBLAS BF16 GEMM's rate).
 NOMINAL_FP8_TFLOPS = 4500.0
+# whole end-to-end calls per measurement (the median is reported)
+E2E_CALLS = 5
 
 
 def gemm_traffic(name):
@@ -1057,10 +1059,11 @@ def run_eigen(args, rank, world, local, dist):
     eng.run_snps_ptr(Xh.data_ptr(), xb, Bh.data_ptr(), Vh.data_ptr())  # warm
     if dist:
         dist.barrier()
-    # three whole calls; the median is reported (the host link is shared on
-    # these machines and single calls vary by up to ~25 %)
+    # five whole calls; the median is reported (the host memory and link are
+    # shared on these machines: single FP64-input calls, which move 134 GB/s
+    # of genotypes, have run up to 3x slower than the others of a run)
     e2e_runs = []
-    for _ in range(3):
+    for _ in range(E2E_CALLS):
         a = time.perf_counter()
         eng.run_snps_ptr(Xh.data_ptr(), E * xb, Bh.data_ptr(), Vh.data_ptr())
         e2e_runs.append(max_over_ranks(time.perf_counter() - a, dist, dev))
@@ -1074,14 +1077,15 @@ def run_eigen(args, rank, world, local, dist):
         Xpk[i * xb:(i + 1) * xb].copy_(pack_2bit_device(pool[i % len(pool)]))
     eng.run_snps_genotypes_ptr(Xpk.data_ptr(), xb, Bh.data_ptr(), Vh.data_ptr(), packed=True)  # warm
     pk_runs = []
-    for _ in range(3):
+    for _ in range(E2E_CALLS):
         a = time.perf_counter()
         eng.run_snps_genotypes_ptr(Xpk.data_ptr(), E * xb, Bh.data_ptr(), Vh.data_ptr(), packed=True)
         pk_runs.append(max_over_ranks(time.perf_counter() - a, dist, dev))
     e2e_packed = {"value": aggregate_throughput(world, E, xb, t, statistics.median(pk_runs)), "unit": UNIT,
                   "h2d_bytes_per_step": xb * ((n + 3) // 4), "d2h_bytes_per_step": t * xb * (p + p * p) * 8,
                   "api": "fglsgpu_run_snps_packed (host pinned 2-bit SNP-major .bed body -> host B/V)",
-                  "calls": [aggregate_throughput(world, E, xb, t, x) for x in pk_runs], "stat": "median of 3 calls",
+                  "calls": [aggregate_throughput(world, E, xb, t, x) for x in pk_runs],
+                  "stat": f"median of {E2E_CALLS} calls",
                   "beta_identical_to_fp64_input": bool(torch.equal(Bh, B_f64))}
     del Xh, Bh, Vh, Xpk, B_f64
 
@@ -1159,7 +1163,8 @@ def run_eigen(args, rank, world, local, dist):
         "e2e": {"value": e2e_value if gate_ok else None, "unit": UNIT, "h2d_bytes_per_step": xb * n * 8,
                 "d2h_bytes_per_step": t * xb * (p + p * p) * 8,
                 "api": "fglsgpu_run_snps (host pinned FP64 XR -> host B/V)", "blocks": E,
-                "calls": [aggregate_throughput(world, E, xb, t, x) for x in e2e_runs], "stat": "median of 3 calls",
+                "calls": [aggregate_throughput(world, E, xb, t, x) for x in e2e_runs],
+                "stat": f"median of {E2E_CALLS} calls",
                 "packed_genotypes": e2e_packed},
         "gpu_launches": launches,
         "clocks": clocks,
