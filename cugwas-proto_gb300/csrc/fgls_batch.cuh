@@ -1,6 +1,5 @@
 // Shared device-side tables of the batched-cohort path (fgls_batch.cu).
 #pragma once
-#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 

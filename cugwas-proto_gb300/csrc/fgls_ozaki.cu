@@ -52,7 +52,6 @@
 //          squares over each 32-row group in registers (no R^2 is written)
 //          and sqsum_combine (fgls_selfgram.cu) adds the groups.
 #include <cuda.h>
-#include <cuda_bf16.h>
 #include <cuda_fp8.h>
 #include <cuda_runtime.h>
 #include <stdint.h>

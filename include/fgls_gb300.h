@@ -262,9 +262,9 @@ int fglsgpu_set_wait_limit(fglsgpu_engine *e, long long ns);
 
 /* Per-kernel-class device time, measured with CUDA events recorded on the
  * engine's compute stream around each class of launches. */
-#define FGLSGPU_PROF_GENOTYPES 0  /* genotype widening / BF16 operand build     */
+#define FGLSGPU_PROF_GENOTYPES 0  /* genotype widening / E4M3 operand build     */
 #define FGLSGPU_PROF_SPLIT_GEMM 1 /* tcgen05 split-precision GEMM               */
-#define FGLSGPU_PROF_SELFGRAM 2   /* quadratic Gram terms (double-FP32)         */
+#define FGLSGPU_PROF_SELFGRAM 2   /* quadratic Gram terms (all variants)        */
 #define FGLSGPU_PROF_SOLVE 3      /* batched p x p solves + B/V emission        */
 #define FGLSGPU_PROF_FP64_GEMM 4  /* FP64 path: Z^T XR                          */
 #define FGLSGPU_PROF_TRSM 5       /* FP64 path: L^-1 XR                         */
