@@ -165,3 +165,15 @@ def test_device_packer_matches_the_host_packer():
         G = rng.integers(0, 3, size=(7, n)).astype(np.uint8)
         got = bench.pack_2bit_device(torch.from_numpy(G)).numpy()
         assert np.array_equal(got, datagen.pack_2bit(G)), n
+
+
+def test_bench_traffic_comes_from_the_committed_profiles():
+    """bench.gemm_traffic finds the DRAM bytes per launch of the default eigen
+    workload's split GEMM and of the 64-cohort grouped GEMM in the committed
+    ncu summaries, and they are the read + write sums those summaries list."""
+    import bench
+    eig = bench.gemm_traffic("ozaki_gemm_n10000_t100_xb16384")
+    coh = bench.gemm_traffic("grouped_gemm_cohorts64_xb2048")
+    assert eig is not None and abs(eig - (16.72 + 5.105) * 1e9) < 0.05e9
+    assert coh is not None and abs(coh - (35.345 + 19.33) * 1e9) < 0.05e9
+    assert bench.gemm_traffic("no_such_profile") is None
